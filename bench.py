@@ -1,0 +1,302 @@
+"""Benchmark of the GB300 brain step on the full-scale synthetic connectome.
+
+Workload (N=1): the 165,122-neuron, ~11M-edge synthetic graph, 2,000 seeded drive neurons at
+U(100, 200) Hz, dt 0.1 ms, current-based LIF; the timed window simulates 2,000 ms (20,000 brain
+steps) from rest. One bench step = 1,000 brain steps (100 ms simulated) in one persistent launch.
+
+  value : synaptic events/s (events = spikes x out-degree, delivered) over the timed window,
+          device time of the step launches (CUDA events on the launching stream), state in HBM
+  e2e   : the same metric through the C ABI with host buffers: each bench step uploads the drive
+          set from host memory, runs, and reads spike counts + the last fired list back
+  cpu_baseline : the oracle port of lif_step (1 core: the reference kernel is serial) on a
+          bounded sample of the same workload
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "fly-brain_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "synaptic events/s & sim-s/wall-s at 165k LIF; batched fwd+adjoint vs plain fwd"
+BRAIN_STEPS_PER_BENCH_STEP = 1000
+L2_FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.stop = gpu, [], threading.Event()
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def _run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 4 + k and r[4 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("FB_BENCH_BACKEND") != "gloo" else "gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def algorithmic_bytes(N, steps, spikes, events):
+    """Bytes the step must move (per brain step: 64 B of state per neuron; per delivered spike
+    20 B of row/sign/resource access; 16 B per synaptic event; 16 B per emitted spike)."""
+    return 64.0 * N * steps + 20.0 * spikes + 16.0 * events + 16.0 * spikes
+
+
+def cpu_baseline(g, idx, hz, params, sample_steps):
+    """The oracle port of lif_step on one host core over sample_steps brain steps."""
+    from oracle import oracle as O
+    O.build(ref=False)
+    ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, params, seed=1, backend="port")
+    for i, h in zip(idx.tolist(), hz.tolist()):
+        ob.setDriveOne(i, h)
+    ob.run(200)  # warm caches
+    sc0 = ob.spikeCount.astype(np.int64)
+    t0 = time.perf_counter()
+    ob.run(sample_steps)
+    dt = time.perf_counter() - t0
+    ev = float(((ob.spikeCount.astype(np.int64) - sc0) * g.outdeg()).sum())
+    return ev / dt, dt, ev
+
+
+def run_ours(args, rank, world):
+    import torch
+    from flybrain import SYNTH_PARAMS, DeviceGraph, LIFCuda, workload
+
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
+    g, idx, hz, _ = workload("full", seed=1)
+    outdeg = g.outdeg().astype(np.int64)
+    brain = LIFCuda(DeviceGraph(g), SYNTH_PARAMS, seed=1)
+    brain._batch.set_drive(0, idx, hz)
+    S = BRAIN_STEPS_PER_BENCH_STEP
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        brain.run(S)
+    brain.reset()
+    torch.cuda.synchronize()
+
+    # ---- device-timed region: K launches of S brain steps, L2 flushed between launches ----
+    launch_ms, events, spikes = [], 0.0, 0.0
+    sc_prev = brain.spikeCount.astype(np.int64)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            brain.run(S)
+            launch_ms.append(brain._batch.last_ms())
+            sc = brain.spikeCount.astype(np.int64)
+            d = sc - sc_prev
+            events += float((d * outdeg).sum())
+            spikes += float(d.sum())
+            sc_prev = sc
+    torch.cuda.synchronize()
+    barrier(world)
+    dev_s = max_over_ranks(sum(launch_ms) / 1e3, world)
+    tot_events = sum_over_ranks(events, world)
+    sim_s = args.steps * S * SYNTH_PARAMS["dt"] / 1000.0
+
+    # ---- end to end through the C ABI with host buffers ----
+    brain.reset()
+    h_idx = np.ascontiguousarray(idx, dtype=np.int32)
+    h_hz = np.ascontiguousarray(hz, dtype=np.float64)
+    e2e_events, h2d, d2h = 0.0, 0, 0
+    sc_prev = np.zeros(g.N, dtype=np.int64)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        brain._batch.set_drive(0, h_idx, h_hz)
+        h2d += h_idx.nbytes + h_hz.nbytes
+        brain.run(S)
+        sc = brain._batch.read("spikeCount", 0).astype(np.int64)
+        fired = brain._batch.fired(0)
+        d2h += g.N * 4 + fired.nbytes
+        e2e_events += float(((sc - sc_prev) * outdeg).sum())
+        sc_prev = sc
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_events = sum_over_ranks(e2e_events, world)
+
+    peak, kind = peaks()
+    per_launch_bytes = algorithmic_bytes(g.N, S, spikes / args.steps, events / args.steps)
+    achieved = per_launch_bytes / (np.mean(launch_ms) / 1e3) / 1e9
+    res = dict(
+        metric=METRIC, value=tot_events / dev_s, unit="synaptic events/s", n_gpus=world,
+        steps=args.steps, warmup=args.warmup, ms_per_step=1e3 * dev_s / args.steps,
+        higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+        data="synthetic (seeded connectome-shaped graph; no dataset)",
+        config=dict(workload="plain forward, full scale: N=165,122 synthetic connectome, "
+                    f"E={g.E:,} edges, 2,000 drive neurons at U(100,200) Hz, dt 0.1 ms, "
+                    f"{args.steps * S} brain steps ({sim_s * 1e3:.0f} ms simulated)",
+                    neurons=g.N, edges=g.E, brain_steps_per_step=S,
+                    delivery="exact (reference per-target order)",
+                    l2="flushed between timed launches (512 MiB write)", parallelism=f"replicas x{world}"),
+        sim_s_per_wall_s=sim_s / dev_s, realtime_factor=sim_s / dev_s, spikes=spikes,
+        events=tot_events,
+        e2e=dict(value=e2e_events / e2e_s, unit="synaptic events/s", h2d_bytes_per_step=h2d // args.steps,
+                 d2h_bytes_per_step=d2h // args.steps, sim_s_per_wall_s=sim_s / e2e_s),
+        gpu_launches=args.steps,
+        roofline=dict(bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
+                      peak_kind=kind, traffic=None,
+                      kernel="fb::step_kernel (persistent, all phases)",
+                      algorithmic_bytes_per_launch=per_launch_bytes),
+        clocks=clk.summary(),
+    )
+    if rank == 0:
+        sample = int(os.environ.get("FB_CPU_SAMPLE_STEPS", "4000"))
+        v, secs, ev = cpu_baseline(g, idx, hz, SYNTH_PARAMS, sample)
+        res["cpu_baseline"] = dict(value=v, unit="synaptic events/s", cores=1, kind="port",
+                                   sample=f"{sample} brain steps of the same workload from rest "
+                                          f"({secs:.1f} s, oracle port of lif_step, 1 thread)")
+        print(json.dumps(res), flush=True)
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU implementation of the path: lif_step as the reference build (when the
+    reference compiled here) or its oracle port, on this machine's host cores."""
+    if rank != 0:
+        return
+    from flybrain import SYNTH_PARAMS, workload
+    from oracle import oracle as O
+    backend = "ref" if os.path.exists(O.REF_LIB) else "port"
+    O.build(ref=False)
+    g, idx, hz, _ = workload("full", seed=1)
+    outdeg = g.outdeg().astype(np.int64)
+    ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, SYNTH_PARAMS, seed=1, backend=backend)
+    for i, h in zip(idx.tolist(), hz.tolist()):
+        ob.setDriveOne(i, h)
+    S = int(os.environ.get("FB_REF_SAMPLE_STEPS", "500"))
+    for _ in range(args.warmup):
+        ob.run(S)
+    ob.reset()
+    sc_prev = ob.spikeCount.astype(np.int64)
+    ev = 0.0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ob.run(S)
+        sc = ob.spikeCount.astype(np.int64)
+        ev += float(((sc - sc_prev) * outdeg).sum())
+        sc_prev = sc
+    secs = time.perf_counter() - t0
+    sim_s = args.steps * S * SYNTH_PARAMS["dt"] / 1000.0
+    v = ev / secs
+    sample = f"{args.steps} x {S} brain steps of the full-scale workload (lif_step is serial: 1 thread)"
+    print(json.dumps(dict(
+        impl="reference", metric=METRIC, value=v, unit="synaptic events/s", n_gpus=world,
+        steps=args.steps, warmup=args.warmup, ms_per_step=1e3 * secs / args.steps,
+        higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+        data="synthetic (seeded connectome-shaped graph; no dataset)",
+        config=dict(workload="plain forward, full scale: N=165,122 synthetic connectome, 2,000 drive "
+                    "neurons at U(100,200) Hz, dt 0.1 ms", brain_steps_per_step=S),
+        sim_s_per_wall_s=sim_s / secs,
+        cpu_baseline=dict(value=v, unit="synaptic events/s", cores=1,
+                          kind="reference" if backend == "ref" else "port", sample=sample),
+        e2e=dict(value=v, unit="synaptic events/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+    )), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    rank, world = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

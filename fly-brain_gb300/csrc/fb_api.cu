@@ -1,0 +1,831 @@
+// C ABI of the brain step (include/flybrain.h): graphs, brain batches, the LIFWasm-shaped
+// injection/readout surface, and the persistent step launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fb_internal.cuh"
+
+namespace fb {
+int step_kernel_blocks_per_sm(size_t smem);
+cudaError_t launch_step(const StepArgs &a, int grid, size_t smem, cudaStream_t st);
+struct Delta {
+  int32_t brain, field, idx, pad;
+  double val;
+};
+cudaError_t launch_deltas(Trial *trials, const Delta *d, const int32_t *gs, int32_t nGroups, cudaStream_t st);
+cudaError_t launch_reset(Trial *trials, int32_t b0, int32_t b1, cudaStream_t st);
+cudaError_t set_step_smem(size_t bytes);
+}  // namespace fb
+
+using namespace fb;
+
+// ---------------------------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CU(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      return fail(e_ == cudaErrorMemoryAllocation ? FB_ENOMEM : FB_ECUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                 \
+    }                                                                                  \
+  } while (0)
+
+extern "C" const char *fb_last_error(void) { return g_err.c_str(); }
+extern "C" int fb_version(void) { return 100; }
+
+extern "C" int fb_device_info(int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor) {
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  cudaDeviceProp p;
+  CU(cudaGetDeviceProperties(&p, dev));
+  if (sm_count) *sm_count = p.multiProcessorCount;
+  if (cc_major) *cc_major = p.major;
+  if (cc_minor) *cc_minor = p.minor;
+  return FB_OK;
+}
+
+extern "C" void fb_default_params(fb_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof *p);
+  p->dt = 0.5; p->vRest = -52; p->vThresh = -45; p->vReset = -52; p->tauM = 20; p->tauSyn = 5;
+  p->tRef = 2.2; p->delay = 1.8; p->traceTau = 30; p->adaptInc = 2.0; p->adaptTau = 100;
+  p->depU = 0.2; p->depTau = 200; p->eExc = 0; p->eInh = -70; p->bgRate = 0; p->bgAmp = 0;
+  p->preInh = 0; p->coba = 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// per-device constants: xorshift32 jump tables
+// ---------------------------------------------------------------------------------------------
+
+// Columns of M^(2^j) for the xorshift32 map M (x ^= x<<13; x ^= x>>17; x ^= x<<5), expanded to 8
+// nibble tables of 16 words each: table[j][n][v] = M^(2^j) applied to (v << 4n).
+static void build_jump_tables(std::vector<uint32_t> &tab) {
+  auto step = [](uint32_t x) { x ^= x << 13; x ^= x >> 17; x ^= x << 5; return x; };
+  uint32_t col[32][32];  // col[j][b] = M^(2^j) e_b
+  for (int b = 0; b < 32; b++) col[0][b] = step(1u << b);
+  auto apply = [&](int j, uint32_t x) {
+    uint32_t y = 0;
+    for (int b = 0; b < 32; b++)
+      if (x >> b & 1u) y ^= col[j][b];
+    return y;
+  };
+  for (int j = 1; j < 32; j++)
+    for (int b = 0; b < 32; b++) col[j][b] = apply(j - 1, col[j - 1][b]);
+  tab.assign(32 * 128, 0);
+  for (int j = 0; j < 32; j++)
+    for (int n = 0; n < 8; n++)
+      for (uint32_t v = 0; v < 16; v++) {
+        uint32_t y = 0;
+        for (int b = 0; b < 4; b++)
+          if (v >> b & 1u) y ^= col[j][4 * n + b];
+        tab[j * 128 + n * 16 + v] = y;
+      }
+}
+
+static std::mutex g_dev_mu;
+static uint32_t *g_jump[64];
+
+static int device_jump(uint32_t **out) {
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FB_ENODEV, "device ordinal %d unsupported", dev);
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (!g_jump[dev]) {
+    cudaDeviceProp p;
+    CU(cudaGetDeviceProperties(&p, dev));
+    if (p.major != 10 || p.minor != 3)
+      return fail(FB_ENODEV, "device %d is sm_%d%d; this library is built for sm_103a", dev, p.major, p.minor);
+    std::vector<uint32_t> tab;
+    build_jump_tables(tab);
+    uint32_t *d = nullptr;
+    CU(cudaMalloc(&d, tab.size() * 4));
+    CU(cudaMemcpy(d, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+    g_jump[dev] = d;
+  }
+  *out = g_jump[dev];
+  return FB_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// graphs
+// ---------------------------------------------------------------------------------------------
+struct Topology {
+  int32_t N = 0;
+  int64_t E = 0;
+  uint32_t *indptr = nullptr, *indices = nullptr;
+  int refs = 0;
+};
+
+struct fb_graph {
+  Topology *topo = nullptr;
+  float *W = nullptr, *sign = nullptr;
+};
+
+static void topo_release(Topology *t) {
+  if (t && --t->refs == 0) {
+    cudaFree(t->indptr);
+    cudaFree(t->indices);
+    delete t;
+  }
+}
+
+extern "C" int fb_graph_create(int32_t N, int64_t E, const uint32_t *indptr, const uint32_t *indices,
+                               const float *weights, const float *sign, fb_graph **out) {
+  if (!out) return fail(FB_EINVAL, "fb_graph_create: out is null");
+  *out = nullptr;
+  if (N <= 0 || E < 0 || !indptr || (E > 0 && (!indices || !weights)) || !sign)
+    return fail(FB_EINVAL, "fb_graph_create: bad sizes or null arrays (N=%d E=%lld)", N, (long long)E);
+  if (E > 0xfffffff0LL) return fail(FB_EINVAL, "fb_graph_create: E=%lld exceeds 32-bit edge offsets", (long long)E);
+  uint32_t *jt;
+  int rc = device_jump(&jt);
+  if (rc) return rc;
+  // validate the CSR on the host (arrays may live on either side)
+  std::vector<uint32_t> ip(N + 1), ix(E);
+  CU(cudaMemcpy(ip.data(), indptr, (size_t)(N + 1) * 4, cudaMemcpyDefault));
+  if (E) CU(cudaMemcpy(ix.data(), indices, (size_t)E * 4, cudaMemcpyDefault));
+  if (ip[0] != 0 || ip[N] != (uint64_t)E) return fail(FB_EINVAL, "fb_graph_create: indptr[0]=%u indptr[N]=%u, E=%lld", ip[0], ip[N], (long long)E);
+  std::vector<int32_t> stamp(N, -1);
+  for (int32_t r = 0; r < N; r++) {
+    if (ip[r + 1] < ip[r]) return fail(FB_EINVAL, "fb_graph_create: indptr decreases at row %d", r);
+    for (uint32_t j = ip[r]; j < ip[r + 1]; j++) {
+      const uint32_t q = ix[j];
+      if (q >= (uint32_t)N) return fail(FB_EINVAL, "fb_graph_create: indices[%u]=%u out of range", j, q);
+      if (stamp[q] == r) return fail(FB_EINVAL, "fb_graph_create: row %d repeats target %u", r, q);
+      stamp[q] = r;
+    }
+  }
+  Topology *t = new (std::nothrow) Topology;
+  fb_graph *g = new (std::nothrow) fb_graph;
+  if (!t || !g) { delete t; delete g; return fail(FB_ENOMEM, "host allocation"); }
+  t->N = N; t->E = E; t->refs = 1;
+  g->topo = t;
+  auto cleanup = [&]() { cudaFree(g->W); cudaFree(g->sign); topo_release(t); delete g; };
+  if (cudaMalloc(&t->indptr, (size_t)(N + 1) * 4) != cudaSuccess ||
+      cudaMalloc(&t->indices, (size_t)std::max<int64_t>(E, 1) * 4) != cudaSuccess ||
+      cudaMalloc(&g->W, (size_t)std::max<int64_t>(E, 1) * 4) != cudaSuccess ||
+      cudaMalloc(&g->sign, (size_t)N * 4) != cudaSuccess) {
+    cleanup();
+    return fail(FB_ENOMEM, "fb_graph_create: device allocation of %lld edges failed", (long long)E);
+  }
+  if (cudaMemcpy(t->indptr, ip.data(), (size_t)(N + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+      (E && cudaMemcpy(t->indices, ix.data(), (size_t)E * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (E && cudaMemcpy(g->W, weights, (size_t)E * 4, cudaMemcpyDefault) != cudaSuccess) ||
+      cudaMemcpy(g->sign, sign, (size_t)N * 4, cudaMemcpyDefault) != cudaSuccess) {
+    cleanup();
+    return fail(FB_ECUDA, "fb_graph_create: upload failed");
+  }
+  *out = g;
+  return FB_OK;
+}
+
+extern "C" int fb_graph_create_shared(const fb_graph *topology, const float *weights, const float *sign,
+                                      fb_graph **out) {
+  if (!topology || !out || !weights || !sign) return fail(FB_EINVAL, "fb_graph_create_shared: null argument");
+  *out = nullptr;
+  Topology *t = topology->topo;
+  fb_graph *g = new (std::nothrow) fb_graph;
+  if (!g) return fail(FB_ENOMEM, "host allocation");
+  if (cudaMalloc(&g->W, (size_t)std::max<int64_t>(t->E, 1) * 4) != cudaSuccess ||
+      cudaMalloc(&g->sign, (size_t)t->N * 4) != cudaSuccess) {
+    cudaFree(g->W); cudaFree(g->sign); delete g;
+    return fail(FB_ENOMEM, "fb_graph_create_shared: device allocation failed");
+  }
+  if ((t->E && cudaMemcpy(g->W, weights, (size_t)t->E * 4, cudaMemcpyDefault) != cudaSuccess) ||
+      cudaMemcpy(g->sign, sign, (size_t)t->N * 4, cudaMemcpyDefault) != cudaSuccess) {
+    cudaFree(g->W); cudaFree(g->sign); delete g;
+    return fail(FB_ECUDA, "fb_graph_create_shared: upload failed");
+  }
+  t->refs++;
+  g->topo = t;
+  *out = g;
+  return FB_OK;
+}
+
+extern "C" int fb_graph_set_sign(fb_graph *g, const float *sign) {
+  if (!g || !sign) return fail(FB_EINVAL, "fb_graph_set_sign: null argument");
+  CU(cudaDeviceSynchronize());  // no step may be reading the old vector
+  CU(cudaMemcpy(g->sign, sign, (size_t)g->topo->N * 4, cudaMemcpyDefault));
+  return FB_OK;
+}
+
+extern "C" int fb_graph_info(const fb_graph *g, int32_t *N, int64_t *E) {
+  if (!g) return fail(FB_EINVAL, "fb_graph_info: null graph");
+  if (N) *N = g->topo->N;
+  if (E) *E = g->topo->E;
+  return FB_OK;
+}
+
+extern "C" int fb_graph_destroy(fb_graph *g) {
+  if (!g) return FB_OK;
+  cudaFree(g->W);
+  cudaFree(g->sign);
+  topo_release(g->topo);
+  delete g;
+  return FB_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// brain batches
+// ---------------------------------------------------------------------------------------------
+
+// Insertion-ordered set of driven neurons (a JS Set: deletion keeps the others' order, re-adding
+// appends). Deleted entries are tombstones until the next sync compacts the list.
+struct DrivenSet {
+  std::vector<int32_t> order;  // neuron or -1
+  std::vector<int32_t> pos;    // index in order, or -1
+  bool dirty = true;
+  void init(int N) { order.clear(); pos.assign(N, -1); dirty = true; }
+  void add(int32_t i) {
+    if (pos[i] >= 0) return;
+    pos[i] = (int32_t)order.size();
+    order.push_back(i);
+    dirty = true;
+  }
+  void remove(int32_t i) {
+    if (pos[i] < 0) return;
+    order[pos[i]] = -1;
+    pos[i] = -1;
+    dirty = true;
+  }
+  void compact() {
+    size_t n = 0;
+    for (size_t k = 0; k < order.size(); k++)
+      if (order[k] >= 0) {
+        order[n] = order[k];
+        pos[order[n]] = (int32_t)n;
+        n++;
+      }
+    order.resize(n);
+  }
+};
+
+struct fb_brains {
+  int B = 0;
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<Trial> host;   // host mirror: constants and device pointers
+  Trial *trials = nullptr;   // device array
+  std::vector<void *> arenas;
+  std::vector<DrivenSet> driven;
+  std::vector<Delta> deltas;
+  std::vector<int32_t> tileTrial;
+  int32_t *d_tileTrial = nullptr, *d_steps = nullptr, *d_err = nullptr, *d_groups = nullptr;
+  Delta *d_deltas = nullptr;
+  size_t deltaCap = 0, groupCap = 0;
+  uint32_t *d_bar = nullptr;   // [count, gen]
+  OvfRec *d_ovf[2] = {nullptr, nullptr};
+  uint32_t *d_ovfTop = nullptr;
+  uint32_t ovfCap = 0;
+  uint32_t *jump = nullptr;
+  std::vector<int32_t> stepsHost;
+  std::vector<double> dts;   // each brain's dt as given (double), for setBackground
+  int grid = 0;
+  size_t smem = 0;
+  int logging = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float lastMs = 0.f;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static int brains_fail_cleanup(fb_brains *br, int rc) {
+  std::string keep = g_err;
+  fb_brains_destroy(br);
+  g_err = keep;
+  return rc;
+}
+
+// Per-brain header constants: each computed in double and rounded once to f32, in the
+// expressions of LIFWasm._writeHeader (src/lifwasm.js:58-67).
+static void fill_constants(Trial &T, const fb_params &p, int32_t N) {
+  T.coba = p.coba ? 1 : 0;
+  T.dt = (float)p.dt; T.vRest = (float)p.vRest; T.vThresh = (float)p.vThresh; T.vReset = (float)p.vReset;
+  T.tRef = (float)p.tRef; T.adaptInc = (float)p.adaptInc; T.depU = (float)p.depU;
+  T.dE = (float)std::exp(-p.dt / p.tauSyn);
+  T.dTr = (float)std::exp(-p.dt / p.traceTau);
+  T.dA = (float)std::exp(-p.dt / p.adaptTau);
+  T.kRec = (float)(p.dt / p.depTau);
+  T.kM = (float)(p.dt / p.tauM);
+  T.dtS = (float)(p.dt / 1000);
+  T.eExc = (float)p.eExc; T.eInh = (float)p.eInh;
+  T.cE = (float)(1 / (p.eExc - p.vRest));
+  T.cI = (float)(1 / (p.vRest - p.eInh));
+  T.bgEvents = (float)((double)N * p.bgRate * p.dt / 1000);
+  T.bgAmp = (float)p.bgAmp;
+  T.preInh = (float)p.preInh;
+  T.flags = (T.bgEvents > 0 ? kHasBg : 0) | (T.depU != 0.f ? kHasDep : 0) | (T.preInh > 0.f ? kHasPreInh : 0);
+}
+
+// JS: (seed * 2654435761) >>> 0 || 1, the product formed in double (src/lifwasm.js:52).
+static uint32_t seed_state(uint32_t seed) {
+  const double prod = (double)seed * 2654435761.0;
+  const double m = std::fmod(std::floor(prod), 4294967296.0);
+  const uint32_t s = (uint32_t)m;
+  return s ? s : 1u;
+}
+
+extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const fb_params *params,
+                                int32_t params_stride, const uint32_t *seeds, fb_brains **out) {
+  if (!out) return fail(FB_EINVAL, "fb_brains_create: out is null");
+  *out = nullptr;
+  if (!graphs || B <= 0 || !params || !seeds) return fail(FB_EINVAL, "fb_brains_create: bad arguments (B=%d)", B);
+  if (B > 8192) return fail(FB_EINVAL, "fb_brains_create: B=%d exceeds 8192 brains per batch", B);
+  fb_brains *br = new (std::nothrow) fb_brains;
+  if (!br) return fail(FB_ENOMEM, "host allocation");
+  int rc = device_jump(&br->jump);
+  if (rc) { delete br; return rc; }
+  if (cudaGetDevice(&br->dev) != cudaSuccess || cudaStreamCreateWithFlags(&br->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete br;
+    return fail(FB_ECUDA, "stream creation failed");
+  }
+  br->B = B;
+  br->host.assign(B, Trial{});
+  br->dts.assign(B, 0.0);
+  br->driven.resize(B);
+  int tileBase = 0;
+  for (int b = 0; b < B; b++) {
+    const fb_graph *g = graphs[b];
+    const fb_params &p = *(const fb_params *)((const char *)params + (size_t)b * params_stride);
+    if (!g) return brains_fail_cleanup(br, fail(FB_EINVAL, "fb_brains_create: graphs[%d] is null", b));
+    if (!(p.dt > 0) || !(p.delay >= 0) || !(p.tauM > 0) || !(p.tauSyn > 0))
+      return brains_fail_cleanup(br, fail(FB_EINVAL, "fb_brains_create: brain %d: dt, tauM, tauSyn must be > 0", b));
+    const int32_t N = g->topo->N;
+    const int64_t E = g->topo->E;
+    // ring depth, src/lifwasm.js:39: max(1, Math.round(delay / dt)) + 1
+    const int ns = (int)std::max(1.0, std::floor(p.delay / p.dt + 0.5)) + 1;
+    if (ns < 3)
+      return brains_fail_cleanup(br, fail(FB_EINVAL, "fb_brains_create: brain %d: delay/dt rounds to %d step; at least 2 are required", b, ns - 1));
+    Trial &T = br->host[b];
+    br->dts[b] = p.dt;
+    T.N = N;
+    T.nslots = ns;
+    T.mode = FB_DELIVER_EXACT;
+    fill_constants(T, p, N);
+    if (T.flags & kHasPreInh) T.mode = FB_DELIVER_SEQUENTIAL;
+    T.nTiles = (N + kTile - 1) / kTile;
+    T.tileBase = tileBase;
+    tileBase += T.nTiles;
+    for (int u = 0; u < T.nTiles; u++) br->tileTrial.push_back(b);
+    T.chunkCap = (E + kChunk - 1) / kChunk + 1;
+    T.indptr = g->topo->indptr;
+    T.indices = g->topo->indices;
+    T.W = g->W;
+    T.sign = g->sign;
+    T.rng = seed_state(seeds[b]);
+    // arena layout
+    const size_t n4 = align256((size_t)N * 4);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
+    size_t o_state = take(n4 * 11);
+    size_t o_ring = take((size_t)ns * N * 4), o_ringCount = take((size_t)ns * 4);
+    size_t o_ringOff = take((size_t)ns * (N + 1) * 4), o_chunkK = take((size_t)ns * T.chunkCap * 4);
+    size_t o_slotEdges = take((size_t)ns * 4), o_driven = take((size_t)N * 4);
+    size_t o_cnt = take((size_t)N * 4), o_bucket = take((size_t)N * kBucket * 8);
+    size_t o_ovfHead = take((size_t)N * 4), o_bg = take((size_t)N * 4), o_arr = take((size_t)N);
+    size_t o_stage = take((size_t)T.nTiles * kTile * 4), o_stageDeg = take((size_t)T.nTiles * kTile * 4);
+    size_t o_tileCnt = take((size_t)T.nTiles * 4), o_tileDeg = take((size_t)T.nTiles * 4);
+    char *base = nullptr;
+    if (cudaMalloc(&base, off) != cudaSuccess)
+      return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: brain %d: %zu bytes of device memory", b, off));
+    br->arenas.push_back(base);
+    if (cudaMemsetAsync(base, 0, off, br->stream) != cudaSuccess ||
+        cudaMemsetAsync(base + o_ovfHead, 0xff, (size_t)N * 4, br->stream) != cudaSuccess)
+      return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: clearing state failed"));
+    float *st = (float *)(base + o_state);
+    T.v = st; T.gE = (float *)((char *)st + n4); T.gI = (float *)((char *)st + 2 * n4);
+    T.refr = (float *)((char *)st + 3 * n4); T.trace = (float *)((char *)st + 4 * n4);
+    T.adapt = (float *)((char *)st + 5 * n4); T.res = (float *)((char *)st + 6 * n4);
+    T.bias = (float *)((char *)st + 7 * n4); T.thr = (float *)((char *)st + 8 * n4);
+    T.drive = (float *)((char *)st + 9 * n4); T.spikeCount = (uint32_t *)((char *)st + 10 * n4);
+    T.ring = (int32_t *)(base + o_ring); T.ringCount = (int32_t *)(base + o_ringCount);
+    T.ringOff = (uint32_t *)(base + o_ringOff); T.chunkK = (uint32_t *)(base + o_chunkK);
+    T.slotEdges = (uint32_t *)(base + o_slotEdges); T.driven = (int32_t *)(base + o_driven);
+    T.cnt = (uint32_t *)(base + o_cnt); T.bucket = (uint2 *)(base + o_bucket);
+    T.ovfHead = (uint32_t *)(base + o_ovfHead); T.bgHits = (uint32_t *)(base + o_bg);
+    T.arrived = (uint8_t *)(base + o_arr);
+    T.stage = (int32_t *)(base + o_stage); T.stageDeg = (uint32_t *)(base + o_stageDeg);
+    T.tileCnt = (int32_t *)(base + o_tileCnt); T.tileDeg = (uint32_t *)(base + o_tileDeg);
+    br->driven[b].init(N);
+  }
+  // batch-wide buffers
+  const int nTiles = (int)br->tileTrial.size();
+  if (cudaMalloc(&br->trials, sizeof(Trial) * B) != cudaSuccess ||
+      cudaMalloc(&br->d_tileTrial, sizeof(int32_t) * nTiles) != cudaSuccess ||
+      cudaMalloc(&br->d_steps, sizeof(int32_t) * B) != cudaSuccess ||
+      cudaMalloc(&br->d_err, sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&br->d_bar, sizeof(uint32_t) * 2) != cudaSuccess ||
+      cudaMalloc(&br->d_ovfTop, sizeof(uint32_t) * 2) != cudaSuccess)
+    return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: batch buffers"));
+  // overflow pool: 1M records per parity plus one per 16 edges of the largest graph
+  int64_t maxE = 0;
+  for (int b = 0; b < B; b++) maxE = std::max<int64_t>(maxE, graphs[b]->topo->E);
+  br->ovfCap = (uint32_t)std::min<int64_t>((1 << 20) + maxE / 16, 0x7fffffff);
+  for (int k = 0; k < 2; k++)
+    if (cudaMalloc(&br->d_ovf[k], sizeof(OvfRec) * (size_t)br->ovfCap) != cudaSuccess)
+      return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: overflow pool"));
+  if (cudaMemsetAsync(br->d_err, 0, 4, br->stream) != cudaSuccess ||
+      cudaMemsetAsync(br->d_bar, 0, 8, br->stream) != cudaSuccess ||
+      cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream) != cudaSuccess ||
+      cudaMemcpyAsync(br->d_tileTrial, br->tileTrial.data(), sizeof(int32_t) * nTiles, cudaMemcpyHostToDevice, br->stream) != cudaSuccess ||
+      cudaMemcpyAsync(br->trials, br->host.data(), sizeof(Trial) * B, cudaMemcpyHostToDevice, br->stream) != cudaSuccess)
+    return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: upload failed"));
+  if (launch_reset(br->trials, 0, B, br->stream) != cudaSuccess)
+    return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: reset launch failed"));
+  // persistent grid: every SM, as many blocks as stay co-resident
+  br->smem = sizeof(int32_t) * (size_t)(4 * B + 1);
+  if (br->smem > 48 * 1024 && set_step_smem(br->smem) != cudaSuccess)
+    return brains_fail_cleanup(br, fail(FB_ECUDA, "step kernel: %zu bytes of shared memory refused", br->smem));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, br->dev);
+  const int per = step_kernel_blocks_per_sm(br->smem);
+  if (per <= 0) return brains_fail_cleanup(br, fail(FB_ECUDA, "step kernel does not fit on an SM (smem %zu)", br->smem));
+  br->grid = sms * per;
+  cudaEventCreate(&br->ev0);
+  cudaEventCreate(&br->ev1);
+  if (cudaStreamSynchronize(br->stream) != cudaSuccess)
+    return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = br;
+  return FB_OK;
+}
+
+extern "C" int fb_brains_destroy(fb_brains *br) {
+  if (!br) return FB_OK;
+  if (br->stream) cudaStreamSynchronize(br->stream);
+  for (int b = 0; b < (int)br->host.size(); b++) {
+    cudaFree(br->host[b].logCount);
+    cudaFree(br->host[b].logRaster);
+  }
+  for (void *p : br->arenas) cudaFree(p);
+  cudaFree(br->trials); cudaFree(br->d_tileTrial); cudaFree(br->d_steps); cudaFree(br->d_err);
+  cudaFree(br->d_groups); cudaFree(br->d_deltas); cudaFree(br->d_bar); cudaFree(br->d_ovfTop);
+  cudaFree(br->d_ovf[0]); cudaFree(br->d_ovf[1]);
+  if (br->ev0) cudaEventDestroy(br->ev0);
+  if (br->ev1) cudaEventDestroy(br->ev1);
+  if (br->stream) cudaStreamDestroy(br->stream);
+  delete br;
+  return FB_OK;
+}
+
+extern "C" int fb_brains_set_mode(fb_brains *br, int32_t mode) {
+  if (!br || mode < FB_DELIVER_EXACT || mode > FB_DELIVER_FAST) return fail(FB_EINVAL, "fb_brains_set_mode: bad mode %d", mode);
+  for (int b = 0; b < br->B; b++) {
+    Trial &T = br->host[b];
+    T.mode = (T.flags & kHasPreInh) && mode == FB_DELIVER_EXACT ? FB_DELIVER_SEQUENTIAL : mode;
+    if (T.mode == FB_DELIVER_FAST && (T.flags & kHasPreInh)) T.mode = FB_DELIVER_SEQUENTIAL;
+    CU(cudaMemcpyAsync(&br->trials[b].mode, &T.mode, 4, cudaMemcpyHostToDevice, br->stream));
+  }
+  CU(cudaStreamSynchronize(br->stream));
+  return FB_OK;
+}
+
+static int check_brain(fb_brains *br, int32_t b, const char *fn) {
+  if (!br) return fail(FB_EINVAL, "%s: null handle", fn);
+  if (b < 0 || b >= br->B) return fail(FB_EINVAL, "%s: brain %d out of range [0, %d)", fn, b, br->B);
+  return FB_OK;
+}
+
+// Applies queued injections (in call order) and re-uploads changed driven lists.
+static int flush(fb_brains *br) {
+  if (!br->deltas.empty()) {
+    std::vector<Delta> &d = br->deltas;
+    std::stable_sort(d.begin(), d.end(), [](const Delta &x, const Delta &y) {
+      if (x.brain != y.brain) return x.brain < y.brain;
+      if (x.field != y.field) return x.field < y.field;
+      return x.idx < y.idx;
+    });
+    std::vector<int32_t> gs;
+    for (size_t k = 0; k < d.size(); k++)
+      if (k == 0 || d[k].brain != d[k - 1].brain || d[k].field != d[k - 1].field || d[k].idx != d[k - 1].idx)
+        gs.push_back((int32_t)k);
+    const int32_t ng = (int32_t)gs.size();
+    gs.push_back((int32_t)d.size());
+    if (d.size() > br->deltaCap) {
+      cudaFree(br->d_deltas);
+      br->deltaCap = std::max<size_t>(d.size(), 1024);
+      CU(cudaMalloc(&br->d_deltas, sizeof(Delta) * br->deltaCap));
+    }
+    if (gs.size() > br->groupCap) {
+      cudaFree(br->d_groups);
+      br->groupCap = std::max<size_t>(gs.size(), 1025);
+      CU(cudaMalloc(&br->d_groups, sizeof(int32_t) * br->groupCap));
+    }
+    CU(cudaMemcpyAsync(br->d_deltas, d.data(), sizeof(Delta) * d.size(), cudaMemcpyHostToDevice, br->stream));
+    CU(cudaMemcpyAsync(br->d_groups, gs.data(), sizeof(int32_t) * gs.size(), cudaMemcpyHostToDevice, br->stream));
+    CU(launch_deltas(br->trials, br->d_deltas, br->d_groups, ng, br->stream));
+    CU(cudaStreamSynchronize(br->stream));  // host vectors are reused by the next flush
+    d.clear();
+  }
+  for (int b = 0; b < br->B; b++) {
+    DrivenSet &ds = br->driven[b];
+    if (!ds.dirty) continue;
+    ds.compact();
+    Trial &T = br->host[b];
+    T.nDriven = (int32_t)ds.order.size();
+    if (T.nDriven)
+      CU(cudaMemcpyAsync(T.driven, ds.order.data(), sizeof(int32_t) * T.nDriven, cudaMemcpyHostToDevice, br->stream));
+    CU(cudaMemcpyAsync(&br->trials[b].nDriven, &T.nDriven, 4, cudaMemcpyHostToDevice, br->stream));
+    CU(cudaStreamSynchronize(br->stream));
+    ds.dirty = false;
+  }
+  return FB_OK;
+}
+
+static int queue(fb_brains *br, int32_t b, int32_t field, const int32_t *idx, const double *val,
+                 int32_t n, const char *fn) {
+  int rc = check_brain(br, b, fn);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!idx || !val))) return fail(FB_EINVAL, "%s: bad list (n=%d)", fn, n);
+  const int32_t N = br->host[b].N;
+  for (int32_t k = 0; k < n; k++) {
+    if (idx[k] < 0 || idx[k] >= N) return fail(FB_EINVAL, "%s: index %d out of range [0, %d)", fn, idx[k], N);
+    if (!std::isfinite(val[k]) && field != FB_FIELD_THR && field != FB_FIELD_BIAS)
+      return fail(FB_EINVAL, "%s: value %g is not finite", fn, val[k]);
+  }
+  for (int32_t k = 0; k < n; k++) br->deltas.push_back(Delta{b, field, idx[k], 0, val[k]});
+  return FB_OK;
+}
+
+extern "C" int fb_set_drive(fb_brains *br, int32_t b, const int32_t *idx, const double *hz, int32_t n) {
+  int rc = queue(br, b, FB_FIELD_DRIVE, idx, hz, n, "fb_set_drive");
+  if (rc) return rc;
+  DrivenSet &ds = br->driven[b];
+  for (int32_t k = 0; k < n; k++) {
+    if (hz[k] > 0) ds.add(idx[k]);
+    else ds.remove(idx[k]);
+  }
+  return FB_OK;
+}
+
+extern "C" int fb_set_bias(fb_brains *br, int32_t b, const int32_t *idx, const double *mv, int32_t n) {
+  return queue(br, b, FB_FIELD_BIAS, idx, mv, n, "fb_set_bias");
+}
+
+extern "C" int fb_set_thr(fb_brains *br, int32_t b, const int32_t *idx, const double *mv, int32_t n) {
+  return queue(br, b, FB_FIELD_THR, idx, mv, n, "fb_set_thr");
+}
+
+extern "C" int fb_add_g(fb_brains *br, int32_t b, const int32_t *idx, const double *e, const double *i, int32_t n) {
+  int rc = queue(br, b, FB_FIELD_GE, idx, e, n, "fb_add_g");
+  if (rc) return rc;
+  if (i) {
+    // addG(i, e, ii) always adds ii || 0 to gI (src/lifwasm.js:75)
+    return queue(br, b, FB_FIELD_GI, idx, i, n, "fb_add_g");
+  }
+  std::vector<double> z(n, 0.0);
+  return queue(br, b, FB_FIELD_GI, idx, z.data(), n, "fb_add_g");
+}
+
+extern "C" int fb_pulse(fb_brains *br, int32_t b, const int32_t *idx, const double *mv, int32_t n) {
+  return queue(br, b, FB_FIELD_GE, idx, mv, n, "fb_pulse");
+}
+
+extern "C" int fb_reset(fb_brains *br, int32_t b) {
+  if (!br) return fail(FB_EINVAL, "fb_reset: null handle");
+  if (b != -1) {
+    int rc = check_brain(br, b, "fb_reset");
+    if (rc) return rc;
+  }
+  int rc = flush(br);
+  if (rc) return rc;
+  CU(launch_reset(br->trials, b < 0 ? 0 : b, b < 0 ? br->B : b + 1, br->stream));
+  CU(cudaStreamSynchronize(br->stream));
+  return FB_OK;
+}
+
+extern "C" int fb_set_background(fb_brains *br, int32_t b, double rate_hz, double amp_mv) {
+  int rc = check_brain(br, b, "fb_set_background");
+  if (rc) return rc;
+  Trial &T = br->host[b];
+  // src/lifwasm.js:69: header f32 at byte 172 <- N * rate * p.dt / 1000 (double dt), 176 <- amp
+  T.bgEvents = (float)((double)T.N * rate_hz * br->dts[b] / 1000);
+  T.bgAmp = (float)amp_mv;
+  T.flags = (T.flags & ~kHasBg) | (T.bgEvents > 0 ? kHasBg : 0);
+  CU(cudaMemcpyAsync(&br->trials[b].bgEvents, &T.bgEvents, 8, cudaMemcpyHostToDevice, br->stream));
+  CU(cudaMemcpyAsync(&br->trials[b].flags, &T.flags, 4, cudaMemcpyHostToDevice, br->stream));
+  CU(cudaStreamSynchronize(br->stream));
+  return FB_OK;
+}
+
+static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
+  int rc = flush(br);
+  if (rc) return rc;
+  if (maxSteps > 0) {
+    CU(cudaMemcpyAsync(br->d_steps, br->stepsHost.data(), sizeof(int32_t) * br->B, cudaMemcpyHostToDevice, br->stream));
+    StepArgs a;
+    memset(&a, 0, sizeof a);
+    a.trials = br->trials;
+    a.B = br->B;
+    a.maxSteps = maxSteps;
+    a.steps = br->d_steps;
+    a.tileTrial = br->d_tileTrial;
+    a.nTilesTotal = (int32_t)br->tileTrial.size();
+    a.jump = br->jump;
+    a.barCount = br->d_bar;
+    a.barGen = br->d_bar + 1;
+    a.err = br->d_err;
+    a.ovf[0] = br->d_ovf[0];
+    a.ovf[1] = br->d_ovf[1];
+    a.ovfTop = br->d_ovfTop;
+    a.ovfCap = br->ovfCap;
+    a.log = br->logging;
+    a.timeoutNs = 5000000000LL;
+    CU(cudaEventRecord(br->ev0, br->stream));
+    CU(launch_step(a, br->grid, br->smem, br->stream));
+    CU(cudaEventRecord(br->ev1, br->stream));
+    int32_t err = 0;
+    CU(cudaMemcpyAsync(&err, br->d_err, 4, cudaMemcpyDeviceToHost, br->stream));
+    CU(cudaStreamSynchronize(br->stream));
+    cudaEventElapsedTime(&br->lastMs, br->ev0, br->ev1);
+    if (err) {
+      // leave the handle launchable: clear the flag, the barrier and the overflow pool
+      cudaMemsetAsync(br->d_err, 0, 4, br->stream);
+      cudaMemsetAsync(br->d_bar, 0, 8, br->stream);
+      cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream);
+      cudaStreamSynchronize(br->stream);
+      return fail(err, err == FB_ETIMEOUT ? "fb_step: a device-side wait timed out; the step was abandoned"
+                                          : "fb_step: delivery overflow (more than %d contributions to one target in one step, or the pool of %u records is full)",
+                  kSortMax, br->ovfCap);
+    }
+  }
+  if (out_nfired) {
+    for (int b = 0; b < br->B; b++)
+      CU(cudaMemcpyAsync(out_nfired + b, &br->trials[b].nFired, 4, cudaMemcpyDefault, br->stream));
+    CU(cudaStreamSynchronize(br->stream));
+  }
+  return FB_OK;
+}
+
+extern "C" int fb_step(fb_brains *br, int32_t nsteps, int32_t *out_nfired) {
+  if (!br) return fail(FB_EINVAL, "fb_step: null handle");
+  if (nsteps < 0) return fail(FB_EINVAL, "fb_step: nsteps=%d", nsteps);
+  br->stepsHost.assign(br->B, nsteps);
+  return run_steps(br, nsteps, out_nfired);
+}
+
+extern "C" int fb_step_uneven(fb_brains *br, const int32_t *steps, int32_t *out_nfired) {
+  if (!br || !steps) return fail(FB_EINVAL, "fb_step_uneven: null argument");
+  br->stepsHost.assign(steps, steps + br->B);
+  int32_t mx = 0;
+  for (int b = 0; b < br->B; b++) {
+    if (steps[b] < 0) return fail(FB_EINVAL, "fb_step_uneven: steps[%d]=%d", b, steps[b]);
+    mx = std::max(mx, steps[b]);
+  }
+  return run_steps(br, mx, out_nfired);
+}
+
+extern "C" int fb_last_step_ms(fb_brains *br, float *ms) {
+  if (!br || !ms) return fail(FB_EINVAL, "fb_last_step_ms: null argument");
+  *ms = br->lastMs;
+  return FB_OK;
+}
+
+extern "C" int fb_record(fb_brains *br, int32_t cap_steps, int64_t cap_spikes) {
+  if (!br || cap_steps < 0 || cap_spikes < 0) return fail(FB_EINVAL, "fb_record: bad arguments");
+  CU(cudaStreamSynchronize(br->stream));
+  for (int b = 0; b < br->B; b++) {
+    Trial &T = br->host[b];
+    cudaFree(T.logCount);
+    cudaFree(T.logRaster);
+    T.logCount = nullptr;
+    T.logRaster = nullptr;
+    T.logCap = T.logRasterCap = 0;
+    if (cap_steps > 0) {
+      CU(cudaMalloc(&T.logCount, sizeof(int32_t) * (size_t)cap_steps));
+      CU(cudaMemsetAsync(T.logCount, 0, sizeof(int32_t) * (size_t)cap_steps, br->stream));
+      T.logCap = cap_steps;
+      if (cap_spikes > 0) {
+        CU(cudaMalloc(&T.logRaster, sizeof(int32_t) * (size_t)cap_spikes));
+        T.logRasterCap = cap_spikes;
+      }
+    }
+    // the device owns stepsDone: read it, start the log at the next step
+    int64_t done = 0;
+    CU(cudaMemcpy(&done, &br->trials[b].stepsDone, 8, cudaMemcpyDeviceToHost));
+    T.stepsDone = done;
+    T.logStart = done;
+    T.logRasterLen[0] = T.logRasterLen[1] = 0;
+    CU(cudaMemcpyAsync(&br->trials[b].logCount, &T.logCount, sizeof(void *) * 2 + sizeof(int64_t) * 2, cudaMemcpyHostToDevice, br->stream));
+    CU(cudaMemcpyAsync(&br->trials[b].logStart, &T.logStart, sizeof(int64_t) * 3, cudaMemcpyHostToDevice, br->stream));
+  }
+  br->logging = cap_steps > 0 ? 1 : 0;
+  CU(cudaStreamSynchronize(br->stream));
+  return FB_OK;
+}
+
+extern "C" int fb_spike_log(fb_brains *br, int32_t b, int32_t *counts, int32_t cap_steps, int32_t *raster,
+                            int64_t cap_spikes, int64_t *n_steps, int64_t *n_spikes) {
+  int rc = check_brain(br, b, "fb_spike_log");
+  if (rc) return rc;
+  CU(cudaStreamSynchronize(br->stream));
+  Trial dev;
+  CU(cudaMemcpy(&dev, &br->trials[b], sizeof(Trial), cudaMemcpyDeviceToHost));
+  const int64_t steps = dev.stepsDone - dev.logStart;
+  const int64_t spikes = dev.logRasterLen[dev.stepsDone & 1];
+  if (n_steps) *n_steps = steps;
+  if (n_spikes) *n_spikes = dev.logRaster ? spikes : 0;
+  if (counts && dev.logCount) {
+    const int64_t n = std::min<int64_t>({(int64_t)cap_steps, steps, dev.logCap});
+    if (n > 0) CU(cudaMemcpy(counts, dev.logCount, sizeof(int32_t) * n, cudaMemcpyDefault));
+  }
+  if (raster && dev.logRaster) {
+    const int64_t n = std::min<int64_t>({cap_spikes, spikes, dev.logRasterCap});
+    if (n > 0) CU(cudaMemcpy(raster, dev.logRaster, sizeof(int32_t) * n, cudaMemcpyDefault));
+  }
+  return FB_OK;
+}
+
+extern "C" int fb_fired(fb_brains *br, int32_t b, int32_t *dst, int32_t cap, int32_t *n) {
+  int rc = check_brain(br, b, "fb_fired");
+  if (rc) return rc;
+  CU(cudaStreamSynchronize(br->stream));
+  int32_t nf_slot[2];
+  CU(cudaMemcpy(nf_slot, &br->trials[b].nFired, 8, cudaMemcpyDeviceToHost));
+  if (n) *n = nf_slot[0];
+  const int32_t m = std::min(nf_slot[0], cap);
+  if (dst && m > 0) {
+    const Trial &T = br->host[b];
+    CU(cudaMemcpy(dst, T.ring + (int64_t)nf_slot[1] * T.N, sizeof(int32_t) * m, cudaMemcpyDefault));
+  }
+  return FB_OK;
+}
+
+static void *field_ptr(Trial &T, int32_t field) {
+  switch (field) {
+    case FB_FIELD_V: return T.v;
+    case FB_FIELD_GE: return T.gE;
+    case FB_FIELD_GI: return T.gI;
+    case FB_FIELD_REFR: return T.refr;
+    case FB_FIELD_TRACE: return T.trace;
+    case FB_FIELD_ADAPT: return T.adapt;
+    case FB_FIELD_RES: return T.res;
+    case FB_FIELD_BIAS: return T.bias;
+    case FB_FIELD_THR: return T.thr;
+    case FB_FIELD_DRIVE: return T.drive;
+    case FB_FIELD_SPIKECOUNT: return T.spikeCount;
+    default: return nullptr;
+  }
+}
+
+extern "C" int fb_read(fb_brains *br, int32_t field, int32_t b, void *dst) {
+  int rc = check_brain(br, b, "fb_read");
+  if (rc) return rc;
+  void *src = field_ptr(br->host[b], field);
+  if (!src || !dst) return fail(FB_EINVAL, "fb_read: bad field %d or null dst", field);
+  rc = flush(br);
+  if (rc) return rc;
+  CU(cudaMemcpyAsync(dst, src, (size_t)br->host[b].N * 4, cudaMemcpyDefault, br->stream));
+  CU(cudaStreamSynchronize(br->stream));
+  return FB_OK;
+}
+
+extern "C" int fb_write(fb_brains *br, int32_t field, int32_t b, const void *src) {
+  int rc = check_brain(br, b, "fb_write");
+  if (rc) return rc;
+  void *dst = field_ptr(br->host[b], field);
+  if (!dst || !src) return fail(FB_EINVAL, "fb_write: bad field %d or null src", field);
+  if (field == FB_FIELD_DRIVE) return fail(FB_EINVAL, "fb_write: the drive field is written through fb_set_drive, which keeps the driven set");
+  rc = flush(br);
+  if (rc) return rc;
+  CU(cudaMemcpyAsync(dst, src, (size_t)br->host[b].N * 4, cudaMemcpyDefault, br->stream));
+  CU(cudaStreamSynchronize(br->stream));
+  return FB_OK;
+}
+
+extern "C" int fb_scalars(fb_brains *br, int32_t b, int32_t *head, uint32_t *rng, int32_t *nfired,
+                          int32_t *last_slot, int32_t *n_driven, int64_t *steps_done) {
+  int rc = check_brain(br, b, "fb_scalars");
+  if (rc) return rc;
+  rc = flush(br);
+  if (rc) return rc;
+  Trial dev;
+  CU(cudaMemcpy(&dev, &br->trials[b], sizeof(Trial), cudaMemcpyDeviceToHost));
+  if (head) *head = dev.head;
+  if (rng) *rng = dev.rng;
+  if (nfired) *nfired = dev.nFired;
+  if (last_slot) *last_slot = dev.lastSlot;
+  if (n_driven) *n_driven = dev.nDriven;
+  if (steps_done) *steps_done = dev.stepsDone;
+  return FB_OK;
+}

@@ -1,0 +1,219 @@
+// Internal device structures and helpers of the GB300 brain step. Not part of the C ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/flybrain.h"
+
+namespace fb {
+
+constexpr int kBlock = 512;          // threads per block of the persistent step kernel
+constexpr int kTile = kBlock;        // neurons per update tile (one per thread)
+constexpr int kChunk = 32;           // edges per delivery work item (one per lane)
+constexpr int kBucket = 8;           // in-place contribution slots per target and step
+constexpr int kSortMax = 64;         // contributions per target sorted in local memory
+constexpr uint32_t kNil = 0xffffffffu;
+
+// Per-brain flags (Trial::flags).
+constexpr int32_t kHasBg = 1;        // background events enabled (bgEvents > 0)
+constexpr int32_t kHasDep = 2;       // synaptic depression enabled (depU != 0)
+constexpr int32_t kHasPreInh = 4;    // presynaptic inhibition (forces sequential delivery)
+
+// One brain of a batch: header constants (f32, rounded once from f64 on the host, the values
+// LIFWasm._writeHeader stores), graph and state pointers, delivery scratch, dynamic scalars.
+struct Trial {
+  int32_t N, nslots, coba, mode;
+  float dt, vRest, vThresh, vReset, tRef, adaptInc, depU, dE, dTr, dA, kRec, kM, dtS;
+  float eExc, eInh, cE, cI, bgEvents, bgAmp, preInh;
+  int32_t tileBase, nTiles, flags, pad0;
+  int64_t chunkCap;  // delivery work items per ring slot
+  // graph (shared, read-only during a step)
+  const uint32_t *indptr, *indices;
+  const float *W, *sign;
+  // state, SoA, N each
+  float *v, *gE, *gI, *refr, *trace, *adapt, *res, *bias, *thr, *drive;
+  uint32_t *spikeCount;
+  // delay ring: nslots lists of N, counts, per-arrival edge offsets (N+1 per slot), the first
+  // arrival of every 32-edge work item (chunkCap per slot), and each slot's total edge count
+  int32_t *ring, *ringCount;
+  uint32_t *ringOff, *chunkK, *slotEdges;
+  int32_t *driven;
+  // delivery scratch: contribution counts and buckets per target, overflow list heads,
+  // background hits, arrival marks
+  uint32_t *cnt;
+  uint2 *bucket;
+  uint32_t *ovfHead, *bgHits;
+  uint8_t *arrived;
+  // threshold-spike staging per update tile (compacted list + out-degree prefix)
+  int32_t *stage;
+  uint32_t *stageDeg;
+  int32_t *tileCnt;
+  uint32_t *tileDeg;
+  // optional per-step log of fired counts and fired lists
+  int32_t *logCount;
+  int32_t *logRaster;
+  int64_t logCap, logRasterCap;
+  // dynamic scalars (device-written)
+  uint32_t rng;
+  int32_t head;
+  float bgAcc;
+  int32_t nDriven;
+  int32_t nFired, lastSlot;
+  int32_t nForced[2];     // driven spikes of the step, by step parity
+  uint32_t forcedDeg[2];  // their total out-degree
+  int64_t stepsDone;
+  int64_t logStart;       // first logged step (global step index)
+  int64_t logRasterLen[2];
+};
+
+// Overflow record of a target that received more than kBucket contributions in one step.
+struct OvfRec {
+  uint32_t key, bits, next, pad;
+};
+
+struct StepArgs {
+  Trial *trials;
+  int32_t B, maxSteps;
+  const int32_t *steps;      // per-brain steps of this launch
+  const int32_t *tileTrial;  // update tile -> brain
+  int32_t nTilesTotal, pad0;
+  const uint32_t *jump;      // xorshift32 jump tables [32][8][16]
+  uint32_t *barCount, *barGen;
+  int32_t *err;
+  OvfRec *ovf[2];
+  uint32_t *ovfTop;          // [2]
+  uint32_t ovfCap;
+  int32_t log;               // 1: record per-step fired counts / lists
+  int64_t timeoutNs;
+};
+
+// ---- memory helpers --------------------------------------------------------------------------
+// Data written by other blocks during the same launch is read through L2 (ld.global.cg): L1 is
+// not coherent across SMs.
+template <typename T>
+__device__ __forceinline__ T ldcg(const T *p) { return __ldcg(p); }
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int32_t ld_volatile(const int32_t *p) {
+  return *(const volatile int32_t *)p;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier for a co-resident (cooperative) grid. Every wait is bounded: by time
+// (timeoutNs, %globaltimer) and by an iteration cap. On a timeout the waiter records
+// FB_ETIMEOUT in *err and returns false; every block returns false once *err is set, so all
+// blocks leave the kernel at the same barrier.
+__device__ __forceinline__ bool grid_sync(const StepArgs &a) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const uint32_t gen = ld_acquire(a.barGen);
+    __threadfence();
+    const uint32_t prev = atomicAdd(a.barCount, 1u);
+    if (prev == gridDim.x - 1) {
+      atomicExch(a.barCount, 0u);
+      __threadfence();
+      st_release(a.barGen, gen + 1);
+    } else {
+      const uint64_t t0 = global_ns();
+      uint32_t it = 0;
+      while (ld_acquire(a.barGen) == gen) {
+        ++it;
+        if ((it & 255u) == 0) {
+          if (ld_volatile(a.err) != 0) { ok = 0; break; }
+          if (global_ns() - t0 > (uint64_t)a.timeoutNs || it > (1u << 30)) {
+            atomicCAS(a.err, 0, FB_ETIMEOUT);
+            ok = 0;
+            break;
+          }
+        }
+      }
+    }
+    __threadfence();
+    if (ok && ld_volatile(a.err) != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---- xorshift32 ------------------------------------------------------------------------------
+// lif.c's generator (src/wasm/lif.c:27). It is linear over GF(2): the state after d draws is
+// M^d s. jump[j] holds M^(2^j) as 8 nibble tables of 16 words, so applying it costs 8 lookups.
+__device__ __forceinline__ uint32_t xs_next(uint32_t x) {
+  x ^= x << 13;
+  x ^= x >> 17;
+  x ^= x << 5;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t xs_apply(const uint32_t *tab, uint32_t x) {
+  uint32_t y = 0;
+#pragma unroll
+  for (int n = 0; n < 8; n++) y ^= __ldg(tab + n * 16 + ((x >> (4 * n)) & 15u));
+  return y;
+}
+
+// State after d draws from s.
+__device__ __forceinline__ uint32_t xs_jump(const uint32_t *jump, uint32_t s, uint32_t d) {
+  while (d) {
+    const int j = __ffs(d) - 1;
+    s = xs_apply(jump + j * 128, s);
+    d &= d - 1;
+  }
+  return s;
+}
+
+// ---- block scans -----------------------------------------------------------------------------
+// Exclusive prefix over the block (blockDim.x a multiple of 32, <= 1024). *total receives the
+// block sum. Uses scratch[32].
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T x, T *total, T *scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  T inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  __syncthreads();
+  if (lane == 31) scratch[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < nw ? scratch[lane] : T(0);
+    T wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < nw) scratch[lane] = wi - w;
+    if (lane == 31) scratch[32] = wi;
+  }
+  __syncthreads();
+  const T res = scratch[warp] + inc - x;
+  *total = scratch[32];
+  __syncthreads();
+  return res;
+}
+
+// Write the "first arrival" index k into every delivery work item that starts inside arrival
+// k's edge range [o, o + deg).
+__device__ __forceinline__ void mark_chunks(uint32_t *chunkK, uint32_t o, uint32_t deg, uint32_t k) {
+  const uint32_t end = o + deg;
+  for (uint32_t c = (o + kChunk - 1) / kChunk; c * kChunk < end; c++) chunkK[c] = k;
+}
+
+}  // namespace fb

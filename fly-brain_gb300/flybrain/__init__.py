@@ -1,0 +1,14 @@
+"""GB300-native brain step of the fly connectome LIF model (the reference's lif_step + LIFDiff).
+
+Public surface:
+  LIFCuda, BrainBatch, DeviceGraph   -- the LIFWasm brain-model API on the sm_103a kernels
+  synth_graph, drive_set, workload   -- seeded synthetic connectome-shaped workloads
+  build                               -- compile libflybrain.so in-tree (nvcc, sm_103a)
+"""
+from .builder import build
+from .synth import Graph, SYNTH_PARAMS, drive_set, synth_graph, workload
+from .brain import DEFAULTS, BrainBatch, DeviceGraph, LIFCuda
+from . import _native
+
+__all__ = ["build", "Graph", "SYNTH_PARAMS", "drive_set", "synth_graph", "workload", "DEFAULTS",
+           "BrainBatch", "DeviceGraph", "LIFCuda", "_native"]

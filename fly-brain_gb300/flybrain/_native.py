@@ -1,0 +1,106 @@
+"""ctypes binding of libflybrain.so (include/flybrain.h).
+
+The library is the only compute path: if it is missing or fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import builder as _build
+
+FB_OK = 0
+FB_EINVAL, FB_ECUDA, FB_ENOMEM, FB_ETIMEOUT, FB_EOVERFLOW, FB_ESTATE, FB_ENODEV = -1, -2, -3, -4, -5, -6, -7
+FB_DELIVER_EXACT, FB_DELIVER_SEQUENTIAL, FB_DELIVER_FAST = 0, 1, 2
+FIELDS = {"v": 0, "gE": 1, "gI": 2, "refr": 3, "trace": 4, "adapt": 5, "res": 6, "bias": 7,
+          "thr": 8, "drive": 9, "spikeCount": 10}
+
+# Every symbol the header declares, with its ctypes signature (restype, argtypes).
+P, I32, I64, U32, D = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32, C.c_double
+PI32, PI64, PU32, PF = C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_uint32), C.POINTER(C.c_float)
+
+
+class FbParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in (
+        "dt", "vRest", "vThresh", "vReset", "tauM", "tauSyn", "tRef", "delay", "traceTau",
+        "adaptInc", "adaptTau", "depU", "depTau", "eExc", "eInh", "bgRate", "bgAmp", "preInh")] + [
+        ("coba", C.c_int32), ("reserved", C.c_int32)]
+
+
+SIGNATURES = {
+    "fb_version": (C.c_int, []),
+    "fb_last_error": (C.c_char_p, []),
+    "fb_device_info": (C.c_int, [PI32, PI32, PI32]),
+    "fb_default_params": (None, [C.POINTER(FbParams)]),
+    "fb_graph_create": (C.c_int, [I32, I64, P, P, P, P, C.POINTER(P)]),
+    "fb_graph_create_shared": (C.c_int, [P, P, P, C.POINTER(P)]),
+    "fb_graph_set_sign": (C.c_int, [P, P]),
+    "fb_graph_info": (C.c_int, [P, PI32, PI64]),
+    "fb_graph_destroy": (C.c_int, [P]),
+    "fb_brains_create": (C.c_int, [P, I32, C.POINTER(FbParams), I32, P, C.POINTER(P)]),
+    "fb_brains_destroy": (C.c_int, [P]),
+    "fb_brains_set_mode": (C.c_int, [P, I32]),
+    "fb_step": (C.c_int, [P, I32, P]),
+    "fb_step_uneven": (C.c_int, [P, P, P]),
+    "fb_record": (C.c_int, [P, I32, I64]),
+    "fb_spike_log": (C.c_int, [P, I32, P, I32, P, I64, PI64, PI64]),
+    "fb_fired": (C.c_int, [P, I32, P, I32, PI32]),
+    "fb_set_drive": (C.c_int, [P, I32, P, P, I32]),
+    "fb_set_bias": (C.c_int, [P, I32, P, P, I32]),
+    "fb_set_thr": (C.c_int, [P, I32, P, P, I32]),
+    "fb_add_g": (C.c_int, [P, I32, P, P, P, I32]),
+    "fb_pulse": (C.c_int, [P, I32, P, P, I32]),
+    "fb_reset": (C.c_int, [P, I32]),
+    "fb_set_background": (C.c_int, [P, I32, D, D]),
+    "fb_read": (C.c_int, [P, I32, I32, P]),
+    "fb_write": (C.c_int, [P, I32, I32, P]),
+    "fb_scalars": (C.c_int, [P, I32, PI32, PU32, PI32, PI32, PI32, PI64]),
+    "fb_last_step_ms": (C.c_int, [P, PF]),
+}
+
+
+class FlyBrainError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads libflybrain.so (building it first if absent); raises if that is impossible."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise FlyBrainError(FB_ENODEV, f"{path} is not built")
+        _build.build()
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != FB_OK:
+        msg = load().fb_last_error()
+        raise FlyBrainError(rc, msg.decode() if msg else "")
+
+
+def ptr(a) -> C.c_void_p:
+    """Address of a contiguous numpy array, or of a torch tensor (host or device)."""
+    if a is None:
+        return C.c_void_p(0)
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)

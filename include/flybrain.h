@@ -1,0 +1,176 @@
+/*
+ * flybrain.h -- C ABI of the GB300 brain step (connectome LIF network + its adjoint).
+ *
+ * This is the drop-in boundary for the reference's brain-model API: the LIFWasm object of
+ * src/lifwasm.js:36-87 (and its WebGPU twin LIFGpu, src/lifgpu.js:183-370), which wraps the native
+ * kernel `int32_t lif_step(Brain*)` of src/wasm/lif.c:29-80, plus the LIFDiff adjoint of
+ * src/lifdiff.js:219-686. Every entry point takes plain pointers and sizes; no C++ or torch types
+ * cross it. Array arguments may be host or device pointers (copies use unified addressing).
+ *
+ * Conventions
+ *   - Every function returns an int status: FB_OK (0) or a negative FB_E* code. The message of the
+ *     last failure on the calling thread is fb_last_error(). Nothing throws across the ABI.
+ *   - A graph is read-only and may be shared by many brain batches (src/brainsetup.js:10-28 shares
+ *     one connectome across flies), except for its sign vector (fb_graph_set_sign).
+ *   - A brain batch holds B independent brains (trials), each with its own state block, seed,
+ *     drive set and graph. Brain b of a batch is what one LIFWasm instance is in the reference.
+ *   - Setters (drive, bias, thr, addG, pulse) are queued and applied in call order before the next
+ *     step or read, so a read always observes every earlier write, as with LIFWasm's shared memory.
+ *   - Handles are not thread-safe: use one handle per host thread (the reference runs one brain per
+ *     worker thread).
+ */
+#ifndef FLYBRAIN_H
+#define FLYBRAIN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FB_OK 0
+#define FB_EINVAL -1     /* bad argument (size, index, null pointer, malformed CSR) */
+#define FB_ECUDA -2      /* a CUDA runtime call failed (message names it) */
+#define FB_ENOMEM -3     /* device allocation failed */
+#define FB_ETIMEOUT -4   /* a device-side wait exceeded its limit; the step was abandoned */
+#define FB_EOVERFLOW -5  /* per-step delivery scratch overflowed; state of that step is invalid */
+#define FB_ESTATE -6     /* call not valid in the handle's current state */
+#define FB_ENODEV -7     /* no CUDA device, or not an sm_103 device */
+
+typedef struct fb_graph fb_graph;   /* opaque: one compiled connectome on the device */
+typedef struct fb_brains fb_brains; /* opaque: a batch of B brains on the device */
+
+/* Model parameters of one brain. Field meaning and units follow DEFAULTS of src/lif.js:6-15 (times
+ * in ms, potentials in mV, rates in Hz). The derived f32 header constants (decays, kM, dtS, cE, cI,
+ * background events per step) are computed from these in double and rounded once, as
+ * LIFWasm._writeHeader does (src/lifwasm.js:55-68). */
+typedef struct fb_params {
+  double dt, vRest, vThresh, vReset, tauM, tauSyn, tRef, delay;
+  double traceTau, adaptInc, adaptTau, depU, depTau;
+  double eExc, eInh, bgRate, bgAmp, preInh;
+  int32_t coba; /* 0: current-based (lif.c:65-71), 1: conductance-based (lif.c:55-63) */
+  int32_t reserved;
+} fb_params;
+
+/* Fills *p with DEFAULTS of src/lif.js:6-15. */
+void fb_default_params(fb_params *p);
+
+/* Delivery modes of fb_brains_set_mode. */
+#define FB_DELIVER_EXACT 0      /* default: per-target sums in the reference's order (bit-exact) */
+#define FB_DELIVER_SEQUENTIAL 1 /* arrivals one by one; exact also with preInh > 0 (slow) */
+#define FB_DELIVER_FAST 2       /* float atomics: statistical parity only */
+
+/* Readable / writable per-neuron fields of fb_read / fb_write. */
+#define FB_FIELD_V 0
+#define FB_FIELD_GE 1
+#define FB_FIELD_GI 2
+#define FB_FIELD_REFR 3
+#define FB_FIELD_TRACE 4
+#define FB_FIELD_ADAPT 5
+#define FB_FIELD_RES 6
+#define FB_FIELD_BIAS 7
+#define FB_FIELD_THR 8
+#define FB_FIELD_DRIVE 9
+#define FB_FIELD_SPIKECOUNT 10 /* uint32 */
+#define FB_NFIELDS 11
+
+/* Library and error reporting. */
+int fb_version(void);             /* 10000 * major + 100 * minor + patch */
+const char *fb_last_error(void);  /* thread-local message of the last failure ("" if none) */
+int fb_device_info(int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor);
+
+/* ---- graphs ------------------------------------------------------------------------------- */
+
+/* Uploads a compiled CSR connectome: the arrays writeGraph lays out (src/lifwasm.js:14-34):
+ * indptr u32[N+1], indices u32[E], weights f32[E], sign f32[N] (sign already carries wSyn).
+ * Rows must not repeat a target (the reference's graph files merge (pre, post) pairs). */
+int fb_graph_create(int32_t N, int64_t E, const uint32_t *indptr, const uint32_t *indices,
+                    const float *weights, const float *sign, fb_graph **out);
+
+/* A second graph over the same topology (indptr/indices shared on the device, not copied) with its
+ * own weights and sign: per-trial type gains bake into weights as writeGraph's outScale does
+ * (src/lifwasm.js:23,31). */
+int fb_graph_create_shared(const fb_graph *topology, const float *weights, const float *sign,
+                           fb_graph **out);
+
+/* Replaces the sign vector, f32[N]. Replaces the direct write into graph.sign that
+ * src/sim/neuromod.js:107 performs through brain.mem; every brain on this graph sees it. */
+int fb_graph_set_sign(fb_graph *g, const float *sign);
+
+/* N and E of a graph. */
+int fb_graph_info(const fb_graph *g, int32_t *N, int64_t *E);
+
+int fb_graph_destroy(fb_graph *g);
+
+/* ---- brain batches (the LIFWasm surface) -------------------------------------------------- */
+
+/* Creates B brains. graphs[b], params[b], seeds[b] per brain (params may be a single struct when
+ * params_stride == 0). Each brain starts as `new LIFWasm(...)` leaves it (src/lifwasm.js:37-53):
+ * state at rest, bias/thr/drive zero, head 0, RNG state (seed * 2654435761) >>> 0 || 1. */
+int fb_brains_create(const fb_graph *const *graphs, int32_t B, const fb_params *params,
+                     int32_t params_stride, const uint32_t *seeds, fb_brains **out);
+int fb_brains_destroy(fb_brains *br);
+
+/* Delivery mode for all brains of the batch (FB_DELIVER_*). */
+int fb_brains_set_mode(fb_brains *br, int32_t mode);
+
+/* Advances every brain by nsteps steps in one persistent launch (lif_step, src/wasm/lif.c:29-80,
+ * nsteps times). out_nfired (optional, int32[B]) receives each brain's fired count of its last
+ * step: the value lif_step returns. */
+int fb_step(fb_brains *br, int32_t nsteps, int32_t *out_nfired);
+
+/* Uneven batch: brain b advances steps[b] steps (0 leaves it untouched), all in one launch. */
+int fb_step_uneven(fb_brains *br, const int32_t *steps, int32_t *out_nfired);
+
+/* Records, from the next step on, every step's fired count and fired list (ring order) of every
+ * brain into device logs of cap_steps counts and cap_spikes indices per brain; fb_spike_log reads
+ * brain b's log back (*n_steps, *n_spikes: totals recorded, which may exceed the caps given to
+ * either call). fb_record(br, 0, 0) stops recording and frees the logs. */
+int fb_record(fb_brains *br, int32_t cap_steps, int64_t cap_spikes);
+int fb_spike_log(fb_brains *br, int32_t b, int32_t *counts, int32_t cap_steps, int32_t *raster,
+                 int64_t cap_spikes, int64_t *n_steps, int64_t *n_spikes);
+
+/* Fired list of brain b's last step, in ring order (driven spikes first, in driven-list order,
+ * then threshold spikes in ascending index): the view LIFWasm.step returns
+ * (src/lifwasm.js:83-84). *n receives the count; at most cap indices are copied. */
+int fb_fired(fb_brains *br, int32_t b, int32_t *dst, int32_t cap, int32_t *n);
+
+/* Injections, queued in call order and applied before the next step or read.
+ * fb_set_drive: drive[idx[k]] = hz[k]; a positive rate appends the neuron to the driven set if
+ *   absent, zero or negative removes it -- the insertion-ordered set of src/lifwasm.js:70-72,
+ *   which fixes the RNG draw order. (setDriveOne / setDrive)
+ * fb_set_bias: bias[idx[k]] = mv[k] (setBias, src/lifwasm.js:73)
+ * fb_set_thr:  thr[idx[k]] = mv[k]  (setThr, :74)
+ * fb_add_g:    gE[idx[k]] += e[k]; gI[idx[k]] += i[k], each sum formed in double and rounded once
+ *              as a JS Float32Array store rounds (addG, :75)
+ * fb_pulse:    gE[idx[k]] += mv[k], same rounding (pulse, :76) */
+int fb_set_drive(fb_brains *br, int32_t b, const int32_t *idx, const double *hz, int32_t n);
+int fb_set_bias(fb_brains *br, int32_t b, const int32_t *idx, const double *mv, int32_t n);
+int fb_set_thr(fb_brains *br, int32_t b, const int32_t *idx, const double *mv, int32_t n);
+int fb_add_g(fb_brains *br, int32_t b, const int32_t *idx, const double *e, const double *i,
+             int32_t n);
+int fb_pulse(fb_brains *br, int32_t b, const int32_t *idx, const double *mv, int32_t n);
+
+/* State back to rest (src/lifwasm.js:78): v = vRest, gE = gI = refr = trace = adapt = 0, res = 1,
+ * spikeCount = 0, ring counts 0. The ring head, RNG and background accumulator are kept, and
+ * bias/thr/drive untouched, exactly as the reference. b == -1 resets every brain. */
+int fb_reset(fb_brains *br, int32_t b);
+
+/* Background synaptic events (setBackground, src/lifwasm.js:69). */
+int fb_set_background(fb_brains *br, int32_t b, double rate_hz, double amp_mv);
+
+/* Copies field (FB_FIELD_*) of brain b, N elements of 4 bytes, into dst / from src. */
+int fb_read(fb_brains *br, int32_t field, int32_t b, void *dst);
+int fb_write(fb_brains *br, int32_t field, int32_t b, const void *src);
+
+/* Scalars of brain b: head, RNG state, last fired count, last slot, driven-set size, t in steps. */
+int fb_scalars(fb_brains *br, int32_t b, int32_t *head, uint32_t *rng, int32_t *nfired,
+               int32_t *last_slot, int32_t *n_driven, int64_t *steps_done);
+
+/* Device-side timing of the last fb_step launch (ms, CUDA events on the launch stream). */
+int fb_last_step_ms(fb_brains *br, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLYBRAIN_H */
