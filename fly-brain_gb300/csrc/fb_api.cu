@@ -16,6 +16,7 @@
 
 namespace fb {
 int step_kernel_blocks_per_sm(size_t smem);
+size_t step_smem_bytes(int B);
 cudaError_t launch_step(const StepArgs &a, int grid, size_t smem, cudaStream_t st);
 struct Delta {
   int32_t brain, field, idx, pad;
@@ -294,7 +295,10 @@ struct fb_brains {
   int32_t *d_tileTrial = nullptr, *d_steps = nullptr, *d_err = nullptr, *d_groups = nullptr;
   Delta *d_deltas = nullptr;
   size_t deltaCap = 0, groupCap = 0;
-  uint32_t *d_bar = nullptr;   // [count, gen]
+  uint32_t *d_bar = nullptr;   // the grid barrier's counter word (own 128-byte line)
+  static constexpr size_t kBarWords = 32;
+  unsigned long long *d_phase = nullptr;  // per-phase ns accumulators when profiling
+  int profiling = 0;
   OvfRec *d_ovf[2] = {nullptr, nullptr};
   uint32_t *d_ovfTop = nullptr;
   uint32_t ovfCap = 0;
@@ -393,19 +397,24 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     T.indices = g->topo->indices;
     T.W = g->W;
     T.sign = g->sign;
-    T.rng = seed_state(seeds[b]);
+    T.rngP[0] = seed_state(seeds[b]);
+    T.maxDch = std::max(1, (N + kBlock - 1) / kBlock);
     // arena layout
     const size_t n4 = align256((size_t)N * 4);
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes); return o; };
     size_t o_state = take(n4 * 11);
     size_t o_ring = take((size_t)ns * N * 4), o_ringCount = take((size_t)ns * 4);
-    size_t o_ringOff = take((size_t)ns * (N + 1) * 4), o_chunkK = take((size_t)ns * T.chunkCap * 4);
+    size_t o_ringOff = take((size_t)ns * (N + 1) * 4), o_chunkK = take((size_t)ns * T.chunkCap * 16);
+    size_t o_ringRow = take((size_t)ns * N * 4);
     size_t o_slotEdges = take((size_t)ns * 4), o_driven = take((size_t)N * 4);
     size_t o_cnt = take((size_t)N * 4), o_bucket = take((size_t)N * kBucket * 8);
     size_t o_ovfHead = take((size_t)N * 4), o_bg = take((size_t)N * 4), o_arr = take((size_t)N);
     size_t o_stage = take((size_t)T.nTiles * kTile * 4), o_stageDeg = take((size_t)T.nTiles * kTile * 4);
     size_t o_tileCnt = take((size_t)T.nTiles * 4), o_tileDeg = take((size_t)T.nTiles * 4);
+    size_t o_dStage = take((size_t)2 * T.maxDch * kBlock * 4), o_dStageDeg = take((size_t)2 * T.maxDch * kBlock * 4);
+    size_t o_dCnt = take((size_t)2 * T.maxDch * 4), o_dDeg = take((size_t)2 * T.maxDch * 4);
+    size_t o_live = take((size_t)T.maxDch * 8);
     char *base = nullptr;
     if (cudaMalloc(&base, off) != cudaSuccess)
       return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: brain %d: %zu bytes of device memory", b, off));
@@ -420,13 +429,17 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     T.bias = (float *)((char *)st + 7 * n4); T.thr = (float *)((char *)st + 8 * n4);
     T.drive = (float *)((char *)st + 9 * n4); T.spikeCount = (uint32_t *)((char *)st + 10 * n4);
     T.ring = (int32_t *)(base + o_ring); T.ringCount = (int32_t *)(base + o_ringCount);
-    T.ringOff = (uint32_t *)(base + o_ringOff); T.chunkK = (uint32_t *)(base + o_chunkK);
+    T.ringOff = (uint32_t *)(base + o_ringOff); T.chunkK = (uint4 *)(base + o_chunkK);
+    T.ringRow = (uint32_t *)(base + o_ringRow);
     T.slotEdges = (uint32_t *)(base + o_slotEdges); T.driven = (int32_t *)(base + o_driven);
     T.cnt = (uint32_t *)(base + o_cnt); T.bucket = (uint2 *)(base + o_bucket);
     T.ovfHead = (uint32_t *)(base + o_ovfHead); T.bgHits = (uint32_t *)(base + o_bg);
     T.arrived = (uint8_t *)(base + o_arr);
     T.stage = (int32_t *)(base + o_stage); T.stageDeg = (uint32_t *)(base + o_stageDeg);
     T.tileCnt = (int32_t *)(base + o_tileCnt); T.tileDeg = (uint32_t *)(base + o_tileDeg);
+    T.dStage = (int32_t *)(base + o_dStage); T.dStageDeg = (uint32_t *)(base + o_dStageDeg);
+    T.dCnt = (int32_t *)(base + o_dCnt); T.dDeg = (uint32_t *)(base + o_dDeg);
+    T.liveTag = (unsigned long long *)(base + o_live);
     br->driven[b].init(N);
   }
   // batch-wide buffers
@@ -435,7 +448,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
       cudaMalloc(&br->d_tileTrial, sizeof(int32_t) * nTiles) != cudaSuccess ||
       cudaMalloc(&br->d_steps, sizeof(int32_t) * B) != cudaSuccess ||
       cudaMalloc(&br->d_err, sizeof(int32_t)) != cudaSuccess ||
-      cudaMalloc(&br->d_bar, sizeof(uint32_t) * 2) != cudaSuccess ||
+      cudaMalloc(&br->d_bar, sizeof(uint32_t) * fb_brains::kBarWords) != cudaSuccess ||
       cudaMalloc(&br->d_ovfTop, sizeof(uint32_t) * 2) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: batch buffers"));
   // overflow pool: 1M records per parity plus one per 16 edges of the largest graph
@@ -446,7 +459,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     if (cudaMalloc(&br->d_ovf[k], sizeof(OvfRec) * (size_t)br->ovfCap) != cudaSuccess)
       return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: overflow pool"));
   if (cudaMemsetAsync(br->d_err, 0, 4, br->stream) != cudaSuccess ||
-      cudaMemsetAsync(br->d_bar, 0, 8, br->stream) != cudaSuccess ||
+      cudaMemsetAsync(br->d_bar, 0, sizeof(uint32_t) * fb_brains::kBarWords, br->stream) != cudaSuccess ||
       cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream) != cudaSuccess ||
       cudaMemcpyAsync(br->d_tileTrial, br->tileTrial.data(), sizeof(int32_t) * nTiles, cudaMemcpyHostToDevice, br->stream) != cudaSuccess ||
       cudaMemcpyAsync(br->trials, br->host.data(), sizeof(Trial) * B, cudaMemcpyHostToDevice, br->stream) != cudaSuccess)
@@ -454,7 +467,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
   if (launch_reset(br->trials, 0, B, br->stream) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: reset launch failed"));
   // persistent grid: every SM, as many blocks as stay co-resident
-  br->smem = sizeof(int32_t) * (size_t)(4 * B + 1);
+  br->smem = step_smem_bytes(B);
   if (br->smem > 48 * 1024 && set_step_smem(br->smem) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ECUDA, "step kernel: %zu bytes of shared memory refused", br->smem));
   int sms = 0;
@@ -480,6 +493,7 @@ extern "C" int fb_brains_destroy(fb_brains *br) {
   for (void *p : br->arenas) cudaFree(p);
   cudaFree(br->trials); cudaFree(br->d_tileTrial); cudaFree(br->d_steps); cudaFree(br->d_err);
   cudaFree(br->d_groups); cudaFree(br->d_deltas); cudaFree(br->d_bar); cudaFree(br->d_ovfTop);
+  cudaFree(br->d_phase);
   cudaFree(br->d_ovf[0]); cudaFree(br->d_ovf[1]);
   if (br->ev0) cudaEventDestroy(br->ev0);
   if (br->ev1) cudaEventDestroy(br->ev1);
@@ -643,7 +657,7 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     a.nTilesTotal = (int32_t)br->tileTrial.size();
     a.jump = br->jump;
     a.barCount = br->d_bar;
-    a.barGen = br->d_bar + 1;
+    a.phaseNs = br->profiling ? br->d_phase : nullptr;
     a.err = br->d_err;
     a.ovf[0] = br->d_ovf[0];
     a.ovf[1] = br->d_ovf[1];
@@ -661,7 +675,7 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     if (err) {
       // leave the handle launchable: clear the flag, the barrier and the overflow pool
       cudaMemsetAsync(br->d_err, 0, 4, br->stream);
-      cudaMemsetAsync(br->d_bar, 0, 8, br->stream);
+      cudaMemsetAsync(br->d_bar, 0, sizeof(uint32_t) * fb_brains::kBarWords, br->stream);
       cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream);
       cudaStreamSynchronize(br->stream);
       return fail(err, err == FB_ETIMEOUT ? "fb_step: a device-side wait timed out; the step was abandoned"
@@ -822,10 +836,30 @@ extern "C" int fb_scalars(fb_brains *br, int32_t b, int32_t *head, uint32_t *rng
   Trial dev;
   CU(cudaMemcpy(&dev, &br->trials[b], sizeof(Trial), cudaMemcpyDeviceToHost));
   if (head) *head = dev.head;
-  if (rng) *rng = dev.rng;
+  if (rng) *rng = dev.rngP[dev.stepsDone & 1];
   if (nfired) *nfired = dev.nFired;
   if (last_slot) *last_slot = dev.lastSlot;
   if (n_driven) *n_driven = dev.nDriven;
   if (steps_done) *steps_done = dev.stepsDone;
+  return FB_OK;
+}
+
+extern "C" int fb_profile(fb_brains *br, int32_t on) {
+  if (!br) return fail(FB_EINVAL, "fb_profile: null handle");
+  if (!br->d_phase) CU(cudaMalloc(&br->d_phase, sizeof(unsigned long long) * FB_NPHASES));
+  CU(cudaMemsetAsync(br->d_phase, 0, sizeof(unsigned long long) * FB_NPHASES, br->stream));
+  CU(cudaStreamSynchronize(br->stream));
+  br->profiling = on ? 1 : 0;
+  return FB_OK;
+}
+
+extern "C" int fb_phase_times(fb_brains *br, double *ms, int32_t n) {
+  if (!br || !ms) return fail(FB_EINVAL, "fb_phase_times: null argument");
+  unsigned long long ns[FB_NPHASES] = {0};
+  if (br->d_phase) {
+    CU(cudaStreamSynchronize(br->stream));
+    CU(cudaMemcpy(ns, br->d_phase, sizeof ns, cudaMemcpyDeviceToHost));
+  }
+  for (int k = 0; k < n && k < FB_NPHASES; k++) ms[k] = ns[k] * 1e-6;
   return FB_OK;
 }

@@ -8,7 +8,9 @@
 namespace fb {
 
 constexpr int kBlock = 512;          // threads per block of the persistent step kernel
-constexpr int kTile = kBlock;        // neurons per update tile (one per thread)
+constexpr int kNPT = 2;              // neurons per thread in the update phase
+constexpr int kTile = kBlock * kNPT; // neurons per update tile
+constexpr int kDrivenPer = 8;        // driven-list entries per thread and round
 constexpr int kChunk = 32;           // edges per delivery work item (one per lane)
 constexpr int kBucket = 8;           // in-place contribution slots per target and step
 constexpr int kSortMax = 64;         // contributions per target sorted in local memory
@@ -33,10 +35,12 @@ struct Trial {
   // state, SoA, N each
   float *v, *gE, *gI, *refr, *trace, *adapt, *res, *bias, *thr, *drive;
   uint32_t *spikeCount;
-  // delay ring: nslots lists of N, counts, per-arrival edge offsets (N+1 per slot), the first
-  // arrival of every 32-edge work item (chunkCap per slot), and each slot's total edge count
+  // delay ring: nslots lists of N, counts, per-arrival edge offsets (N+1 per slot) and row starts
+  // (N per slot), each slot's total edge count, and per 32-edge delivery work item (chunkCap per
+  // slot) its first arrival: {rank k, presynaptic neuron, end of k's edges, row start - offset}
   int32_t *ring, *ringCount;
-  uint32_t *ringOff, *chunkK, *slotEdges;
+  uint32_t *ringOff, *ringRow, *slotEdges;
+  uint4 *chunkK;
   int32_t *driven;
   // delivery scratch: contribution counts and buckets per target, overflow list heads,
   // background hits, arrival marks
@@ -49,18 +53,26 @@ struct Trial {
   uint32_t *stageDeg;
   int32_t *tileCnt;
   uint32_t *tileDeg;
+  // forced-spike staging per driven-list chunk of kBlock entries, two step parities:
+  // dStage/dStageDeg [2][maxDch * kBlock], dCnt/dDeg [2][maxDch]; liveTag[maxDch] publishes each
+  // chunk's count of non-refractory entries (high word: step + 1) for the chunks after it
+  int32_t *dStage;
+  uint32_t *dStageDeg;
+  int32_t *dCnt;
+  uint32_t *dDeg;
+  unsigned long long *liveTag;
+  int32_t maxDch, pad1;
   // optional per-step log of fired counts and fired lists
   int32_t *logCount;
   int32_t *logRaster;
   int64_t logCap, logRasterCap;
-  // dynamic scalars (device-written)
-  uint32_t rng;
+  // dynamic scalars (device-written). The RNG state and background accumulator at the start of
+  // global step g are rngP[g & 1] and bgAccP[g & 1]; step g writes the other halves.
+  uint32_t rngP[2];
+  float bgAccP[2];
   int32_t head;
-  float bgAcc;
   int32_t nDriven;
   int32_t nFired, lastSlot;
-  int32_t nForced[2];     // driven spikes of the step, by step parity
-  uint32_t forcedDeg[2];  // their total out-degree
   int64_t stepsDone;
   int64_t logStart;       // first logged step (global step index)
   int64_t logRasterLen[2];
@@ -78,7 +90,8 @@ struct StepArgs {
   const int32_t *tileTrial;  // update tile -> brain
   int32_t nTilesTotal, pad0;
   const uint32_t *jump;      // xorshift32 jump tables [32][8][16]
-  uint32_t *barCount, *barGen;
+  uint32_t *barCount;         // the barrier word
+  unsigned long long *phaseNs;  // optional per-phase time accumulators (null: off)
   int32_t *err;
   OvfRec *ovf[2];
   uint32_t *ovfTop;          // [2]
@@ -110,34 +123,37 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Grid-wide barrier for a co-resident (cooperative) grid. Every wait is bounded: by time
-// (timeoutNs, %globaltimer) and by an iteration cap. On a timeout the waiter records
-// FB_ETIMEOUT in *err and returns false; every block returns false once *err is set, so all
-// blocks leave the kernel at the same barrier.
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier for a co-resident (cooperative) grid on one counter word: block 0 adds
+// 0x80000000 - (grid - 1), every other block adds 1, so bit 31 of the word flips exactly when the
+// last block arrives (sense reversal by overflow: the word never needs resetting). A block waits
+// until bit 31 differs from the value its own arrival returned. Every wait is bounded, by
+// %globaltimer (timeoutNs) and by an iteration cap: a waiter that gives up records FB_ETIMEOUT in
+// *err and returns false; every block returns false once *err is set, so all blocks leave the
+// kernel at the same barrier.
 __device__ __forceinline__ bool grid_sync(const StepArgs &a) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const uint32_t gen = ld_acquire(a.barGen);
+    const uint32_t add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
     __threadfence();
-    const uint32_t prev = atomicAdd(a.barCount, 1u);
-    if (prev == gridDim.x - 1) {
-      atomicExch(a.barCount, 0u);
-      __threadfence();
-      st_release(a.barGen, gen + 1);
-    } else {
-      const uint64_t t0 = global_ns();
-      uint32_t it = 0;
-      while (ld_acquire(a.barGen) == gen) {
-        ++it;
-        if ((it & 255u) == 0) {
-          if (ld_volatile(a.err) != 0) { ok = 0; break; }
-          if (global_ns() - t0 > (uint64_t)a.timeoutNs || it > (1u << 30)) {
-            atomicCAS(a.err, 0, FB_ETIMEOUT);
-            ok = 0;
-            break;
-          }
+    const uint32_t old = atomicAdd(a.barCount, add);
+    const uint64_t t0 = global_ns();
+    uint32_t it = 0;
+    while (((ld_relaxed(a.barCount) ^ old) & 0x80000000u) == 0) {
+      ++it;
+      if ((it & 63u) == 0) {
+        if (ld_volatile(a.err) != 0) { ok = 0; break; }
+        if (global_ns() - t0 > (uint64_t)a.timeoutNs || it > (1u << 30)) {
+          atomicCAS(a.err, 0, FB_ETIMEOUT);
+          ok = 0;
+          break;
         }
       }
     }
@@ -162,7 +178,7 @@ __device__ __forceinline__ uint32_t xs_next(uint32_t x) {
 __device__ __forceinline__ uint32_t xs_apply(const uint32_t *tab, uint32_t x) {
   uint32_t y = 0;
 #pragma unroll
-  for (int n = 0; n < 8; n++) y ^= __ldg(tab + n * 16 + ((x >> (4 * n)) & 15u));
+  for (int n = 0; n < 8; n++) y ^= tab[n * 16 + ((x >> (4 * n)) & 15u)];
   return y;
 }
 
@@ -209,11 +225,34 @@ __device__ __forceinline__ T block_exclusive_scan(T x, T *total, T *scratch) {
   return res;
 }
 
+// Sum over the block; every thread receives it. Uses scratch[33].
+template <typename T>
+__device__ __forceinline__ T block_sum(T x, T *scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < nw ? scratch[lane] : T(0);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (lane == 0) scratch[32] = w;
+  }
+  __syncthreads();
+  const T r = scratch[32];
+  __syncthreads();
+  return r;
+}
+
 // Write the "first arrival" index k into every delivery work item that starts inside arrival
 // k's edge range [o, o + deg).
-__device__ __forceinline__ void mark_chunks(uint32_t *chunkK, uint32_t o, uint32_t deg, uint32_t k) {
+__device__ __forceinline__ void mark_chunks(uint4 *chunkK, uint32_t o, uint32_t deg, uint32_t k,
+                                            uint32_t pre, uint32_t row) {
   const uint32_t end = o + deg;
-  for (uint32_t c = (o + kChunk - 1) / kChunk; c * kChunk < end; c++) chunkK[c] = k;
+  const uint4 rec = make_uint4(k, pre, end, row - o);  // edge e of arrival k is row + (e - o)
+  for (uint32_t c = (o + kChunk - 1) / kChunk; c * kChunk < end; c++) chunkK[c] = rec;
 }
 
 }  // namespace fb

@@ -30,215 +30,261 @@ namespace fb {
 // Phase A pieces
 // ---------------------------------------------------------------------------------------------
 
-// The serial parts of one brain's step, executed by one block (lif.c:35-52 minus the scatter).
-__device__ void brain_control(const StepArgs &a, Trial *T, int s, uint64_t gstep, int head,
-                              int slot, uint32_t *scan) {
-  __shared__ uint32_t sh_s0, sh_nbg;
-  __shared__ float sh_amp;
-  __shared__ bool sh_go;
-  const int tid = threadIdx.x;
-  const int N = T->N;
-  const int mode = T->mode;
-  if (tid == 0) {
-    // lif.c:47: bgAcc += bgEvents; nbg = (int)bgAcc; bgAcc -= nbg (f32 throughout)
-    float acc = __fadd_rn(ldcg(&T->bgAcc), T->bgEvents);
-    const int32_t nbg = (int32_t)acc;
-    acc = __fsub_rn(acc, (float)nbg);
-    T->bgAcc = acc;
-    sh_nbg = (uint32_t)nbg;
-    sh_s0 = ldcg(&T->rng);
-  }
-  __syncthreads();
-  const uint32_t s0 = sh_s0, nbg = sh_nbg;
-  const int32_t *arr = T->ring + (int64_t)head * N;
-
-  // Sequential delivery (exact also with presynaptic inhibition, lif.c:36-43): arrivals one at a
-  // time in list order; each row's targets are distinct, so a row scatters in parallel.
-  if (mode == FB_DELIVER_SEQUENTIAL) {
-    const int32_t na = ldcg(T->ringCount + head);
-    for (int32_t k = 0; k < na; k++) {
-      const int32_t pre = ldcg(arr + k);
-      if (tid == 0) {
-        float r = ldcg(T->res + pre);
-        float amp = __fmul_rn(__ldg(T->sign + pre), r);
-        sh_go = amp != 0.f;  // lif.c:37 skips only a zero sign*res, not a zero after :38
-        if (sh_go) {
-          if (T->preInh > 0.f && ldcg(T->drive + pre) > 0.f) {
-            const float gi = ldcg(T->gI + pre);
-            amp = __fdiv_rn(amp, __fadd_rn(1.f, __fmul_rn(T->preInh, gi < 0.f ? -gi : 0.f)));
-          }
-          T->res[pre] = __fsub_rn(r, __fmul_rn(T->depU, r));
-        }
-        sh_amp = amp;
-      }
-      __syncthreads();
-      const float amp = sh_amp;
-      if (sh_go) {
-        const uint32_t lo = __ldg(T->indptr + pre), hi = __ldg(T->indptr + pre + 1);
-        float *g = amp > 0 ? T->gE : T->gI;
-        for (uint32_t j = lo + tid; j < hi; j += blockDim.x) {
-          const uint32_t q = __ldg(T->indices + j);
-          g[q] = __fadd_rn(ldcg(g + q), __fmul_rn(__ldg(T->W + j), amp));
-        }
-      }
-      __syncthreads();
-    }
-  } else if (T->flags & kHasDep) {
-    // Mark arrivals so the update phase applies the depression res -= depU*res (lif.c:39).
-    const int32_t na = ldcg(T->ringCount + head);
-    for (int32_t k = tid; k < na; k += blockDim.x) T->arrived[ldcg(arr + k)] = 1;
-  }
-  __syncthreads();  // every thread has read ringCount[head] above
-  if (tid == 0) T->ringCount[head] = 0;  // lif.c:44
-
-  // Background draws 1..nbg (lif.c:48): target = draw % N, counted per target; the update phase
-  // adds bgAmp once per hit after the synaptic contributions, as lif.c orders them.
-  for (uint32_t d = 1 + tid; d <= nbg; d += blockDim.x) {
-    const uint32_t x = xs_jump(a.jump, s0, d);
-    atomicAdd(T->bgHits + (x % (uint32_t)N), 1u);
-  }
-
-  // Poisson-driven forced spikes (lif.c:49-52), in driven-list order, blockDim at a time.
-  const int32_t nD = ldcg(&T->nDriven);
-  int32_t *out = T->ring + (int64_t)slot * N;
-  uint32_t *outOff = T->ringOff + (int64_t)slot * (N + 1);
-  uint32_t *chunkK = T->chunkK + (int64_t)slot * T->chunkCap;
-  uint32_t draws = 0, nd = 0, deg = 0;
-  for (int32_t r0 = 0; r0 < nD; r0 += blockDim.x) {
-    const int32_t k = r0 + tid;
-    int32_t i = 0;
-    uint32_t live = 0;
-    if (k < nD) {
-      i = ldcg(T->driven + k);
-      live = ldcg(T->refr + i) > 0 ? 0u : 1u;  // refractory neurons draw nothing
-    }
-    uint32_t nlive;
-    const uint32_t dpos = block_exclusive_scan(live, &nlive, scan);
-    uint32_t fire = 0;
-    if (live) {
-      const uint32_t x = xs_jump(a.jump, s0, nbg + draws + dpos + 1);
-      const float u = __fmul_rn((float)(x >> 8), 1.0f / 16777216.0f);
-      const float p = __fmul_rn(ldcg(T->drive + i), T->dtS);
-      fire = u < p ? 1u : 0u;
-    }
-    uint32_t nfire;
-    const uint32_t fpos = block_exclusive_scan(fire, &nfire, scan);
-    uint32_t dg = 0;
-    if (fire) dg = __ldg(T->indptr + i + 1) - __ldg(T->indptr + i);
-    uint32_t dsum;
-    const uint32_t opos = block_exclusive_scan(dg, &dsum, scan);
-    if (fire) {
-      const uint32_t kk = nd + fpos, o = deg + opos;
-      out[kk] = i;
-      outOff[kk] = o;
-      mark_chunks(chunkK, o, dg, kk);
-      T->v[i] = T->vReset;
-      T->refr[i] = __fadd_rn(T->tRef, T->dt);
-      T->spikeCount[i] = ldcg(T->spikeCount + i) + 1u;
-      T->trace[i] = 1.f;
-      T->adapt[i] = __fadd_rn(ldcg(T->adapt + i), T->adaptInc);
-    }
-    draws += nlive;
-    nd += nfire;
-    deg += dsum;
-  }
-  if (tid == 0) {
-    T->rng = xs_jump(a.jump, s0, nbg + draws);
-    T->nForced[gstep & 1] = (int32_t)nd;
-    T->forcedDeg[gstep & 1] = deg;
+// Phase timer (fb_profile): thread 0 of block 0 adds the time since its last lap to counter k.
+__device__ __forceinline__ void prof_lap(const StepArgs &a, int k, uint64_t &tp) {
+  if (a.phaseNs != nullptr && blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint64_t now = global_ns();
+    atomicAdd(a.phaseNs + k, (unsigned long long)(now - tp));
+    tp = now;
   }
 }
 
-// Copies tile t's threshold spikes of step `gstep` (staged in the update phase) into the ring
-// slot, after the driven spikes and all lower tiles: ascending neuron order (lif.c:74-76).
-__device__ void materialize_tile(const StepArgs &a, Trial *T, int t, uint64_t gstep, int slot,
-                                 int64_t logBase) {
-  __shared__ uint32_t sh_cnt, sh_deg;
+__device__ __forceinline__ void st_relaxed64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Phase A for chunk c (entries c*kBlock ... +kBlock) of one brain's driven list. Chunk 0 also runs
+// the brain's other serial parts of lif.c's step: sequential delivery or arrival marks, the
+// ring-count clear, the background accumulator and draws (lif.c:34-48).
+//
+// Draw order is lif.c's (lif.c:48-52): draws 1..nbg go to the background, then one draw per
+// non-refractory driven entry in list order. A chunk's first draw index needs the non-refractory
+// count of every earlier chunk: each chunk publishes its count tagged with the step, and reads
+// the earlier ones (a bounded wait; chunks only wait on lower chunks, which never wait on higher
+// ones, and the grid is co-resident). xorshift32 is linear over GF(2), so each entry jumps to its
+// draw with the M^(2^j) tables. Forced spikes are staged per chunk; the next phase places them
+// at the head of the ring list.
+__device__ void driven_item(const StepArgs &a, const Trial &T, Trial *G, int c, int nDch, int32_t nD,
+                            uint64_t gstep, int head, uint32_t *scan, uint64_t *scan64,
+                            const uint32_t *jump, uint64_t &tp) {
+  __shared__ uint32_t sh_base;
+  __shared__ float sh_amp;
+  __shared__ bool sh_go;
   const int tid = threadIdx.x;
-  const int local = t - T->tileBase;
-  const bool last = local == T->nTiles - 1;
-  const int32_t m = ldcg(T->tileCnt + t);
-  if (m == 0 && !last && !(local == 0 && a.log)) return;  // uniform across the block
-  // counts and out-degrees of the lower tiles of this brain (the last tile also needs its own)
-  if (tid < 32) {
-    uint32_t c = 0, d = 0;
-    for (int u = tid; u < local; u += 32) {
-      c += (uint32_t)ldcg(T->tileCnt + T->tileBase + u);
-      d += ldcg(T->tileDeg + T->tileBase + u);
+  const int N = T.N;
+  const uint32_t par = (uint32_t)(gstep & 1);
+  // lif.c:47 on this step's copy: bgAcc += bgEvents; nbg = (int)bgAcc; bgAcc -= nbg (f32)
+  const float acc = __fadd_rn(ldcg(G->bgAccP + par), T.bgEvents);
+  const int32_t nbgI = (int32_t)acc;
+  const uint32_t nbg = (uint32_t)nbgI;
+  const uint32_t s0 = ldcg(G->rngP + par);
+  // this chunk's entries: one per thread
+  const int32_t k = c * kBlock + tid;
+  const bool valid = k < nD;
+  const int32_t i = valid ? ldcg(T.driven + k) : 0;
+  const float rf = ldcg(T.refr + i), dr = ldcg(T.drive + i);
+
+  if (c == 0) {
+    if (tid == 0) G->bgAccP[par ^ 1u] = __fsub_rn(acc, (float)nbgI);
+    const int32_t *arr = T.ring + (int64_t)head * N;
+    if (T.mode == FB_DELIVER_SEQUENTIAL) {
+      // Sequential delivery (exact also with presynaptic inhibition, lif.c:36-43): arrivals one
+      // at a time in list order; each row's targets are distinct, so a row scatters in parallel.
+      const int32_t na = ldcg(T.ringCount + head);
+      for (int32_t q0 = 0; q0 < na; q0++) {
+        const int32_t pre = ldcg(arr + q0);
+        if (tid == 0) {
+          const float r = ldcg(T.res + pre);
+          float amp = __fmul_rn(__ldg(T.sign + pre), r);
+          sh_go = amp != 0.f;  // lif.c:37 skips only a zero sign*res, not a zero after :38
+          if (sh_go) {
+            if (T.preInh > 0.f && ldcg(T.drive + pre) > 0.f) {
+              const float gi = ldcg(T.gI + pre);
+              amp = __fdiv_rn(amp, __fadd_rn(1.f, __fmul_rn(T.preInh, gi < 0.f ? -gi : 0.f)));
+            }
+            T.res[pre] = __fsub_rn(r, __fmul_rn(T.depU, r));
+          }
+          sh_amp = amp;
+        }
+        __syncthreads();
+        const float amp = sh_amp;
+        if (sh_go) {
+          const uint32_t lo = __ldg(T.indptr + pre), hi = __ldg(T.indptr + pre + 1);
+          float *g = amp > 0 ? T.gE : T.gI;
+          for (uint32_t j = lo + tid; j < hi; j += blockDim.x) {
+            const uint32_t q = __ldg(T.indices + j);
+            g[q] = __fadd_rn(ldcg(g + q), __fmul_rn(__ldg(T.W + j), amp));
+          }
+        }
+        __syncthreads();
+      }
+    } else if (T.flags & kHasDep) {
+      // Mark arrivals so the update phase applies the depression res -= depU*res (lif.c:39).
+      const int32_t na = ldcg(T.ringCount + head);
+      for (int32_t q0 = tid; q0 < na; q0 += blockDim.x) T.arrived[ldcg(arr + q0)] = 1;
     }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      c += __shfl_xor_sync(0xffffffffu, c, o);
-      d += __shfl_xor_sync(0xffffffffu, d, o);
+    __syncthreads();  // every thread has read ringCount[head] above
+    if (tid == 0) T.ringCount[head] = 0;  // lif.c:44
+    // background draws 1..nbg (lif.c:48): target = draw % N, counted per target; the update
+    // phase adds bgAmp once per hit after the synaptic contributions, as lif.c orders them
+    for (uint32_t d = 1 + tid; d <= nbg; d += blockDim.x) {
+      const uint32_t x = xs_jump(jump, s0, d);
+      atomicAdd(T.bgHits + (x % (uint32_t)N), 1u);
     }
-    if (tid == 0) { sh_cnt = c; sh_deg = d; }
+  }
+  prof_lap(a, 5, tp);
+
+  const uint32_t live = (valid && !(rf > 0)) ? 1u : 0u;  // refractory entries draw nothing
+  uint32_t L;
+  const uint32_t lp = block_exclusive_scan(live, &L, scan);
+  if (tid == 0) {
+    const unsigned long long tag = (unsigned long long)(gstep + 1) << 32;
+    st_relaxed64(T.liveTag + c, tag | L);
+    uint32_t base = 0;
+    const uint64_t t0 = global_ns();
+    uint32_t it = 0;
+    for (int c2 = 0; c2 < c; c2++) {
+      unsigned long long x;
+      while (((x = ld_relaxed64(T.liveTag + c2)) >> 32) != (gstep + 1)) {
+        if ((++it & 63u) == 0 && (global_ns() - t0 > (uint64_t)a.timeoutNs || it > (1u << 30) ||
+                                  ld_volatile(a.err) != 0)) {
+          atomicCAS(a.err, 0, FB_ETIMEOUT);
+          break;
+        }
+      }
+      base += (uint32_t)x;
+    }
+    sh_base = base;
   }
   __syncthreads();
-  const int N = T->N;
-  const uint32_t nd = (uint32_t)ldcg(T->nForced + (gstep & 1));
-  const uint32_t Fd = ldcg(T->forcedDeg + (gstep & 1));
-  const uint32_t before = nd + sh_cnt, dbefore = Fd + sh_deg;
-  int32_t *out = T->ring + (int64_t)slot * N;
-  uint32_t *outOff = T->ringOff + (int64_t)slot * (N + 1);
-  uint32_t *chunkK = T->chunkK + (int64_t)slot * T->chunkCap;
-  const int32_t *stage = T->stage + (int64_t)local * kTile;
-  const uint32_t *stageDeg = T->stageDeg + (int64_t)local * kTile;
-  const bool logging = a.log && T->logRaster != nullptr;
-  const int64_t rbase = logging ? ldcg(T->logRasterLen + (gstep & 1)) : 0;
+  prof_lap(a, 6, tp);
+  const uint32_t base = sh_base;
+  uint32_t fire = 0, dg = 0;
+  if (live) {
+    const uint32_t x = xs_jump(jump, s0, nbg + base + lp + 1);
+    const float u = __fmul_rn((float)(x >> 8), 1.0f / 16777216.0f);
+    if (u < __fmul_rn(dr, T.dtS)) {
+      fire = 1;
+      dg = __ldg(T.indptr + i + 1) - __ldg(T.indptr + i);
+    }
+  }
+  if (c == nDch - 1 && tid == 0) G->rngP[par ^ 1u] = xs_jump(jump, s0, nbg + base + L);
+  prof_lap(a, 7, tp);
+  const int64_t cidx = (int64_t)par * T.maxDch + c;
+  if (__syncthreads_or(fire)) {
+    uint64_t tot;
+    const uint64_t pre = block_exclusive_scan(((uint64_t)fire << 32) | dg, &tot, scan64);
+    if (fire) {
+      const int64_t o = cidx * kBlock + (int64_t)(pre >> 32);
+      T.dStage[o] = i;
+      T.dStageDeg[o] = (uint32_t)pre;
+      // lif.c:52
+      T.v[i] = T.vReset;
+      T.refr[i] = __fadd_rn(T.tRef, T.dt);
+      T.spikeCount[i] = ldcg(T.spikeCount + i) + 1u;
+      T.trace[i] = 1.f;
+      T.adapt[i] = __fadd_rn(ldcg(T.adapt + i), T.adaptInc);
+    }
+    if (tid == 0) {
+      T.dCnt[cidx] = (int32_t)(tot >> 32);
+      T.dDeg[cidx] = (uint32_t)tot;
+    }
+  } else if (tid == 0) {
+    T.dCnt[cidx] = 0;
+    T.dDeg[cidx] = 0;
+  }
+  prof_lap(a, 8, tp);
+}
+
+// Copies one staging unit of step `gstep` into its ring slot: units are the brain's driven-list
+// chunks (forced spikes, list order) followed by its update tiles (threshold spikes, ascending),
+// so the slot holds lif.c's order (lif.c:51-52 then :74-76). Each unit's offset is the sum over
+// the units before it; the last unit also writes the list's totals.
+__device__ void materialize_unit(const StepArgs &a, const Trial &T, Trial *G, int u, int nDch,
+                                 uint64_t gstep, int slot, int64_t logBase, uint64_t *scan64) {
+  __shared__ uint32_t sh_cnt, sh_deg;
+  const int tid = threadIdx.x;
+  const int64_t dpar = (int64_t)(gstep & 1) * T.maxDch;
+  const bool drv = u < nDch;
+  const int tt = T.tileBase + (u - nDch);  // tile index when !drv
+  const bool last = u == nDch + T.nTiles - 1;
+  const int32_t m = drv ? ldcg(T.dCnt + dpar + u) : ldcg(T.tileCnt + tt);
+  if (m == 0 && !last) return;  // uniform across the block
+  uint64_t acc = 0;
+  for (int v = tid; v < u; v += blockDim.x) {
+    if (v < nDch) acc += ((uint64_t)(uint32_t)ldcg(T.dCnt + dpar + v) << 32) | ldcg(T.dDeg + dpar + v);
+    else acc += ((uint64_t)(uint32_t)ldcg(T.tileCnt + T.tileBase + v - nDch) << 32) |
+                ldcg(T.tileDeg + T.tileBase + v - nDch);
+  }
+  acc = block_sum(acc, scan64);
+  if (tid == 0) {
+    sh_cnt = (uint32_t)(acc >> 32);
+    sh_deg = (uint32_t)acc;
+  }
+  __syncthreads();
+  const int N = T.N;
+  const uint32_t before = sh_cnt, dbefore = sh_deg;
+  int32_t *out = T.ring + (int64_t)slot * N;
+  uint32_t *outOff = T.ringOff + (int64_t)slot * (N + 1);
+  uint32_t *outRow = T.ringRow + (int64_t)slot * N;
+  uint4 *chunkK = T.chunkK + (int64_t)slot * T.chunkCap;
+  const int32_t *stage = drv ? T.dStage + (dpar + u) * kBlock : T.stage + (int64_t)(u - nDch) * kTile;
+  const uint32_t *stageDeg = drv ? T.dStageDeg + (dpar + u) * kBlock : T.stageDeg + (int64_t)(u - nDch) * kTile;
+  const bool logging = a.log && T.logRaster != nullptr;
+  const int64_t rbase = logging ? ldcg(G->logRasterLen + (gstep & 1)) : 0;
   for (int p = tid; p < m; p += blockDim.x) {
     const int32_t i = ldcg(stage + p);
     const uint32_t k = before + p, o = dbefore + ldcg(stageDeg + p);
+    const uint32_t r0 = __ldg(T.indptr + i), r1 = __ldg(T.indptr + i + 1);
     out[k] = i;
     outOff[k] = o;
-    mark_chunks(chunkK, o, __ldg(T->indptr + i + 1) - __ldg(T->indptr + i), k);
-    if (logging && rbase + k < T->logRasterCap) T->logRaster[rbase + k] = i;
-  }
-  if (logging && local == 0) {  // the driven spikes head the list
-    for (uint32_t p = tid; p < nd; p += blockDim.x)
-      if (rbase + p < T->logRasterCap) T->logRaster[rbase + p] = ldcg(out + p);
+    outRow[k] = r0;
+    mark_chunks(chunkK, o, r1 - r0, k, (uint32_t)i, r0);
+    if (logging && rbase + k < T.logRasterCap) T.logRaster[rbase + k] = i;
   }
   if (last && tid == 0) {
     const uint32_t nf = before + (uint32_t)m;
-    const uint32_t F = dbefore + ldcg(T->tileDeg + t);
+    const uint32_t F = dbefore + (drv ? ldcg(T.dDeg + dpar + u) : ldcg(T.tileDeg + tt));
     outOff[nf] = F;
-    T->ringCount[slot] = (int32_t)nf;
-    T->slotEdges[slot] = F;
-    T->nFired = (int32_t)nf;
-    T->lastSlot = slot;
+    T.ringCount[slot] = (int32_t)nf;
+    T.slotEdges[slot] = F;
+    G->nFired = (int32_t)nf;
+    G->lastSlot = slot;
     if (a.log) {
-      if (T->logCount && logBase >= 0 && logBase < T->logCap) T->logCount[logBase] = (int32_t)nf;
-      if (T->logRaster) T->logRasterLen[(gstep + 1) & 1] = rbase + nf;
+      if (T.logCount && logBase >= 0 && logBase < T.logCap) T.logCount[logBase] = (int32_t)nf;
+      if (T.logRaster) G->logRasterLen[(gstep + 1) & 1] = rbase + nf;
     }
   }
 }
 
 // One delivery work item: 32 consecutive edges of the concatenated rows of the arrivals in
-// `slot`, starting at edge c * 32. Lane l takes edge c*32+l.
-__device__ __forceinline__ void deliver_chunk(const StepArgs &a, Trial *T, int slot, uint32_t F,
+// `slot`, starting at edge c * 32. Lane l takes edge c*32+l. The item's record names its first
+// arrival; lanes past that arrival's edges find theirs through the offsets.
+__device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T, Trial *G, int slot, uint32_t F,
                                               uint32_t c, uint32_t gparity) {
   const int lane = threadIdx.x & 31;
   const uint32_t e = c * kChunk + lane;
   if (e >= F) return;
-  const int N = T->N;
-  const int32_t *arr = T->ring + (int64_t)slot * N;
-  const uint32_t *off = T->ringOff + (int64_t)slot * (N + 1);
-  uint32_t k = ldcg(T->chunkK + (int64_t)slot * T->chunkCap + c);
-  while (ldcg(off + k + 1) <= e) k++;
-  const int32_t pre = ldcg(arr + k);
-  const float amp = __fmul_rn(__ldg(T->sign + pre), ldcg(T->res + pre));  // lif.c:37
+  const int N = T.N;
+  const uint4 ck = ldcg(T.chunkK + (int64_t)slot * T.chunkCap + c);
+  uint32_t k = ck.x, pre = ck.y, j = ck.w + e;
+  if (e >= ck.z) {  // a later arrival of this item
+    const uint32_t *off = T.ringOff + (int64_t)slot * (N + 1);
+    k++;
+    while (ldcg(off + k + 1) <= e) k++;
+    pre = (uint32_t)ldcg(T.ring + (int64_t)slot * N + k);
+    j = ldcg(T.ringRow + (int64_t)slot * N + k) + (e - ldcg(off + k));
+  }
+  // the edge's loads are issued with the presynaptic ones, before the zero-amplitude test
+  const uint32_t q = __ldg(T.indices + j);
+  const float wj = __ldg(T.W + j);
+  const float amp = __fmul_rn(__ldg(T.sign + pre), ldcg(T.res + pre));  // lif.c:37
   if (amp == 0.f) return;
-  const uint32_t j = __ldg(T->indptr + pre) + (e - ldcg(off + k));
-  const uint32_t q = __ldg(T->indices + j);
-  const float w = __fmul_rn(__ldg(T->W + j), amp);  // lif.c:41-42, one rounding
+  const float w = __fmul_rn(wj, amp);  // lif.c:41-42, one rounding
   const bool inh = !(amp > 0);
-  if (T->mode == FB_DELIVER_FAST) {
-    atomicAdd(inh ? T->gI + q : T->gE + q, w);
+  if (T.mode == FB_DELIVER_FAST) {
+    atomicAdd(inh ? T.gI + q : T.gE + q, w);
     return;
   }
   const uint32_t key = (k << 1) | (inh ? 1u : 0u);
-  const uint32_t pos = atomicAdd(T->cnt + q, 1u);
+  const uint32_t pos = atomicAdd(T.cnt + q, 1u);
   if (pos < (uint32_t)kBucket) {
-    T->bucket[(int64_t)q * kBucket + pos] = make_uint2(key, __float_as_uint(w));
+    T.bucket[(int64_t)q * kBucket + pos] = make_uint2(key, __float_as_uint(w));
   } else {
     const uint32_t r = atomicAdd(a.ovfTop + gparity, 1u);
     if (r >= a.ovfCap) {
@@ -249,7 +295,7 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, Trial *T, int s
     rec.key = key;
     rec.bits = __float_as_uint(w);
     rec.pad = q;
-    rec.next = atomicExch(T->ovfHead + q, r);
+    rec.next = atomicExch(T.ovfHead + q, r);
     a.ovf[gparity][r] = rec;
   }
 }
@@ -259,9 +305,9 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, Trial *T, int s
 // ---------------------------------------------------------------------------------------------
 
 // Adds target i's contributions in ascending key (arrival rank) order; inhibitory keys go to gI.
-__device__ __forceinline__ void apply_contributions(const StepArgs &a, Trial *T, int i, uint32_t n,
+__device__ __forceinline__ void apply_contributions(const StepArgs &a, const Trial &T, Trial *G, int i, uint32_t n,
                                                     uint32_t gparity, float &ge, float &gi) {
-  const uint2 *bk = T->bucket + (int64_t)i * kBucket;
+  const uint2 *bk = T.bucket + (int64_t)i * kBucket;
   if (n == 1) {
     const uint2 x = ldcg(bk);
     if (x.x & 1u) gi = __fadd_rn(gi, __uint_as_float(x.y));
@@ -273,13 +319,13 @@ __device__ __forceinline__ void apply_contributions(const StepArgs &a, Trial *T,
   for (uint32_t u = 0; u < m; u++) e[u] = ldcg(bk + u);
   const bool spill = n > (uint32_t)kBucket;
   if (spill) {
-    uint32_t r = ldcg(T->ovfHead + i);
+    uint32_t r = ldcg(T.ovfHead + i);
     while (r != kNil && m < (uint32_t)kSortMax) {
       const OvfRec rec = a.ovf[gparity][r];
       e[m++] = make_uint2(rec.key, rec.bits);
       r = rec.next;
     }
-    T->ovfHead[i] = kNil;
+    T.ovfHead[i] = kNil;
     if (r != kNil) atomicCAS(a.err, 0, FB_EOVERFLOW);  // more than kSortMax in one step
   }
   for (uint32_t u = 1; u < m; u++) {  // insertion sort by key
@@ -297,86 +343,127 @@ __device__ __forceinline__ void apply_contributions(const StepArgs &a, Trial *T,
   }
 }
 
-__device__ void update_tile(const StepArgs &a, Trial *T, int t, uint32_t gparity, uint32_t *scan) {
-  const int tid = threadIdx.x;
-  const int local = t - T->tileBase;
-  const int i = local * kTile + tid;
-  const int N = T->N;
-  bool fired = false;
-  uint32_t dg = 0;
-  if (i < N) {
-    float v = ldcg(T->v + i), r = ldcg(T->refr + i);
-    float ge = ldcg(T->gE + i), gi = ldcg(T->gI + i);
-    float tr = ldcg(T->trace + i), ad = ldcg(T->adapt + i), rs = ldcg(T->res + i);
-    const float bias = ldcg(T->bias + i), thr = ldcg(T->thr + i);
-    if (T->mode == FB_DELIVER_EXACT) {
-      const uint32_t n = ldcg(T->cnt + i);
-      if (n) {
-        apply_contributions(a, T, i, n, gparity, ge, gi);
-        T->cnt[i] = 0;
-      }
-    }
-    if (T->flags & kHasBg) {  // lif.c:48, after every synaptic contribution
-      const uint32_t h = ldcg(T->bgHits + i);
-      if (h) {
-        for (uint32_t u = 0; u < h; u++) ge = __fadd_rn(ge, T->bgAmp);
-        T->bgHits[i] = 0;
-      }
-    }
-    if ((T->flags & kHasDep) && T->mode != FB_DELIVER_SEQUENTIAL) {
-      if (ldcg(T->arrived + i)) {  // lif.c:37-39: depressed at delivery unless sign*res == 0
-        T->arrived[i] = 0;
-        if (!(__fmul_rn(__ldg(T->sign + i), rs) == 0.f)) rs = __fsub_rn(rs, __fmul_rn(T->depU, rs));
-      }
-    }
-    // lif.c:55-72, one IEEE f32 operation per C operation, in C order
-    float acc = __fsub_rn(T->vRest, v);
-    if (T->coba) {
-      acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(ge, __fsub_rn(T->eExc, v)), T->cE));
-      acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(gi, __fsub_rn(v, T->eInh)), T->cI));
-    } else {
-      acc = __fadd_rn(acc, ge);
-      acc = __fadd_rn(acc, gi);
-    }
-    acc = __fadd_rn(acc, bias);
-    const float dv = __fmul_rn(acc, T->kM);
-    const bool refractory = r > 0;
-    v = refractory ? T->vReset : __fadd_rn(v, dv);
-    r = refractory ? __fsub_rn(r, T->dt) : r;
-    ge = __fmul_rn(ge, T->dE);
-    gi = __fmul_rn(gi, T->dE);
-    tr = __fmul_rn(tr, T->dTr);
-    ad = __fmul_rn(ad, T->dA);
-    rs = __fadd_rn(rs, __fmul_rn(__fsub_rn(1.f, rs), T->kRec));
-    // lif.c:74-75: threshold against the decayed adapt
-    if (v >= __fadd_rn(__fadd_rn(T->vThresh, ad), thr) && r <= 0) {
-      v = T->vReset;
-      r = T->tRef;
-      tr = 1.f;
-      ad = __fadd_rn(ad, T->adaptInc);
-      T->spikeCount[i] = ldcg(T->spikeCount + i) + 1u;
-      fired = true;
-      dg = __ldg(T->indptr + i + 1) - __ldg(T->indptr + i);
-    }
-    T->v[i] = v;
-    T->refr[i] = r;
-    T->gE[i] = ge;
-    T->gI[i] = gi;
-    T->trace[i] = tr;
-    T->adapt[i] = ad;
-    T->res[i] = rs;
+// A neuron's state as loaded at the start of the update phase.
+struct NState {
+  float v, r, ge, gi, tr, ad, rs, bias, thr;
+  uint32_t n, hits;
+  uint8_t arrived;
+};
+
+__device__ __forceinline__ NState load_neuron(const Trial &T, int i) {
+  NState x;
+  x.v = ldcg(T.v + i);
+  x.r = ldcg(T.refr + i);
+  x.ge = ldcg(T.gE + i);
+  x.gi = ldcg(T.gI + i);
+  x.tr = ldcg(T.trace + i);
+  x.ad = ldcg(T.adapt + i);
+  x.rs = ldcg(T.res + i);
+  x.bias = ldcg(T.bias + i);
+  x.thr = ldcg(T.thr + i);
+  x.n = T.mode == FB_DELIVER_EXACT ? ldcg(T.cnt + i) : 0u;
+  x.hits = (T.flags & kHasBg) ? ldcg(T.bgHits + i) : 0u;
+  x.arrived = ((T.flags & kHasDep) && T.mode != FB_DELIVER_SEQUENTIAL) ? ldcg(T.arrived + i) : (uint8_t)0;
+  return x;
+}
+
+// One neuron's step after delivery: contributions in order, background hits, depression,
+// membrane and decays (lif.c:55-72), threshold (lif.c:73-76). Returns the out-degree + 1 if it
+// fired, 0 otherwise.
+__device__ __forceinline__ uint32_t update_neuron(const StepArgs &a, const Trial &T, Trial *G, int i,
+                                                  NState x, uint32_t gparity) {
+  float v = x.v, r = x.r, ge = x.ge, gi = x.gi, tr = x.tr, ad = x.ad, rs = x.rs;
+  if (x.n) {
+    apply_contributions(a, T, G, i, x.n, gparity, ge, gi);
+    T.cnt[i] = 0;
   }
-  // ascending compaction of the tile's spikes (and their out-degree prefix) into the staging area
-  uint32_t nf, dsum;
-  const uint32_t pos = block_exclusive_scan(fired ? 1u : 0u, &nf, scan);
-  const uint32_t dpos = block_exclusive_scan(dg, &dsum, scan);
-  if (fired) {
-    T->stage[(int64_t)local * kTile + pos] = i;
-    T->stageDeg[(int64_t)local * kTile + pos] = dpos;
+  if (x.hits) {  // lif.c:48, after every synaptic contribution
+    for (uint32_t u = 0; u < x.hits; u++) ge = __fadd_rn(ge, T.bgAmp);
+    T.bgHits[i] = 0;
+  }
+  if (x.arrived) {  // lif.c:37-39: depressed at delivery unless sign*res == 0
+    T.arrived[i] = 0;
+    if (!(__fmul_rn(__ldg(T.sign + i), rs) == 0.f)) rs = __fsub_rn(rs, __fmul_rn(T.depU, rs));
+  }
+  // lif.c:55-72, one IEEE f32 operation per C operation, in C order
+  float acc = __fsub_rn(T.vRest, v);
+  if (T.coba) {
+    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(ge, __fsub_rn(T.eExc, v)), T.cE));
+    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(gi, __fsub_rn(v, T.eInh)), T.cI));
+  } else {
+    acc = __fadd_rn(acc, ge);
+    acc = __fadd_rn(acc, gi);
+  }
+  acc = __fadd_rn(acc, x.bias);
+  const float dv = __fmul_rn(acc, T.kM);
+  const bool refractory = r > 0;
+  v = refractory ? T.vReset : __fadd_rn(v, dv);
+  r = refractory ? __fsub_rn(r, T.dt) : r;
+  ge = __fmul_rn(ge, T.dE);
+  gi = __fmul_rn(gi, T.dE);
+  tr = __fmul_rn(tr, T.dTr);
+  ad = __fmul_rn(ad, T.dA);
+  rs = __fadd_rn(rs, __fmul_rn(__fsub_rn(1.f, rs), T.kRec));
+  uint32_t fired = 0;
+  // lif.c:74-75: threshold against the decayed adapt
+  if (v >= __fadd_rn(__fadd_rn(T.vThresh, ad), x.thr) && r <= 0) {
+    v = T.vReset;
+    r = T.tRef;
+    tr = 1.f;
+    ad = __fadd_rn(ad, T.adaptInc);
+    T.spikeCount[i] = ldcg(T.spikeCount + i) + 1u;
+    fired = 1 + __ldg(T.indptr + i + 1) - __ldg(T.indptr + i);
+  }
+  T.v[i] = v;
+  T.refr[i] = r;
+  T.gE[i] = ge;
+  T.gI[i] = gi;
+  T.trace[i] = tr;
+  T.adapt[i] = ad;
+  T.res[i] = rs;
+  return fired;
+}
+
+// One tile of kTile neurons: thread t updates local neurons t and t + kBlock. The tile's spikes
+// are compacted in ascending order with their out-degree prefix (skipped when none fired).
+__device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, uint32_t gparity, uint32_t *scan,
+                            uint64_t *scan64) {
+  const int tid = threadIdx.x;
+  const int local = t - T.tileBase;
+  const int i0 = local * kTile + tid, i1 = i0 + kBlock;
+  const int N = T.N;
+  // both neurons' loads are issued before either is stored (the stores could alias them)
+  const NState x0 = load_neuron(T, i0 < N ? i0 : 0);
+  const NState x1 = load_neuron(T, i1 < N ? i1 : 0);
+  const uint32_t f0 = i0 < N ? update_neuron(a, T, G, i0, x0, gparity) : 0;
+  const uint32_t f1 = i1 < N ? update_neuron(a, T, G, i1, x1, gparity) : 0;
+  if (!__syncthreads_or(f0 | f1)) {
+    if (tid == 0) {
+      T.tileCnt[t] = 0;
+      T.tileDeg[t] = 0;
+    }
+    return;
+  }
+  const uint32_t c0 = f0 ? 1u : 0u, c1 = f1 ? 1u : 0u;
+  const uint32_t d0 = f0 ? f0 - 1 : 0u, d1 = f1 ? f1 - 1 : 0u;
+  uint32_t ctot;
+  const uint32_t cpre = block_exclusive_scan(c0 | (c1 << 16), &ctot, scan);
+  uint64_t dtot;
+  const uint64_t dpre = block_exclusive_scan((uint64_t)d0 | ((uint64_t)d1 << 32), &dtot, scan64);
+  const uint32_t n0 = ctot & 0xffffu, dsum0 = (uint32_t)dtot;
+  int32_t *stage = T.stage + (int64_t)local * kTile;
+  uint32_t *stageDeg = T.stageDeg + (int64_t)local * kTile;
+  if (f0) {
+    stage[cpre & 0xffffu] = i0;
+    stageDeg[cpre & 0xffffu] = (uint32_t)dpre;
+  }
+  if (f1) {
+    stage[n0 + (cpre >> 16)] = i1;
+    stageDeg[n0 + (cpre >> 16)] = dsum0 + (uint32_t)(dpre >> 32);
   }
   if (tid == 0) {
-    T->tileCnt[t] = (int32_t)nf;
-    T->tileDeg[t] = dsum;
+    T.tileCnt[t] = (int32_t)(n0 + (ctot >> 16));
+    T.tileDeg[t] = dsum0 + (uint32_t)(dtot >> 32);
   }
 }
 
@@ -384,57 +471,108 @@ __device__ void update_tile(const StepArgs &a, Trial *T, int t, uint32_t gparity
 // The persistent kernel
 // ---------------------------------------------------------------------------------------------
 
+// Brain headers of the first kTrialCache brains of a batch are copied to shared memory once per
+// launch: the acquire fence that ends every grid barrier invalidates L1, so constants read from
+// global memory would be refetched from L2 at every step.
+constexpr int kTrialCache = 4;
+
 __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
-  extern __shared__ uint32_t sm[];
-  // per-brain launch constants: start head, ring depth, steps of this launch; then the prefix of
-  // this step's delivery work items over brains
-  int32_t *sHead0 = (int32_t *)sm;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  // per-brain launch constants (layout mirrors step_smem_bytes): step count and log start at
+  // launch, start head, ring depth, steps of this launch, first tile; then the prefix of this
+  // step's delivery work items over brains
+  int64_t *sDone = (int64_t *)smraw;
+  int64_t *sLog = sDone + a.B;
+  int32_t *sHead0 = (int32_t *)(sLog + a.B);
   int32_t *sNs = sHead0 + a.B;
   int32_t *sSteps = sNs + a.B;
-  uint32_t *sPre = (uint32_t *)(sSteps + a.B);  // B + 1
+  int32_t *sND = sSteps + a.B;             // driven-list length at launch
+  int32_t *sTile0 = sND + a.B;             // B + 1: first update tile of each brain
+  int32_t *sDch0 = sTile0 + a.B + 1;       // B + 1: first driven chunk item of each brain
+  int32_t *sU0 = sDch0 + a.B + 1;          // B + 1: first staging unit of each brain
+  uint32_t *sPre = (uint32_t *)(sU0 + a.B + 1);  // B + 1
   __shared__ uint32_t scan[33];
-  __shared__ int64_t sStepsDone;
+  __shared__ uint64_t scan64[33];
+  __shared__ uint32_t sJump[32 * 128];
+  __shared__ Trial sTr[kTrialCache];
   const int tid = threadIdx.x;
+  for (int k = tid; k < 32 * 128; k += blockDim.x) sJump[k] = a.jump[k];
+  {
+    const int nc = min(a.B, kTrialCache);
+    const uint32_t *src = (const uint32_t *)a.trials;
+    uint32_t *dst = (uint32_t *)sTr;
+    for (int k = tid; k < nc * (int)(sizeof(Trial) / 4); k += blockDim.x) dst[k] = ldcg(src + k);
+  }
   for (int b = tid; b < a.B; b += blockDim.x) {
-    sHead0[b] = ldcg(&a.trials[b].head);
-    sNs[b] = a.trials[b].nslots;
+    const Trial *G = a.trials + b;
+    sDone[b] = ldcg(&G->stepsDone);
+    sLog[b] = ldcg(&G->logStart);
+    sHead0[b] = ldcg(&G->head);
+    sNs[b] = G->nslots;
     sSteps[b] = a.steps[b];
+    sND[b] = ldcg(&G->nDriven);
+    sTile0[b] = G->tileBase;
   }
   __syncthreads();
+  if (tid == 0) {
+    sTile0[a.B] = a.nTilesTotal;
+    int dc = 0, uc = 0;
+    for (int b = 0; b < a.B; b++) {
+      const int nd = max(1, (sND[b] + kBlock - 1) / kBlock);
+      sDch0[b] = dc;
+      sU0[b] = uc;
+      dc += nd;
+      uc += nd + (sTile0[b + 1] - sTile0[b]);
+    }
+    sDch0[a.B] = dc;
+    sU0[a.B] = uc;
+  }
+  __syncthreads();
+  auto hdr = [&](int b) -> const Trial & { return b < kTrialCache ? sTr[b] : a.trials[b]; };
+  auto find = [&](const int32_t *first, int x) {  // b with first[b] <= x < first[b+1]
+    int lo = 0, hi = a.B;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (first[mid] <= x) lo = mid;
+      else hi = mid;
+    }
+    return lo;
+  };
+  auto tile_brain = [&](int t) { return find(sTile0, t); };
+  const int nDItems = sDch0[a.B], nUItems = sU0[a.B];
   const int warpsPerBlock = blockDim.x >> 5;
   const uint32_t gwarp = blockIdx.x * warpsPerBlock + (tid >> 5);
   const uint32_t nwarps = gridDim.x * warpsPerBlock;
 
+  uint64_t tp = a.phaseNs != nullptr ? global_ns() : 0;
+  auto lap = [&](int k) { prof_lap(a, k, tp); };
   for (int s = 0; s <= a.maxSteps; s++) {
     // ---------------- phase A: materialize step s-1, control + deliver step s ----------------
-    for (int item = blockIdx.x; item < a.B + a.nTilesTotal; item += gridDim.x) {
-      if (item < a.B) {
-        const int b = item;
+    for (int item = blockIdx.x; item < nDItems + nUItems; item += gridDim.x) {
+      if (item < nDItems) {
+        const int b = find(sDch0, item);
         if (s < sSteps[b]) {
-          Trial *T = a.trials + b;
-          if (tid == 0) sStepsDone = ldcg(&T->stepsDone);
-          __syncthreads();
           const int ns = sNs[b];
           const int head = (sHead0[b] + s) % ns;
-          brain_control(a, T, s, (uint64_t)(sStepsDone + s), head, (head + ns - 1) % ns, scan);
+          driven_item(a, hdr(b), a.trials + b, item - sDch0[b], sDch0[b + 1] - sDch0[b], sND[b],
+                      (uint64_t)(sDone[b] + s), head, scan, scan64, sJump, tp);
           __syncthreads();
         }
       } else {
-        const int t = item - a.B;
-        const int b = a.tileTrial[t];
+        const int m = item - nDItems;
+        const int b = find(sU0, m);
         if (s >= 1 && s <= sSteps[b]) {
-          Trial *T = a.trials + b;
-          if (tid == 0) sStepsDone = ldcg(&T->stepsDone);
-          __syncthreads();
           const int ns = sNs[b];
           const int head = (sHead0[b] + s - 1) % ns;
-          const uint64_t g = (uint64_t)(sStepsDone + s - 1);
-          materialize_tile(a, T, t, g, (head + ns - 1) % ns, (int64_t)g - ldcg(&T->logStart));
+          const uint64_t g = (uint64_t)(sDone[b] + s - 1);
+          materialize_unit(a, hdr(b), a.trials + b, m - sU0[b], sDch0[b + 1] - sDch0[b], g,
+                           (head + ns - 1) % ns, (int64_t)g - sLog[b], scan64);
           __syncthreads();
         }
       }
     }
     if (s == a.maxSteps) break;
+    lap(0);
     // delivery work items of every brain still stepping, enumerated through a prefix over brains
     {
       uint32_t carry = 0;
@@ -442,10 +580,10 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
         const int b = b0 + tid;
         uint32_t n = 0;
         if (b < a.B && s < sSteps[b]) {
-          const Trial *T = a.trials + b;
-          if (T->mode != FB_DELIVER_SEQUENTIAL) {
+          const Trial &T = hdr(b);
+          if (T.mode != FB_DELIVER_SEQUENTIAL) {
             const int head = (sHead0[b] + s) % sNs[b];
-            n = (ldcg(T->slotEdges + head) + kChunk - 1) / kChunk;
+            n = (ldcg(T.slotEdges + head) + kChunk - 1) / kChunk;
           }
         }
         uint32_t tot;
@@ -456,37 +594,42 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
       if (tid == 0) sPre[a.B] = carry;
       __syncthreads();
     }
+    // work items go to warps from the far end of the grid, whose blocks have the fewest items
     const uint32_t total = sPre[a.B];
-    for (uint32_t w = gwarp; w < total; w += nwarps) {
+    for (uint32_t w = nwarps - 1 - gwarp; w < total; w += nwarps) {
       int lo = 0, hi = a.B;  // brain b with sPre[b] <= w < sPre[b+1]
       while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (sPre[mid] <= w) lo = mid;
         else hi = mid;
       }
-      Trial *T = a.trials + lo;
+      const Trial &T = hdr(lo);
       const int head = (sHead0[lo] + s) % sNs[lo];
-      deliver_chunk(a, T, head, ldcg(T->slotEdges + head), w - sPre[lo], (uint32_t)(s & 1));
+      deliver_chunk(a, T, a.trials + lo, head, ldcg(T.slotEdges + head), w - sPre[lo], (uint32_t)(s & 1));
     }
+    lap(1);
     if (!grid_sync(a)) return;
+    lap(2);
 
     // ---------------- phase B: update every neuron of every brain still stepping --------------
     // the overflow pool alternates with the launch-local step parity; the half used next step
     // was last read in the update phase of the step before this one
     if (blockIdx.x == 0 && tid == 0) a.ovfTop[(s + 1) & 1] = 0;
     for (int t = blockIdx.x; t < a.nTilesTotal; t += gridDim.x) {
-      const int b = a.tileTrial[t];
-      if (s < sSteps[b]) update_tile(a, a.trials + b, t, (uint32_t)(s & 1), scan);
+      const int b = tile_brain(t);
+      if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (uint32_t)(s & 1), scan, scan64);
     }
+    lap(3);
     if (!grid_sync(a)) return;
+    lap(4);
   }
   // per-brain scalars after the launch: ring head and step count
   __syncthreads();
   if (!grid_sync(a)) return;
   for (int b = blockIdx.x * blockDim.x + tid; b < a.B; b += gridDim.x * blockDim.x) {
-    Trial *T = a.trials + b;
-    T->head = (sHead0[b] + sSteps[b]) % sNs[b];
-    T->stepsDone = T->stepsDone + sSteps[b];
+    Trial *G = a.trials + b;
+    G->head = (sHead0[b] + sSteps[b]) % sNs[b];
+    G->stepsDone = sDone[b] + sSteps[b];
   }
   if (blockIdx.x == 0 && tid == 0) {  // the next launch starts with an empty overflow pool
     a.ovfTop[0] = 0;
@@ -558,6 +701,10 @@ __global__ void reset_kernel(Trial *trials, int32_t b0, int32_t b1) {
 // Host-side launch glue (internal; called from fb_api.cu)
 // ---------------------------------------------------------------------------------------------
 namespace fb {
+
+size_t step_smem_bytes(int B) {
+  return (size_t)B * 8 * 2 + (size_t)B * 4 * 4 + (size_t)(B + 1) * 4 * 4;
+}
 
 int step_kernel_blocks_per_sm(size_t smem) {
   int n = 0;

@@ -56,6 +56,8 @@ SIGNATURES = {
     "fb_write": (C.c_int, [P, I32, I32, P]),
     "fb_scalars": (C.c_int, [P, I32, PI32, PU32, PI32, PI32, PI32, PI64]),
     "fb_last_step_ms": (C.c_int, [P, PF]),
+    "fb_profile": (C.c_int, [P, I32]),
+    "fb_phase_times": (C.c_int, [P, C.POINTER(C.c_double), I32]),
 }
 
 

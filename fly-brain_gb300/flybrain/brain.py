@@ -125,6 +125,16 @@ class BrainBatch:
         nat.check(self.L.fb_last_step_ms(self.h, C.byref(ms)))
         return ms.value
 
+    def profile(self, on: bool = True):
+        nat.check(self.L.fb_profile(self.h, 1 if on else 0))
+
+    def phase_times(self) -> dict:
+        """Accumulated per-phase milliseconds (grid block 0's view) since profile(True)."""
+        ms = (C.c_double * 10)()
+        nat.check(self.L.fb_phase_times(self.h, ms, 10))
+        return dict(zip(("serial", "deliver", "barrier1", "update", "barrier2", "ctl_head",
+                         "ctl_loads", "ctl_draw", "ctl_emit", "ctl_tail"), list(ms)))
+
     def record(self, cap_steps: int, cap_spikes: int = 0):
         nat.check(self.L.fb_record(self.h, int(cap_steps), int(cap_spikes)))
 

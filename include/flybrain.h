@@ -170,6 +170,18 @@ int fb_scalars(fb_brains *br, int32_t b, int32_t *head, uint32_t *rng, int32_t *
 /* Device-side timing of the last fb_step launch (ms, CUDA events on the launch stream). */
 int fb_last_step_ms(fb_brains *br, float *ms);
 
+/* In-library phase timer (no counterpart in the reference, which times stages from JS with
+ * performance.now, scripts/profile_fly.mjs:13-27). fb_profile(br, 1) zeroes and enables it; each
+ * step then adds, as seen by the first block of the grid, the time of: [0] the per-brain serial
+ * part and ring bookkeeping, [1] the delivery work items, [2] the wait at the first barrier,
+ * [3] the neuron update, [4] the wait at the second barrier; within [0], for the brain block 0
+ * serves: [5] the header and background draws, [6] the driven-list gathers, [7] the draws,
+ * [8] the forced spikes' emission, [9] the RNG advance. fb_phase_times copies up to n
+ * accumulated totals in ms. */
+#define FB_NPHASES 10
+int fb_profile(fb_brains *br, int32_t on);
+int fb_phase_times(fb_brains *br, double *ms, int32_t n);
+
 #ifdef __cplusplus
 }
 #endif
