@@ -25,6 +25,15 @@ struct Delta {
 cudaError_t launch_deltas(Trial *trials, const Delta *d, const int32_t *gs, int32_t nGroups, cudaStream_t st);
 cudaError_t launch_reset(Trial *trials, int32_t b0, int32_t b1, cudaStream_t st);
 cudaError_t set_step_smem(size_t bytes);
+struct CompileArgs {
+  int32_t N;
+  const uint32_t *indptr, *indices;
+  const float *counts, *edgeGain, *preSign, *inScale, *outScale;
+  const uint8_t *sensory;
+  double wSyn, inhGain, minSyn, preInh;
+  float *W, *sign;
+};
+cudaError_t launch_compile(const CompileArgs &a, cudaStream_t st);
 }  // namespace fb
 
 using namespace fb;
@@ -224,6 +233,85 @@ extern "C" int fb_graph_create_shared(const fb_graph *topology, const float *wei
   return FB_OK;
 }
 
+// A device-resident view of an argument array: the array itself when it already lives on the
+// device, else a temporary device copy (released by the caller through `tmp`).
+static int device_view(const void *src, size_t bytes, const void **dst, std::vector<void *> &tmp) {
+  *dst = nullptr;
+  if (!src) return FB_OK;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeDevice) {
+    *dst = src;
+    return FB_OK;
+  }
+  cudaGetLastError();
+  void *d = nullptr;
+  CU(cudaMalloc(&d, bytes ? bytes : 1));
+  tmp.push_back(d);
+  CU(cudaMemcpy(d, src, bytes, cudaMemcpyDefault));
+  *dst = d;
+  return FB_OK;
+}
+
+extern "C" int fb_graph_compile(const fb_graph *topology, const float *counts, const float *pre_sign,
+                                const float *in_scale, const float *out_scale,
+                                const uint8_t *sensory_mask, const float *edge_gain,
+                                const fb_compile_params *p, fb_graph **out) {
+  if (!topology || !counts || !pre_sign || !p || !out) return fail(FB_EINVAL, "fb_graph_compile: null argument");
+  *out = nullptr;
+  Topology *t = topology->topo;
+  const size_t N = (size_t)t->N, E = (size_t)t->E;
+  std::vector<void *> tmp;
+  auto release = [&]() { for (void *q : tmp) cudaFree(q); };
+  CompileArgs a;
+  memset(&a, 0, sizeof a);
+  const void *v;
+  int rc;
+#define VIEW(ptr, bytes, field, type)                          \
+  rc = device_view(ptr, bytes, &v, tmp);                       \
+  if (rc) { release(); return rc; }                            \
+  a.field = (const type *)v;
+  VIEW(counts, E * 4, counts, float)
+  VIEW(edge_gain, E * 4, edgeGain, float)
+  VIEW(pre_sign, N * 4, preSign, float)
+  VIEW(in_scale, N * 4, inScale, float)
+  VIEW(out_scale, N * 4, outScale, float)
+  VIEW(sensory_mask, N, sensory, uint8_t)
+#undef VIEW
+  fb_graph *g = new (std::nothrow) fb_graph;
+  if (!g) { release(); return fail(FB_ENOMEM, "host allocation"); }
+  if (cudaMalloc(&g->W, std::max<size_t>(E, 1) * 4) != cudaSuccess || cudaMalloc(&g->sign, N * 4) != cudaSuccess) {
+    cudaFree(g->W); cudaFree(g->sign); delete g; release();
+    return fail(FB_ENOMEM, "fb_graph_compile: device allocation failed");
+  }
+  a.N = t->N;
+  a.indptr = t->indptr;
+  a.indices = t->indices;
+  a.wSyn = p->wSyn;
+  a.inhGain = p->inhGain;
+  a.minSyn = p->minSyn;
+  a.preInh = p->preInh;
+  a.W = g->W;
+  a.sign = g->sign;
+  cudaError_t e = launch_compile(a, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  release();
+  if (e != cudaSuccess) {
+    cudaFree(g->W); cudaFree(g->sign); delete g;
+    return fail(FB_ECUDA, "fb_graph_compile: %s", cudaGetErrorString(e));
+  }
+  t->refs++;
+  g->topo = t;
+  *out = g;
+  return FB_OK;
+}
+
+extern "C" int fb_graph_read(const fb_graph *g, float *weights, float *sign) {
+  if (!g) return fail(FB_EINVAL, "fb_graph_read: null graph");
+  if (weights && g->topo->E) CU(cudaMemcpy(weights, g->W, (size_t)g->topo->E * 4, cudaMemcpyDefault));
+  if (sign) CU(cudaMemcpy(sign, g->sign, (size_t)g->topo->N * 4, cudaMemcpyDefault));
+  return FB_OK;
+}
+
 extern "C" int fb_graph_set_sign(fb_graph *g, const float *sign) {
   if (!g || !sign) return fail(FB_EINVAL, "fb_graph_set_sign: null argument");
   CU(cudaDeviceSynchronize());  // no step may be reading the old vector
@@ -298,6 +386,7 @@ struct fb_brains {
   uint32_t *d_bar = nullptr;   // the grid barrier's counter word (own 128-byte line)
   static constexpr size_t kBarWords = 32;
   unsigned long long *d_phase = nullptr;  // per-phase ns accumulators when profiling
+  uint32_t *d_dbg = nullptr;              // index-check record of checked builds
   int profiling = 0;
   OvfRec *d_ovf[2] = {nullptr, nullptr};
   uint32_t *d_ovfTop = nullptr;
@@ -384,6 +473,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     Trial &T = br->host[b];
     br->dts[b] = p.dt;
     T.N = N;
+    T.E = E;
     T.nslots = ns;
     T.mode = FB_DELIVER_EXACT;
     fill_constants(T, p, N);
@@ -448,6 +538,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
       cudaMalloc(&br->d_tileTrial, sizeof(int32_t) * nTiles) != cudaSuccess ||
       cudaMalloc(&br->d_steps, sizeof(int32_t) * B) != cudaSuccess ||
       cudaMalloc(&br->d_err, sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&br->d_dbg, sizeof(uint32_t) * 4) != cudaSuccess ||
       cudaMalloc(&br->d_bar, sizeof(uint32_t) * fb_brains::kBarWords) != cudaSuccess ||
       cudaMalloc(&br->d_ovfTop, sizeof(uint32_t) * 2) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: batch buffers"));
@@ -459,6 +550,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     if (cudaMalloc(&br->d_ovf[k], sizeof(OvfRec) * (size_t)br->ovfCap) != cudaSuccess)
       return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: overflow pool"));
   if (cudaMemsetAsync(br->d_err, 0, 4, br->stream) != cudaSuccess ||
+      cudaMemsetAsync(br->d_dbg, 0, 16, br->stream) != cudaSuccess ||
       cudaMemsetAsync(br->d_bar, 0, sizeof(uint32_t) * fb_brains::kBarWords, br->stream) != cudaSuccess ||
       cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream) != cudaSuccess ||
       cudaMemcpyAsync(br->d_tileTrial, br->tileTrial.data(), sizeof(int32_t) * nTiles, cudaMemcpyHostToDevice, br->stream) != cudaSuccess ||
@@ -494,6 +586,7 @@ extern "C" int fb_brains_destroy(fb_brains *br) {
   cudaFree(br->trials); cudaFree(br->d_tileTrial); cudaFree(br->d_steps); cudaFree(br->d_err);
   cudaFree(br->d_groups); cudaFree(br->d_deltas); cudaFree(br->d_bar); cudaFree(br->d_ovfTop);
   cudaFree(br->d_phase);
+  cudaFree(br->d_dbg);
   cudaFree(br->d_ovf[0]); cudaFree(br->d_ovf[1]);
   if (br->ev0) cudaEventDestroy(br->ev0);
   if (br->ev1) cudaEventDestroy(br->ev1);
@@ -665,6 +758,7 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     a.ovfCap = br->ovfCap;
     a.log = br->logging;
     a.timeoutNs = 5000000000LL;
+    a.dbg = br->d_dbg;
     CU(cudaEventRecord(br->ev0, br->stream));
     CU(launch_step(a, br->grid, br->smem, br->stream));
     CU(cudaEventRecord(br->ev1, br->stream));
@@ -678,6 +772,11 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
       cudaMemsetAsync(br->d_bar, 0, sizeof(uint32_t) * fb_brains::kBarWords, br->stream);
       cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream);
       cudaStreamSynchronize(br->stream);
+      uint32_t dbg[4] = {0, 0, 0, 0};
+      cudaMemcpy(dbg, br->d_dbg, 16, cudaMemcpyDeviceToHost);
+      cudaMemset(br->d_dbg, 0, 16);
+      if (err == FB_EINVAL)
+        return fail(err, "fb_step: index check failed at site %u (values %u, %u; %u failures)", dbg[0], dbg[1], dbg[2], dbg[3]);
       return fail(err, err == FB_ETIMEOUT ? "fb_step: a device-side wait timed out; the step was abandoned"
                                           : "fb_step: delivery overflow (more than %d contributions to one target in one step, or the pool of %u records is full)",
                   kSortMax, br->ovfCap);

@@ -25,6 +25,7 @@ constexpr int32_t kHasPreInh = 4;    // presynaptic inhibition (forces sequentia
 // LIFWasm._writeHeader stores), graph and state pointers, delivery scratch, dynamic scalars.
 struct Trial {
   int32_t N, nslots, coba, mode;
+  int64_t E;
   float dt, vRest, vThresh, vReset, tRef, adaptInc, depU, dE, dTr, dA, kRec, kM, dtS;
   float eExc, eInh, cE, cI, bgEvents, bgAmp, preInh;
   int32_t tileBase, nTiles, flags, pad0;
@@ -51,7 +52,7 @@ struct Trial {
   // threshold-spike staging per update tile (compacted list + out-degree prefix)
   int32_t *stage;
   uint32_t *stageDeg;
-  int32_t *tileCnt;
+  int32_t *tileCnt;    // [nTiles], indexed by the brain-local tile
   uint32_t *tileDeg;
   // forced-spike staging per driven-list chunk of kBlock entries, two step parities:
   // dStage/dStageDeg [2][maxDch * kBlock], dCnt/dDeg [2][maxDch]; liveTag[maxDch] publishes each
@@ -98,7 +99,29 @@ struct StepArgs {
   uint32_t ovfCap;
   int32_t log;               // 1: record per-step fired counts / lists
   int64_t timeoutNs;
+  uint32_t *dbg;             // checked builds: [site, value, value, count] of the first bad index
 };
+
+// Index checks of the checked build (-DFB_CHECK): a failed check records its site and values in
+// a.dbg (the first one only), sets FB_EINVAL and skips the access. Compiled out otherwise.
+#ifdef FB_CHECK
+#define FB_GUARD(a, cond, site, v1, v2, skip)                                    \
+  do {                                                                           \
+    if (!(cond)) {                                                               \
+      if ((a).dbg && atomicCAS((a).dbg, 0u, (uint32_t)(site)) == 0u) {         \
+        (a).dbg[1] = (uint32_t)(v1);                                            \
+        (a).dbg[2] = (uint32_t)(v2);                                            \
+      }                                                                          \
+      if ((a).dbg) atomicAdd((a).dbg + 3, 1u);                                  \
+      atomicCAS((a).err, 0, FB_EINVAL);                                          \
+      skip;                                                                      \
+    }                                                                            \
+  } while (0)
+#else
+#define FB_GUARD(a, cond, site, v1, v2, skip) \
+  do {                                        \
+  } while (0)
+#endif
 
 // ---- memory helpers --------------------------------------------------------------------------
 // Data written by other blocks during the same launch is read through L2 (ld.global.cg): L1 is
@@ -252,7 +275,7 @@ __device__ __forceinline__ void mark_chunks(uint4 *chunkK, uint32_t o, uint32_t 
                                             uint32_t pre, uint32_t row) {
   const uint32_t end = o + deg;
   const uint4 rec = make_uint4(k, pre, end, row - o);  // edge e of arrival k is row + (e - o)
-  for (uint32_t c = (o + kChunk - 1) / kChunk; c * kChunk < end; c++) chunkK[c] = rec;
+  for (uint32_t c = (o + kChunk - 1) / kChunk; c * kChunk < end; c++) chunkK[c] = rec;  // c < chunkCap: end <= E
 }
 
 }  // namespace fb

@@ -76,7 +76,8 @@ __device__ void driven_item(const StepArgs &a, const Trial &T, Trial *G, int c, 
   // this chunk's entries: one per thread
   const int32_t k = c * kBlock + tid;
   const bool valid = k < nD;
-  const int32_t i = valid ? ldcg(T.driven + k) : 0;
+  int32_t i = valid ? ldcg(T.driven + k) : 0;
+  FB_GUARD(a, i >= 0 && i < N, 5, i, k, i = 0);
   const float rf = ldcg(T.refr + i), dr = ldcg(T.drive + i);
 
   if (c == 0) {
@@ -191,55 +192,74 @@ __device__ void driven_item(const StepArgs &a, const Trial &T, Trial *G, int c, 
   prof_lap(a, 8, tp);
 }
 
-// Copies one staging unit of step `gstep` into its ring slot: units are the brain's driven-list
-// chunks (forced spikes, list order) followed by its update tiles (threshold spikes, ascending),
-// so the slot holds lif.c's order (lif.c:51-52 then :74-76). Each unit's offset is the sum over
-// the units before it; the last unit also writes the list's totals.
-__device__ void materialize_unit(const StepArgs &a, const Trial &T, Trial *G, int u, int nDch,
-                                 uint64_t gstep, int slot, int64_t logBase, uint64_t *scan64) {
-  __shared__ uint32_t sh_cnt, sh_deg;
+// Materializes brain b's fired list of step `gstep` into its ring slot, one block per brain. The
+// staging units are the driven-list chunks (forced spikes, list order) followed by the update
+// tiles (threshold spikes, ascending), so the slot holds lif.c's order (lif.c:51-52 then
+// :74-76). Units are scanned blockDim at a time: counts and out-degree sums give each unit's
+// offset, the non-empty ones are compacted, and the block copies their spikes with each arrival's
+// edge offset, row start and delivery work-item records.
+__device__ void materialize_brain(const StepArgs &a, const Trial &T, Trial *G, int nDch, uint64_t gstep,
+                                  int slot, int64_t logBase, uint64_t *scan64, uint32_t *scan) {
+  __shared__ uint32_t uIdx[kBlock];   // non-empty units of the round (compacted)
+  __shared__ uint32_t uCnt[kBlock], uOff[kBlock], uDeg[kBlock];
   const int tid = threadIdx.x;
-  const int64_t dpar = (int64_t)(gstep & 1) * T.maxDch;
-  const bool drv = u < nDch;
-  const int tt = T.tileBase + (u - nDch);  // tile index when !drv
-  const bool last = u == nDch + T.nTiles - 1;
-  const int32_t m = drv ? ldcg(T.dCnt + dpar + u) : ldcg(T.tileCnt + tt);
-  if (m == 0 && !last) return;  // uniform across the block
-  uint64_t acc = 0;
-  for (int v = tid; v < u; v += blockDim.x) {
-    if (v < nDch) acc += ((uint64_t)(uint32_t)ldcg(T.dCnt + dpar + v) << 32) | ldcg(T.dDeg + dpar + v);
-    else acc += ((uint64_t)(uint32_t)ldcg(T.tileCnt + T.tileBase + v - nDch) << 32) |
-                ldcg(T.tileDeg + T.tileBase + v - nDch);
-  }
-  acc = block_sum(acc, scan64);
-  if (tid == 0) {
-    sh_cnt = (uint32_t)(acc >> 32);
-    sh_deg = (uint32_t)acc;
-  }
-  __syncthreads();
   const int N = T.N;
-  const uint32_t before = sh_cnt, dbefore = sh_deg;
+  const int64_t dpar = (int64_t)(gstep & 1) * T.maxDch;
+  const int nUnits = nDch + T.nTiles;
   int32_t *out = T.ring + (int64_t)slot * N;
   uint32_t *outOff = T.ringOff + (int64_t)slot * (N + 1);
   uint32_t *outRow = T.ringRow + (int64_t)slot * N;
   uint4 *chunkK = T.chunkK + (int64_t)slot * T.chunkCap;
-  const int32_t *stage = drv ? T.dStage + (dpar + u) * kBlock : T.stage + (int64_t)(u - nDch) * kTile;
-  const uint32_t *stageDeg = drv ? T.dStageDeg + (dpar + u) * kBlock : T.stageDeg + (int64_t)(u - nDch) * kTile;
   const bool logging = a.log && T.logRaster != nullptr;
   const int64_t rbase = logging ? ldcg(G->logRasterLen + (gstep & 1)) : 0;
-  for (int p = tid; p < m; p += blockDim.x) {
-    const int32_t i = ldcg(stage + p);
-    const uint32_t k = before + p, o = dbefore + ldcg(stageDeg + p);
-    const uint32_t r0 = __ldg(T.indptr + i), r1 = __ldg(T.indptr + i + 1);
-    out[k] = i;
-    outOff[k] = o;
-    outRow[k] = r0;
-    mark_chunks(chunkK, o, r1 - r0, k, (uint32_t)i, r0);
-    if (logging && rbase + k < T.logRasterCap) T.logRaster[rbase + k] = i;
+  uint32_t cntBase = 0, degBase = 0;
+  for (int u0 = 0; u0 < nUnits; u0 += blockDim.x) {
+    const int u = u0 + tid;
+    uint32_t m = 0, dsum = 0;
+    if (u < nUnits) {
+      if (u < nDch) {
+        m = (uint32_t)ldcg(T.dCnt + dpar + u);
+        dsum = ldcg(T.dDeg + dpar + u);
+      } else {
+        m = (uint32_t)ldcg(T.tileCnt + (u - nDch));  // brain-local tile index
+        dsum = ldcg(T.tileDeg + (u - nDch));
+      }
+    }
+    uint64_t tot;
+    const uint64_t pre = block_exclusive_scan(((uint64_t)m << 32) | dsum, &tot, scan64);
+    uint32_t nz;
+    const uint32_t zpos = block_exclusive_scan(m ? 1u : 0u, &nz, scan);
+    if (m) {
+      uIdx[zpos] = (uint32_t)u;
+      uCnt[zpos] = m;
+      uOff[zpos] = cntBase + (uint32_t)(pre >> 32);
+      uDeg[zpos] = degBase + (uint32_t)pre;
+    }
+    __syncthreads();
+    // each warp copies whole units, warps striding over the non-empty units
+    for (uint32_t z = tid >> 5; z < nz; z += blockDim.x >> 5) {
+      const uint32_t uu = uIdx[z], mm = uCnt[z], before = uOff[z], dbefore = uDeg[z];
+      const bool drv = (int)uu < nDch;
+      const int32_t *stage = drv ? T.dStage + (dpar + uu) * kBlock : T.stage + (int64_t)(uu - nDch) * kTile;
+      const uint32_t *stageDeg = drv ? T.dStageDeg + (dpar + uu) * kBlock : T.stageDeg + (int64_t)(uu - nDch) * kTile;
+      for (uint32_t p = tid & 31; p < mm; p += 32) {
+        const int32_t i = ldcg(stage + p);
+        const uint32_t k = before + p, o = dbefore + ldcg(stageDeg + p);
+        FB_GUARD(a, i >= 0 && i < N && k < (uint32_t)N, 6, i, k, continue);
+        const uint32_t r0 = __ldg(T.indptr + i), r1 = __ldg(T.indptr + i + 1);
+        out[k] = i;
+        outOff[k] = o;
+        outRow[k] = r0;
+        mark_chunks(chunkK, o, r1 - r0, k, (uint32_t)i, r0);
+        if (logging && rbase + k < T.logRasterCap) T.logRaster[rbase + k] = i;
+      }
+    }
+    cntBase += (uint32_t)(tot >> 32);
+    degBase += (uint32_t)tot;
+    __syncthreads();
   }
-  if (last && tid == 0) {
-    const uint32_t nf = before + (uint32_t)m;
-    const uint32_t F = dbefore + (drv ? ldcg(T.dDeg + dpar + u) : ldcg(T.tileDeg + tt));
+  if (tid == 0) {
+    const uint32_t nf = cntBase, F = degBase;
     outOff[nf] = F;
     T.ringCount[slot] = (int32_t)nf;
     T.slotEdges[slot] = F;
@@ -261,15 +281,18 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T,
   const uint32_t e = c * kChunk + lane;
   if (e >= F) return;
   const int N = T.N;
+  FB_GUARD(a, (int64_t)c < T.chunkCap, 1, c, slot, return);
   const uint4 ck = ldcg(T.chunkK + (int64_t)slot * T.chunkCap + c);
   uint32_t k = ck.x, pre = ck.y, j = ck.w + e;
   if (e >= ck.z) {  // a later arrival of this item
     const uint32_t *off = T.ringOff + (int64_t)slot * (N + 1);
     k++;
-    while (ldcg(off + k + 1) <= e) k++;
+    while (k < (uint32_t)N && ldcg(off + k + 1) <= e) k++;
+    FB_GUARD(a, k < (uint32_t)N, 2, k, e, return);
     pre = (uint32_t)ldcg(T.ring + (int64_t)slot * N + k);
     j = ldcg(T.ringRow + (int64_t)slot * N + k) + (e - ldcg(off + k));
   }
+  FB_GUARD(a, pre < (uint32_t)N && (int64_t)j < T.E, 3, pre, j, return);
   // the edge's loads are issued with the presynaptic ones, before the zero-amplitude test
   const uint32_t q = __ldg(T.indices + j);
   const float wj = __ldg(T.W + j);
@@ -282,6 +305,7 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T,
     return;
   }
   const uint32_t key = (k << 1) | (inh ? 1u : 0u);
+  FB_GUARD(a, q < (uint32_t)N, 4, q, j, return);
   const uint32_t pos = atomicAdd(T.cnt + q, 1u);
   if (pos < (uint32_t)kBucket) {
     T.bucket[(int64_t)q * kBucket + pos] = make_uint2(key, __float_as_uint(w));
@@ -321,6 +345,7 @@ __device__ __forceinline__ void apply_contributions(const StepArgs &a, const Tri
   if (spill) {
     uint32_t r = ldcg(T.ovfHead + i);
     while (r != kNil && m < (uint32_t)kSortMax) {
+      FB_GUARD(a, r < a.ovfCap, 7, r, i, break);
       const OvfRec rec = a.ovf[gparity][r];
       e[m++] = make_uint2(rec.key, rec.bits);
       r = rec.next;
@@ -430,6 +455,7 @@ __device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, 
                             uint64_t *scan64) {
   const int tid = threadIdx.x;
   const int local = t - T.tileBase;
+  FB_GUARD(a, local >= 0 && local < T.nTiles, 8, local, t, return);
   const int i0 = local * kTile + tid, i1 = i0 + kBlock;
   const int N = T.N;
   // both neurons' loads are issued before either is stored (the stores could alias them)
@@ -439,8 +465,8 @@ __device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, 
   const uint32_t f1 = i1 < N ? update_neuron(a, T, G, i1, x1, gparity) : 0;
   if (!__syncthreads_or(f0 | f1)) {
     if (tid == 0) {
-      T.tileCnt[t] = 0;
-      T.tileDeg[t] = 0;
+      T.tileCnt[local] = 0;
+      T.tileDeg[local] = 0;
     }
     return;
   }
@@ -462,8 +488,8 @@ __device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, 
     stageDeg[n0 + (cpre >> 16)] = dsum0 + (uint32_t)(dpre >> 32);
   }
   if (tid == 0) {
-    T.tileCnt[t] = (int32_t)(n0 + (ctot >> 16));
-    T.tileDeg[t] = dsum0 + (uint32_t)(dtot >> 32);
+    T.tileCnt[local] = (int32_t)(n0 + (ctot >> 16));
+    T.tileDeg[local] = dsum0 + (uint32_t)(dtot >> 32);
   }
 }
 
@@ -489,8 +515,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
   int32_t *sND = sSteps + a.B;             // driven-list length at launch
   int32_t *sTile0 = sND + a.B;             // B + 1: first update tile of each brain
   int32_t *sDch0 = sTile0 + a.B + 1;       // B + 1: first driven chunk item of each brain
-  int32_t *sU0 = sDch0 + a.B + 1;          // B + 1: first staging unit of each brain
-  uint32_t *sPre = (uint32_t *)(sU0 + a.B + 1);  // B + 1
+  uint32_t *sPre = (uint32_t *)(sDch0 + a.B + 1);  // B + 1
   __shared__ uint32_t scan[33];
   __shared__ uint64_t scan64[33];
   __shared__ uint32_t sJump[32 * 128];
@@ -516,19 +541,18 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
   __syncthreads();
   if (tid == 0) {
     sTile0[a.B] = a.nTilesTotal;
-    int dc = 0, uc = 0;
+    int dc = 0;
     for (int b = 0; b < a.B; b++) {
-      const int nd = max(1, (sND[b] + kBlock - 1) / kBlock);
       sDch0[b] = dc;
-      sU0[b] = uc;
-      dc += nd;
-      uc += nd + (sTile0[b + 1] - sTile0[b]);
+      dc += max(1, (sND[b] + kBlock - 1) / kBlock);
     }
     sDch0[a.B] = dc;
-    sU0[a.B] = uc;
   }
   __syncthreads();
-  auto hdr = [&](int b) -> const Trial & { return b < kTrialCache ? sTr[b] : a.trials[b]; };
+  auto hdr = [&](int b) -> const Trial & {
+    const Trial *p = b < kTrialCache ? (const Trial *)sTr + b : (const Trial *)a.trials + b;
+    return *p;
+  };
   auto find = [&](const int32_t *first, int x) {  // b with first[b] <= x < first[b+1]
     int lo = 0, hi = a.B;
     while (hi - lo > 1) {
@@ -539,7 +563,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
     return lo;
   };
   auto tile_brain = [&](int t) { return find(sTile0, t); };
-  const int nDItems = sDch0[a.B], nUItems = sU0[a.B];
+  const int nDItems = sDch0[a.B];
   const int warpsPerBlock = blockDim.x >> 5;
   const uint32_t gwarp = blockIdx.x * warpsPerBlock + (tid >> 5);
   const uint32_t nwarps = gridDim.x * warpsPerBlock;
@@ -548,7 +572,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
   auto lap = [&](int k) { prof_lap(a, k, tp); };
   for (int s = 0; s <= a.maxSteps; s++) {
     // ---------------- phase A: materialize step s-1, control + deliver step s ----------------
-    for (int item = blockIdx.x; item < nDItems + nUItems; item += gridDim.x) {
+    for (int item = blockIdx.x; item < nDItems + a.B; item += gridDim.x) {
       if (item < nDItems) {
         const int b = find(sDch0, item);
         if (s < sSteps[b]) {
@@ -559,14 +583,13 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
           __syncthreads();
         }
       } else {
-        const int m = item - nDItems;
-        const int b = find(sU0, m);
+        const int b = item - nDItems;
         if (s >= 1 && s <= sSteps[b]) {
           const int ns = sNs[b];
           const int head = (sHead0[b] + s - 1) % ns;
           const uint64_t g = (uint64_t)(sDone[b] + s - 1);
-          materialize_unit(a, hdr(b), a.trials + b, m - sU0[b], sDch0[b + 1] - sDch0[b], g,
-                           (head + ns - 1) % ns, (int64_t)g - sLog[b], scan64);
+          materialize_brain(a, hdr(b), a.trials + b, sDch0[b + 1] - sDch0[b], g, (head + ns - 1) % ns,
+                            (int64_t)g - sLog[b], scan64, scan);
           __syncthreads();
         }
       }
@@ -703,7 +726,7 @@ __global__ void reset_kernel(Trial *trials, int32_t b0, int32_t b1) {
 namespace fb {
 
 size_t step_smem_bytes(int B) {
-  return (size_t)B * 8 * 2 + (size_t)B * 4 * 4 + (size_t)(B + 1) * 4 * 4;
+  return (size_t)B * 8 * 2 + (size_t)B * 4 * 4 + (size_t)(B + 1) * 4 * 3;
 }
 
 int step_kernel_blocks_per_sm(size_t smem) {

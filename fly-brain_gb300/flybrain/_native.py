@@ -27,6 +27,10 @@ class FbParams(C.Structure):
         ("coba", C.c_int32), ("reserved", C.c_int32)]
 
 
+class FbCompileParams(C.Structure):
+    _fields_ = [("wSyn", C.c_double), ("inhGain", C.c_double), ("minSyn", C.c_double), ("preInh", C.c_double)]
+
+
 SIGNATURES = {
     "fb_version": (C.c_int, []),
     "fb_last_error": (C.c_char_p, []),
@@ -35,6 +39,8 @@ SIGNATURES = {
     "fb_graph_create": (C.c_int, [I32, I64, P, P, P, P, C.POINTER(P)]),
     "fb_graph_create_shared": (C.c_int, [P, P, P, C.POINTER(P)]),
     "fb_graph_set_sign": (C.c_int, [P, P]),
+    "fb_graph_compile": (C.c_int, [P, P, P, P, P, P, P, C.POINTER(FbCompileParams), C.POINTER(P)]),
+    "fb_graph_read": (C.c_int, [P, P, P]),
     "fb_graph_info": (C.c_int, [P, PI32, PI64]),
     "fb_graph_destroy": (C.c_int, [P]),
     "fb_brains_create": (C.c_int, [P, I32, C.POINTER(FbParams), I32, P, C.POINTER(P)]),
@@ -71,7 +77,8 @@ _lib = None
 
 
 def lib_path() -> str:
-    return _build.LIB
+    """libflybrain.so, or its index-checked build when FLYBRAIN_CHECKED=1."""
+    return _build.CHECK_LIB if os.environ.get("FLYBRAIN_CHECKED") == "1" else _build.LIB
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:
@@ -83,7 +90,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     if not os.path.exists(path):
         if not build_if_missing:
             raise FlyBrainError(FB_ENODEV, f"{path} is not built")
-        _build.build()
+        _build.build(checked=os.environ.get("FLYBRAIN_CHECKED") == "1")
     L = C.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(L, name)

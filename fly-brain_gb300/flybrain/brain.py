@@ -68,6 +68,43 @@ class DeviceGraph:
         g.indptr = getattr(self, "indptr", None)
         return g
 
+    def compile(self, counts, pre_sign, p: dict, in_scale=None, out_scale=None, sensory_mask=None,
+                edge_gain=None) -> "DeviceGraph":
+        """writeGraph (src/lifwasm.js:14-34) on the device over this graph's topology.
+
+        counts, edge_gain: per edge; pre_sign, in_scale, out_scale (type gain), sensory_mask: per
+        neuron. Arrays may be numpy (host) or torch CUDA tensors. p supplies wSyn, inhGain,
+        minSyn and preInh (merged over DEFAULTS)."""
+        q = dict(DEFAULTS, **p)
+        cp = nat.FbCompileParams(float(q["wSyn"]), float(q["inhGain"]), float(q["minSyn"]), float(q["preInh"] or 0))
+        keep = []
+
+        def arr(x, dt):
+            if x is None:
+                return None
+            if hasattr(x, "data_ptr"):
+                keep.append(x)
+                return x
+            y = np.ascontiguousarray(x, dtype=dt)
+            keep.append(y)
+            return y
+
+        h = C.c_void_p()
+        nat.check(self.L.fb_graph_compile(
+            self.h, nat.ptr(arr(counts, np.float32)), nat.ptr(arr(pre_sign, np.float32)),
+            nat.ptr(arr(in_scale, np.float32)), nat.ptr(arr(out_scale, np.float32)),
+            nat.ptr(arr(sensory_mask, np.uint8)), nat.ptr(arr(edge_gain, np.float32)), C.byref(cp), C.byref(h)))
+        g = DeviceGraph(N=self.N, _handle=h, _keep=self.E)
+        g.indptr = getattr(self, "indptr", None)
+        return g
+
+    def read(self):
+        """(weights f32[E], sign f32[N]) as the device holds them."""
+        w = np.zeros(self.E, dtype=np.float32)
+        s = np.zeros(self.N, dtype=np.float32)
+        nat.check(self.L.fb_graph_read(self.h, nat.ptr(w), nat.ptr(s)))
+        return w, s
+
     def set_sign(self, sign):
         s = np.ascontiguousarray(sign, dtype=np.float32)
         nat.check(self.L.fb_graph_set_sign(self.h, nat.ptr(s)))

@@ -16,7 +16,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libflybrain.so")
-SOURCES = ["fb_step.cu", "fb_api.cu", "fb_adjoint.cu"]
+CHECK_LIB = os.path.join(OUT_DIR, "libflybrain_check.so")
+SOURCES = ["fb_step.cu", "fb_api.cu", "fb_graph.cu", "fb_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--fmad=false"]
 
@@ -35,9 +36,13 @@ def _stale(obj: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
+def build(verbose: bool = False, force: bool = False, checked: bool = False) -> str:
+    """checked=True builds libflybrain_check.so: every data-dependent index in the step kernel is
+    bounds-checked (a failure is recorded and reported by fb_step, the access skipped)."""
     os.makedirs(OUT_DIR, exist_ok=True)
-    obj_dir = os.path.join(OUT_DIR, "obj")
+    obj_dir = os.path.join(OUT_DIR, "obj_check" if checked else "obj")
+    lib = CHECK_LIB if checked else LIB
+    flags = FLAGS + (["-DFB_CHECK"] if checked else [])
     os.makedirs(obj_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(os.path.dirname(ROOT), "include", "flybrain.h"))
@@ -48,7 +53,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         src = os.path.join(CSRC, s)
         obj = os.path.join(obj_dir, s.replace(".cu", ".o"))
         if force or _stale(obj, [src] + headers):
-            jobs.append([cc, *ARCH, *FLAGS, "-c", src, "-o", obj])
+            jobs.append([cc, *ARCH, *flags, "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -60,10 +65,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(run, jobs))
     objs = [os.path.join(obj_dir, s.replace(".cu", ".o")) for s in srcs]
-    if force or jobs or _stale(LIB, objs):
-        run([cc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart_static"])
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        run([cc, "-shared", *ARCH, "-o", lib, *objs, "-lcudart_static"])
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv, checked="--checked" in sys.argv))

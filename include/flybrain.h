@@ -93,6 +93,26 @@ int fb_graph_create(int32_t N, int64_t E, const uint32_t *indptr, const uint32_t
 int fb_graph_create_shared(const fb_graph *topology, const float *weights, const float *sign,
                            fb_graph **out);
 
+/* writeGraph (src/lifwasm.js:14-34) on the device: a new graph over topology's CSR whose sign and
+ * weights are compiled from raw per-edge synapse counts:
+ *   sign[j] = f32(pre_sign[j] * wSyn)
+ *   W[k] = (counts[k] >= minSyn && keep) ? f32(counts[k] * edge_gain[k] * in_scale[q] * ig) : 0
+ *   ig = (pre_sign[j] < 0 ? inhGain : 1) * out_scale[j]
+ *   keep = !sensory_mask[q] || (preInh > 0 && pre_sign[j] < 0)
+ * each product formed in double in that order and rounded once, as the reference's Float32Array
+ * stores round. in_scale, out_scale, sensory_mask and edge_gain may be null (factor 1 / no mask).
+ * Arrays may be host or device pointers: f32 counts[E], edge_gain[E], pre_sign[N], in_scale[N],
+ * out_scale[N] (outScale, the per-presynaptic type gain), u8 sensory_mask[N]. */
+typedef struct fb_compile_params {
+  double wSyn, inhGain, minSyn, preInh;
+} fb_compile_params;
+int fb_graph_compile(const fb_graph *topology, const float *counts, const float *pre_sign,
+                     const float *in_scale, const float *out_scale, const uint8_t *sensory_mask,
+                     const float *edge_gain, const fb_compile_params *p, fb_graph **out);
+
+/* Copies a graph's weights f32[E] and/or sign f32[N] out (either may be null). */
+int fb_graph_read(const fb_graph *g, float *weights, float *sign);
+
 /* Replaces the sign vector, f32[N]. Replaces the direct write into graph.sign that
  * src/sim/neuromod.js:107 performs through brain.mem; every brain on this graph sees it. */
 int fb_graph_set_sign(fb_graph *g, const float *sign);

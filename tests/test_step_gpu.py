@@ -169,3 +169,49 @@ def test_invalid_arguments_are_rejected():
     # the handle still works after rejected calls
     b.set_drive(0, [1, 2], [100.0, 100.0])
     b.step(10)
+
+
+def _six_brain_batch():
+    """Six brains (more than the kernel caches headers for) of uneven sizes, each against the
+    oracle, bit for bit."""
+    from oracle import oracle as O
+    from flybrain import BrainBatch, DeviceGraph, SYNTH_PARAMS, synth_graph
+    rng = np.random.default_rng(6)
+    sizes = (2100, 900, 4000, 1500, 3100, 700)
+    graphs = [synth_graph(n, 60 + k) for k, n in enumerate(sizes)]
+    batch = BrainBatch([DeviceGraph(g) for g in graphs], SYNTH_PARAMS, list(range(1, 7)))
+    steps = rng.integers(300, 900, len(sizes)).astype(np.int32)
+    oracles = []
+    for b, g in enumerate(graphs):
+        idx = rng.choice(g.N, min(g.N // 4, 700), replace=False).astype(np.int32)
+        hz = rng.uniform(50, 250, idx.shape[0])
+        batch.set_drive(b, idx, hz)
+        ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, SYNTH_PARAMS, seed=b + 1)
+        for i, h in zip(idx, hz):
+            ob.setDriveOne(int(i), float(h))
+        oracles.append(ob)
+    batch.record(int(steps.max()), 1 << 21)
+    batch.step_uneven(steps)
+    for b, ob in enumerate(oracles):
+        c0, r0 = ob.run(int(steps[b]), raster=True)
+        c1, r1 = batch.spike_log(b, int(steps[b]), 1 << 21)
+        np.testing.assert_array_equal(c1, c0)
+        np.testing.assert_array_equal(r1, r0)
+        assert ob.v.tobytes() == batch.read("v", b).tobytes()
+
+
+def test_batch_more_brains_than_cached_headers():
+    _six_brain_batch()
+
+
+def test_checked_build_finds_no_bad_index():
+    """The same batch under the index-checked library (every data-dependent index bounds-checked
+    on the device, failures reported by fb_step) in a fresh process."""
+    import subprocess
+    import sys
+    from conftest import ROOT
+    code = ("import sys; sys.path[:0] = [%r, %r, %r]; import test_step_gpu as t; t._six_brain_batch()"
+            % (ROOT, os.path.join(ROOT, "fly-brain_gb300"), os.path.dirname(os.path.abspath(__file__))))
+    env = dict(os.environ, FLYBRAIN_CHECKED="1")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
