@@ -114,6 +114,15 @@ static void build_jump_tables(std::vector<uint32_t> &tab) {
       }
 }
 
+namespace fb {
+// The jump tables and the error slot, for the allocation-free entry point.
+void host_jump_tables(std::vector<uint32_t> &tab) { build_jump_tables(tab); }
+int set_error(int code, const char *msg) {
+  g_err = msg;
+  return code;
+}
+}  // namespace fb
+
 static std::mutex g_dev_mu;
 static uint32_t *g_jump[64];
 

@@ -31,6 +31,20 @@ class FbCompileParams(C.Structure):
     _fields_ = [("wSyn", C.c_double), ("inhGain", C.c_double), ("minSyn", C.c_double), ("preInh", C.c_double)]
 
 
+class FbBrainView(C.Structure):
+    """fb_brain_view: the reference Brain header with device-pointer arrays."""
+    _fields_ = ([("N", C.c_int32), ("nslots", C.c_int32), ("head", C.c_int32), ("coba", C.c_int32)]
+                + [(k, C.c_float) for k in ("dt", "vRest", "vThresh", "vReset", "tRef", "adaptInc", "depU",
+                                            "dE", "dTr", "dA", "kRec", "kM", "dtS", "eExc", "eInh", "cE", "cI")]
+                + [("rng", C.c_uint32)]
+                + [(k, C.c_void_p) for k in ("v", "gE", "gI", "refr", "trace", "adapt", "res", "bias",
+                                             "thr", "drive", "sign", "spikeCount", "indptr", "indices",
+                                             "weights", "ring", "ringCount", "driven")]
+                + [("nDriven", C.c_int32), ("nFired", C.c_int32), ("lastSlot", C.c_int32)]
+                + [(k, C.c_float) for k in ("bgEvents", "bgAmp", "bgAcc", "preInh")]
+                + [("E", C.c_int64)])
+
+
 SIGNATURES = {
     "fb_version": (C.c_int, []),
     "fb_last_error": (C.c_char_p, []),
@@ -64,6 +78,7 @@ SIGNATURES = {
     "fb_last_step_ms": (C.c_int, [P, PF]),
     "fb_profile": (C.c_int, [P, I32]),
     "fb_phase_times": (C.c_int, [P, C.POINTER(C.c_double), I32]),
+    "fb_lif_step_noalloc": (C.c_int, [C.POINTER(FbBrainView), I32, P]),
 }
 
 

@@ -202,6 +202,48 @@ int fb_last_step_ms(fb_brains *br, float *ms);
 int fb_profile(fb_brains *br, int32_t on);
 int fb_phase_times(fb_brains *br, double *ms, int32_t n);
 
+/* ---- allocation-free step ----------------------------------------------------------------- */
+
+/* A caller-owned brain for fb_lif_step_noalloc: the fields of the reference's Brain header
+ * (src/wasm/lif.c:4-25, as LIFWasm._writeHeader fills it) with every array a DEVICE pointer the
+ * caller allocated, plus the edge count E (= indptr[N]). Sizes: f32[N] v gE gI refr trace adapt
+ * res bias thr drive sign; u32[N] spikeCount; u32[N+1] indptr; u32[E] indices; f32[E] weights;
+ * i32[nslots * N] ring; i32[nslots] ringCount; i32[N] driven (the first nDriven entries are the
+ * driven list, in insertion order). A fresh brain has v = vRest, res = 1, everything else zero. */
+typedef struct fb_brain_view {
+  int32_t N, nslots, head, coba;
+  float dt, vRest, vThresh, vReset, tRef, adaptInc, depU;
+  float dE, dTr, dA, kRec, kM, dtS, eExc, eInh, cE, cI;
+  uint32_t rng;
+  float *v, *gE, *gI, *refr, *trace, *adapt, *res, *bias, *thr, *drive, *sign;
+  uint32_t *spikeCount;
+  const uint32_t *indptr, *indices;
+  const float *weights;
+  int32_t *ring, *ringCount;
+  int32_t *driven;
+  int32_t nDriven;
+  int32_t nFired, lastSlot;
+  float bgEvents, bgAmp, bgAcc, preInh;
+  int64_t E;
+} fb_brain_view;
+
+/* nsteps brain steps on caller-owned memory, allocating nothing -- no counterpart in the
+ * reference (whose lif_step allocates nothing either, but also runs no GPU kernels). For callers
+ * that may not call cudaMalloc/cudaFree: code inside a CUDA graph capture, a host framework that
+ * owns all device memory through its own pool, or a real-time loop where the implicit device
+ * synchronisation of an allocation is not allowed. The step's scratch is a file-scope __device__
+ * array of 32 MiB that every GPU loading this library holds until exit; a brain must fit it
+ * (about N = 20,000 neurons with 1.2M edges and a 19-slot ring), larger ones are rejected with
+ * FB_EINVAL (use fb_brains_create). Results are those of fb_step, bit for bit. On return the
+ * view's head, rng, bgAcc, nFired and lastSlot hold the state after the last step, and
+ * ring[lastSlot * N ...] its fired list. stream: a cudaStream_t (NULL: the legacy default stream);
+ * the call synchronises it before returning. The first call on a device sets the device up (it
+ * looks up the scratch array's device address and writes the xorshift jump tables into it), so
+ * make that first call before any stream capture. Every call shares the one array and keeps the
+ * last call's contents, so each call clears what must start at zero first; calls that overlap on
+ * the GPU race on the array: serialise them. */
+int fb_lif_step_noalloc(fb_brain_view *brain, int32_t nsteps, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
