@@ -34,6 +34,9 @@ import numpy as np  # noqa: E402
 METRIC = "synaptic events/s & sim-s/wall-s at 165k LIF; batched fwd+adjoint vs plain fwd"
 BRAIN_STEPS_PER_BENCH_STEP = int(os.environ.get("FB_BRAIN_STEPS", "1000"))
 L2_FLUSH_BYTES = 512 << 20
+# DRAM bytes (read + write) per brain step of the single-trial full-scale step kernel, from one
+# ncu capture of a 100-step launch (16.83 MB); traffic grows in proportion to steps.
+DRAM_BYTES_PER_STEP_SINGLE = 16.826112e6 / 100
 
 
 def peaks():
@@ -223,7 +226,7 @@ def run_ours(args, rank, world):
                  d2h_bytes_per_step=d2h // args.steps, sim_s_per_wall_s=sim_s / e2e_s),
         gpu_launches=args.steps,
         roofline=dict(bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
-                      peak_kind=kind, traffic=None,
+                      peak_kind=kind, traffic=DRAM_BYTES_PER_STEP_SINGLE * S,
                       kernel="fb::step_kernel (persistent, all phases)",
                       algorithmic_bytes_per_launch=per_launch_bytes),
         clocks=clk.summary(),
