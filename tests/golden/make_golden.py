@@ -143,8 +143,21 @@ def cases():
     return out
 
 
+def adjoint_fixture():
+    """The 600-neuron induced subgraph with its raw synapse counts and transmitter classes, the
+    input scripts/grad_check.mjs:45-46 builds for the adjoint check."""
+    if not os.path.exists(f"{REF}/public/data/graph_w3.bin"):
+        return
+    n, ip, ix, cnt, nt = real_subgraph(600)
+    os.makedirs(os.path.join(HERE, "adjoint"), exist_ok=True)
+    path = os.path.join(HERE, "adjoint", "real_subgraph_counts.npz")
+    np.savez_compressed(path, N=np.int32(n), indptr=ip, indices=ix, counts=cnt, nt=nt)
+    print(f"real_subgraph_counts: N={n} E={len(ix)} -> {os.path.getsize(path)} bytes")
+
+
 def main():
     O.build(ref=True)
+    adjoint_fixture()
     for name, g, params, seed, script in cases():
         brain = O.OracleBrain(len(g["sign"]), g["indptr"], g["indices"], g["W"], g["sign"], params,
                               seed=seed, backend="ref")
