@@ -787,8 +787,8 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
       if (err == FB_EINVAL)
         return fail(err, "fb_step: index check failed at site %u (values %u, %u; %u failures)", dbg[0], dbg[1], dbg[2], dbg[3]);
       return fail(err, err == FB_ETIMEOUT ? "fb_step: a device-side wait timed out; the step was abandoned"
-                                          : "fb_step: delivery overflow (more than %d contributions to one target in one step, or the pool of %u records is full)",
-                  kSortMax, br->ovfCap);
+                                          : "fb_step: delivery overflow (the pool of %u overflow records for one step is full)",
+                  br->ovfCap);
     }
   }
   if (out_nfired) {

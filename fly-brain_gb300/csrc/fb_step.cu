@@ -329,8 +329,11 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T,
 // ---------------------------------------------------------------------------------------------
 
 // Adds target i's contributions in ascending key (arrival rank) order; inhibitory keys go to gI.
-__device__ __forceinline__ void apply_contributions(const StepArgs &a, const Trial &T, Trial *G, int i, uint32_t n,
-                                                    uint32_t gparity, float &ge, float &gi) {
+// Up to kSortMax contributions are sorted in local memory; beyond that they are applied in
+// successive windows of the kSortMax smallest keys above the last one applied (keys are unique
+// per target: one contribution per arrival).
+__device__ void apply_contributions(const StepArgs &a, const Trial &T, Trial *G, int i, uint32_t n,
+                                    uint32_t gparity, float &ge, float &gi) {
   const uint2 *bk = T.bucket + (int64_t)i * kBucket;
   if (n == 1) {
     const uint2 x = ldcg(bk);
@@ -339,33 +342,42 @@ __device__ __forceinline__ void apply_contributions(const StepArgs &a, const Tri
     return;
   }
   uint2 e[kSortMax];
-  uint32_t m = n < (uint32_t)kBucket ? n : (uint32_t)kBucket;
-  for (uint32_t u = 0; u < m; u++) e[u] = ldcg(bk + u);
-  const bool spill = n > (uint32_t)kBucket;
-  if (spill) {
-    uint32_t r = ldcg(T.ovfHead + i);
-    while (r != kNil && m < (uint32_t)kSortMax) {
-      FB_GUARD(a, r < a.ovfCap, 7, r, i, break);
-      const OvfRec rec = a.ovf[gparity][r];
-      e[m++] = make_uint2(rec.key, rec.bits);
-      r = rec.next;
+  const uint32_t nb = n < (uint32_t)kBucket ? n : (uint32_t)kBucket;
+  bool any = false;
+  uint32_t last = 0;
+  for (uint32_t done = 0; done < n;) {
+    uint32_t m = 0;
+    auto offer = [&](uint2 x) {  // keep the kSortMax smallest keys above `last`, sorted
+      if (any && x.x <= last) return;
+      if (m == (uint32_t)kSortMax && x.x >= e[m - 1].x) return;
+      uint32_t w = m < (uint32_t)kSortMax ? m++ : m - 1;
+      while (w > 0 && e[w - 1].x > x.x) {
+        e[w] = e[w - 1];
+        w--;
+      }
+      e[w] = x;
+    };
+    for (uint32_t u = 0; u < nb; u++) offer(ldcg(bk + u));
+    if (n > (uint32_t)kBucket)
+      for (uint32_t r = ldcg(T.ovfHead + i), hops = 0; r != kNil && hops < n; hops++) {
+        FB_GUARD(a, r < a.ovfCap, 7, r, i, break);
+        const OvfRec rec = a.ovf[gparity][r];
+        offer(make_uint2(rec.key, rec.bits));
+        r = rec.next;
+      }
+    if (m == 0) {  // fewer entries than counted: the overflow pool ran out
+      atomicCAS(a.err, 0, FB_EOVERFLOW);
+      break;
     }
-    T.ovfHead[i] = kNil;
-    if (r != kNil) atomicCAS(a.err, 0, FB_EOVERFLOW);  // more than kSortMax in one step
-  }
-  for (uint32_t u = 1; u < m; u++) {  // insertion sort by key
-    const uint2 x = e[u];
-    uint32_t w = u;
-    while (w > 0 && e[w - 1].x > x.x) {
-      e[w] = e[w - 1];
-      w--;
+    for (uint32_t u = 0; u < m; u++) {
+      if (e[u].x & 1u) gi = __fadd_rn(gi, __uint_as_float(e[u].y));
+      else ge = __fadd_rn(ge, __uint_as_float(e[u].y));
     }
-    e[w] = x;
+    last = e[m - 1].x;
+    any = true;
+    done += m;
   }
-  for (uint32_t u = 0; u < m; u++) {
-    if (e[u].x & 1u) gi = __fadd_rn(gi, __uint_as_float(e[u].y));
-    else ge = __fadd_rn(ge, __uint_as_float(e[u].y));
-  }
+  if (n > (uint32_t)kBucket) T.ovfHead[i] = kNil;
 }
 
 // A neuron's state as loaded at the start of the update phase.

@@ -45,6 +45,27 @@ class FbBrainView(C.Structure):
                 + [("E", C.c_int64)])
 
 
+class FbDiffParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in (
+        "dt", "vRest", "vThresh", "vReset", "tauM", "tauSyn", "tRef", "delay", "wSyn", "adaptInc",
+        "adaptTau", "depU", "depTau", "minSyn", "eExc", "eInh", "inhGain", "sizeAlpha",
+        "maxSizeScale", "boostCap", "kcThreshold", "laminaBias", "surrogateBeta", "adjClip")] + [
+        (k, C.c_int32) for k in ("coba", "soft", "checkpoint", "pad")]
+
+
+class FbDiffNet(C.Structure):
+    _fields_ = [("N", C.c_int32), ("nDriven", C.c_int32), ("E", C.c_int64)] + [
+        (k, C.c_void_p) for k in ("indptr", "indices", "counts", "edge_gain", "sign", "size_log",
+                                  "in_scale", "log_gain", "out_scale", "thr_offset", "beta", "bias",
+                                  "thr_mask", "bias_mask", "sensory", "drive", "driven")]
+
+
+class FbDiffGrads(C.Structure):
+    _fields_ = [("params", C.c_double * 9), ("clamped_params", C.c_int32),
+                ("clamped_log_gain", C.c_int32), ("log_gain", C.c_void_p), ("edge", C.c_void_p),
+                ("bias", C.c_void_p), ("out_scale", C.c_void_p)]
+
+
 SIGNATURES = {
     "fb_version": (C.c_int, []),
     "fb_last_error": (C.c_char_p, []),
@@ -79,6 +100,14 @@ SIGNATURES = {
     "fb_profile": (C.c_int, [P, I32]),
     "fb_phase_times": (C.c_int, [P, C.POINTER(C.c_double), I32]),
     "fb_lif_step_noalloc": (C.c_int, [C.POINTER(FbBrainView), I32, P]),
+    "fb_diff_default_params": (None, [C.POINTER(FbDiffParams)]),
+    "fb_diff_create": (C.c_int, [C.POINTER(FbDiffNet), I64, C.POINTER(P)]),
+    "fb_diff_destroy": (C.c_int, [P]),
+    "fb_diff_set": (C.c_int, [P, I32, P]),
+    "fb_diff_forward": (C.c_int, [P, C.POINTER(FbDiffParams), I32, U32, I32, P]),
+    "fb_diff_tape": (C.c_int, [P, P, P, P, I64, PI64]),
+    "fb_diff_raster": (C.c_int, [P, I32, P, P]),
+    "fb_diff_backward": (C.c_int, [P, P, I32, P, I32, I32, C.POINTER(FbDiffGrads)]),
 }
 
 

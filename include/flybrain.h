@@ -202,6 +202,92 @@ int fb_last_step_ms(fb_brains *br, float *ms);
 int fb_profile(fb_brains *br, int32_t on);
 int fb_phase_times(fb_brains *br, double *ms, int32_t n);
 
+/* ---- the differentiable brain (LIFDiff) and its adjoint ------------------------------------ */
+
+/* Model parameters of LIFDiff (src/lifdiff.js:85-110): the brain step's parameters plus the nine
+ * differentiable globals and the gradient options. coba 1 is the reference's conductance-based
+ * model; 0 a current-based variant (lif.c's current-based membrane, src/wasm/lif.c:67). soft 1
+ * replaces the hard threshold by a logistic in the forward pass too (src/lifdiff.js:101). */
+typedef struct fb_diff_params {
+  double dt, vRest, vThresh, vReset, tauM, tauSyn, tRef, delay;
+  double wSyn, adaptInc, adaptTau, depU, depTau, minSyn;
+  double eExc, eInh, inhGain, sizeAlpha, maxSizeScale, boostCap;
+  double kcThreshold, laminaBias, surrogateBeta, adjClip;
+  int32_t coba, soft, checkpoint, pad;
+} fb_diff_params;
+
+/* Fills *p with the defaults of src/lifdiff.js:86-109 (checkpoint 16, conductance-based). */
+void fb_diff_default_params(fb_diff_params *p);
+
+/* The network of a differentiable brain (src/lifdiff.js:84-145), host or device arrays:
+ * CSR over raw synapse counts (indptr u32[N+1], indices u32[E], counts f32[E]); sign f32[N]
+ * (before wSyn); optional: edge_gain f32[E], size_log / in_scale / log_gain / out_scale /
+ * thr_offset / beta / bias f32[N], thr_mask / bias_mask / sensory u8[N]; the drive (drive f32[N]
+ * in Hz and the driven set in insertion order, nDriven entries). bias is an additive per-neuron
+ * current (mV) on top of bias_mask * laminaBias; it has no counterpart in LIFDiff, whose only bias
+ * is laminaBias, and defaults to none. Fields given as null cannot be set later. */
+typedef struct fb_diff_net {
+  int32_t N, nDriven;
+  int64_t E;
+  const uint32_t *indptr, *indices;
+  const float *counts, *edge_gain, *sign, *size_log, *in_scale, *log_gain, *out_scale;
+  const float *thr_offset, *beta, *bias;
+  const uint8_t *thr_mask, *bias_mask, *sensory;
+  const float *drive;
+  const int32_t *driven;
+} fb_diff_net;
+
+/* Gradients returned by fb_diff_backward (host arrays; each pointer may be null):
+ * params[9] in the reference's order wSyn sizeAlpha inhGain eInh vThresh kcThreshold laminaBias
+ * adaptInc depU (src/lifdiff.js:75); log_gain f32[N] (:658); edge f64[E]: dLoss/dW_j of each gated
+ * edge's effective weight W_j = count * edge_gain * in_scale[post] (* inhGain); bias f64[N]:
+ * dLoss/d per-neuron bias; out_scale f64[N]: dLoss/d out_scale (= log_gain / out_scale).
+ * Non-finite values are zeroed and counted (src/lifdiff.js:681-684). */
+typedef struct fb_diff_grads {
+  double params[9];
+  int32_t clamped_params, clamped_log_gain;
+  float *log_gain;
+  double *edge, *bias, *out_scale;
+} fb_diff_grads;
+
+typedef struct fb_diff fb_diff; /* opaque */
+
+#define FB_DIFF_LOG_GAIN 0
+#define FB_DIFF_OUT_SCALE 1
+#define FB_DIFF_THR_OFFSET 2
+#define FB_DIFF_BIAS 3
+#define FB_DIFF_EDGE_GAIN 4
+#define FB_DIFF_DRIVE 5
+
+/* new LIFDiff(data, opts) (src/lifdiff.js:84): uploads the network. tape_cap bounds the spike
+ * tape (entries over all steps; 0: 64 N, at least 1M). */
+int fb_diff_create(const fb_diff_net *net, int64_t tape_cap, fb_diff **out);
+int fb_diff_destroy(fb_diff *d);
+
+/* Replaces one per-neuron (or, for FB_DIFF_EDGE_GAIN, per-edge) array given at creation. */
+int fb_diff_set(fb_diff *d, int32_t field, const float *values);
+
+/* forward(steps, {seed, record}) (src/lifdiff.js:219-353): runs from reset; spike_count (f32[N],
+ * host or device, may be null) receives the per-neuron spike totals (soft amplitudes summed).
+ * record keeps the tape and a state checkpoint every p->checkpoint steps for fb_diff_backward. */
+int fb_diff_forward(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed, int32_t record,
+                    float *spike_count);
+
+/* The recorded forward's spike tape: offsets i64[steps+1] (step t's spikes are entries
+ * offsets[t] .. offsets[t+1]-1, forced spikes first), neuron indices and amplitudes (up to cap
+ * entries; *len gets the total). */
+int fb_diff_tape(fb_diff *d, int64_t *offsets, int32_t *idx, float *amp, int64_t cap, int64_t *len);
+
+/* The recorded forward's spikes of nro readout neurons as a dense raster out f32[steps][nro]
+ * (amplitudes; host or device). */
+int fb_diff_raster(fb_diff *d, int32_t nro, const int32_t *readout, float *out);
+
+/* backward(tape, dLdSpike, {truncate, lossFrom}) (src/lifdiff.js:494-686) over the recorded
+ * forward. dL: f32[N] applied at every scored step (nro == 0), or f32[steps][nro] over the readout
+ * neurons `readout` (a per-step generalisation of dLdSpikePerEpoch, :519-522). */
+int fb_diff_backward(fb_diff *d, const float *dL, int32_t nro, const int32_t *readout, int32_t truncate,
+                     int32_t loss_from, fb_diff_grads *g);
+
 /* ---- allocation-free step ----------------------------------------------------------------- */
 
 /* A caller-owned brain for fb_lif_step_noalloc: the fields of the reference's Brain header

@@ -1,0 +1,159 @@
+"""The differentiable brain step and its adjoint on the GPU (fb_diff_*) against the oracle's
+restatement of LIFDiff, and against central finite differences of the GPU's own forward pass.
+
+Tolerances: both sides compute in double with float32 state and the same per-target summation
+order, so the hard-spike forward is bit-identical (tape and spike counts); gradients differ only
+by summation order of a warp's gather and of per-target inScale sums (double vs the reference's
+float32) and by the device exp(): relative 1e-5 (plus 1e-9 absolute). Finite differences use the
+tolerance of scripts/grad_check.mjs:98."""
+import numpy as np
+import pytest
+
+from adjoint_problem import H, P0, grad_check_inputs, within_tolerance
+
+pytestmark = pytest.mark.gpu
+REL, ABS = 1e-5, 1e-9
+
+
+def _pair(ins, params, driven=None, hz=None):
+    from oracle.lifdiff_oracle import DiffProblem
+    from flybrain.diff import DiffNet
+    prob = DiffProblem(**ins, params=params, driven=driven, drive_hz=hz)
+    data = dict(N=ins["N"], indptr=ins["indptr"], indices=ins["indices"], weights=ins["counts"], sign=ins["sign"])
+    opts = dict(params)
+    for k_src, k_dst in (("sizeLog", "sizeLog"), ("thrMask", "thrMask"), ("biasMask", "biasMask"),
+                         ("logGain", "logGain"), ("outScale", "outScale"), ("thrOffset", "thrOffset")):
+        if ins.get(k_src) is not None:
+            opts[k_dst] = ins[k_src]
+    net = DiffNet(data, opts)
+    if driven is not None:
+        for i, h in zip(driven, hz):
+            net.setDriveOne(int(i), float(h))
+    return prob, net
+
+
+def _close(a, b, rel=REL, abs_=ABS):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    same = (a == b) | (np.isnan(a) & np.isnan(b))  # non-finite entries must agree exactly
+    with np.errstate(invalid="ignore"):
+        near = np.abs(a - b) <= rel * np.maximum(np.abs(a), np.abs(b)) + abs_
+    return bool(np.all(same | near))
+
+
+def _compare_grads(g0, g1, E_check=True):
+    for k, v in g0["params"].items():
+        assert _close(v, g1["params"][k]), (k, v, g1["params"][k])
+    assert _close(g0["logGain"], g1["logGain"], abs_=1e-7)
+    assert _close(g0["gBias"], g1["bias"])
+    if E_check:
+        assert _close(g0["gEdge"], g1["edge"], abs_=1e-9)
+
+
+def test_soft_gradients_match_oracle():
+    ins, target = grad_check_inputs()
+    prob, net = _pair(ins, P0)
+    dL = np.zeros(ins["N"], np.float32)
+    dL[target] = 1
+    sc0, tape = prob.forward(60)
+    g0 = prob.backward(tape, dL)
+    sc1 = net.forward(60)
+    assert _close(sc0, sc1, rel=1e-6)
+    g1 = net.backward(dL)
+    _compare_grads(g0, g1)
+
+
+@pytest.mark.parametrize("name", ["wSyn", "vThresh", "depU", "sizeAlpha"])
+def test_soft_gradient_matches_gpu_finite_difference(name):
+    ins, target = grad_check_inputs()
+    _, net = _pair(ins, P0)
+    dL = np.zeros(ins["N"], np.float32)
+    dL[target] = 1
+    L = float(net.forward(60)[target].astype(np.float64).sum())
+    g = net.backward(dL)["params"][name]
+    h = H[name]
+    lp = float(net.forward(60, record=False, **{name: P0[name] + h})[target].astype(np.float64).sum())
+    lm = float(net.forward(60, record=False, **{name: P0[name] - h})[target].astype(np.float64).sum())
+    fd = (lp - lm) / (2 * h)
+    ok, rel = within_tolerance(g, fd, h, L)
+    assert ok, (name, g, fd, rel)
+
+
+def _hard_inputs():
+    ins, target = grad_check_inputs(seed=7)
+    ins["logGain"] = np.zeros(ins["N"], np.float32)  # exp(0) = 1 exactly on both sides
+    rng = np.random.default_rng(7)
+    driven = rng.choice(ins["N"], 40, replace=False).astype(np.int32)
+    hz = rng.uniform(50, 250, 40)
+    # the hard-spike adjoint grows exponentially on this very active recurrent subgraph (about
+    # 1e8 after 120 steps with beta = 2; with the fast-sigmoid slope 25/mV, beta = 0.04, it
+    # overflows within a few hundred steps, identically on both sides): comparisons of finite
+    # gradients use beta = 2 over 120 steps
+    params = dict(coba=True, soft=False, surrogateBeta=2.0, wSyn=0.5, minSyn=3.0, adaptInc=0.3,
+                  depU=0.1, laminaBias=9.0, kcThreshold=2.0, inhGain=0.8, sizeAlpha=0.5, checkpoint=16)
+    return ins, target, driven, hz, params
+
+
+def test_hard_forward_tape_is_identical_to_oracle():
+    ins, target, driven, hz, params = _hard_inputs()
+    prob, net = _pair(ins, params, driven, hz)
+    sc0, tape = prob.forward(400, seed=3)
+    sc1 = net.forward(400, seed=3)
+    off, idx, amp = net.tape()
+    np.testing.assert_array_equal(off, tape["off"])
+    np.testing.assert_array_equal(idx, tape["idx"])
+    np.testing.assert_array_equal(amp, tape["amp"])
+    assert sc0.tobytes() == sc1.tobytes()
+    assert tape["forced"].sum() > 0 and idx.shape[0] > 1000
+
+
+def test_hard_gradients_match_oracle():
+    ins, target, driven, hz, params = _hard_inputs()
+    prob, net = _pair(ins, params, driven, hz)
+    dL = np.zeros(ins["N"], np.float32)
+    dL[target] = 1
+    _, tape = prob.forward(120, seed=3)
+    g0 = prob.backward(tape, dL)
+    net.forward(120, seed=3)
+    g1 = net.backward(dL)
+    assert all(np.isfinite(v) for v in g1["params"].values()) and np.isfinite(g1["edge"]).all()
+    _compare_grads(g0, g1)
+
+
+def test_steep_surrogate_nonfinite_values_agree():
+    """With the steep surrogate the adjoint overflows; both sides zero and count the same
+    non-finite gradients (src/lifdiff.js:681-684)."""
+    ins, target, driven, hz, params = _hard_inputs()
+    prob, net = _pair(ins, dict(params, surrogateBeta=0.04), driven, hz)
+    dL = np.zeros(ins["N"], np.float32)
+    dL[target] = 1
+    _, tape = prob.forward(400, seed=3)
+    g0 = prob.backward(tape, dL)
+    net.forward(400, seed=3)
+    g1 = net.backward(dL)
+    assert g1["clamped"]["params"] == g0["clamped"][0] and g1["clamped"]["logGain"] == g0["clamped"][1]
+    _compare_grads(g0, g1)
+
+
+def test_readout_loss_truncation_clip_current_based():
+    """Per-step loss over a readout set, lossFrom, truncated BPTT and the adjoint clip, with the
+    current-based membrane."""
+    ins, target, driven, hz, params = _hard_inputs()
+    params = dict(params, coba=False, adjClip=5.0, checkpoint=25)
+    prob, net = _pair(ins, params, driven, hz)
+    steps = 160
+    rng = np.random.default_rng(1)
+    readout = np.sort(rng.choice(ins["N"], 50, replace=False)).astype(np.int32)
+    dLro = rng.normal(0, 1, (steps, readout.shape[0])).astype(np.float32)
+    dense = np.zeros((steps, ins["N"]), np.float32)
+    dense[:, readout] = dLro
+    _, tape = prob.forward(steps, seed=5, checkpoint=25)
+    g0 = prob.backward(tape, dense, truncate=40, lossFrom=20)
+    net.forward(steps, seed=5)
+    g1 = net.backward(dLro, truncate=40, lossFrom=20, readout=readout)
+    _compare_grads(g0, g1)
+    r = net.raster(readout)
+    off, idx, amp = net.tape()
+    t = int(np.argmax([off[k + 1] - off[k] for k in range(steps)]))
+    for i, a in zip(idx[off[t]:off[t + 1]], amp[off[t]:off[t + 1]]):
+        if i in set(readout.tolist()):
+            assert r[t, int(np.searchsorted(readout, i))] == a

@@ -215,3 +215,32 @@ def test_checked_build_finds_no_bad_index():
     env = dict(os.environ, FLYBRAIN_CHECKED="1")
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_synchronous_burst_into_one_target():
+    """~150 presynaptic spikes reach one neuron in the same step: more contributions than a
+    target's in-place bucket and local sort hold, still summed in the reference's order."""
+    from oracle import oracle as O
+    from flybrain import DeviceGraph, LIFCuda, SYNTH_PARAMS
+    N = 500
+    rows = [[499, (p * 7) % 450 + 40] if p < 300 else [(p * 13) % 499] for p in range(N)]
+    rows = [sorted(set(r)) for r in rows]
+    indptr = np.zeros(N + 1, np.uint32)
+    indptr[1:] = np.cumsum([len(r) for r in rows])
+    indices = np.concatenate([np.array(r, np.uint32) for r in rows])
+    rng = np.random.default_rng(3)
+    W = rng.uniform(0.5, 3.0, indices.shape[0]).astype(np.float32)
+    sign = np.where(rng.random(N) < 0.7, 1.0, -1.0).astype(np.float32)
+    p = dict(SYNTH_PARAMS)
+    ob = O.OracleBrain(N, indptr, indices, W, sign, p, seed=9)
+    gb = LIFCuda(DeviceGraph(N=N, indptr=indptr, indices=indices, weights=W, sign=sign), p, seed=9)
+    for i in range(300):
+        ob.setDriveOne(i, 4000.0)
+        gb.setDriveOne(i, 4000.0)
+    c0, r0 = ob.run(400, raster=True)
+    c1, r1 = gpu_multistep(gb, 400)
+    np.testing.assert_array_equal(c1, c0)
+    np.testing.assert_array_equal(r1, r0)
+    assert c0.max() > 100
+    for k in ("v", "gE", "gI"):
+        assert getattr(ob, k).tobytes() == getattr(gb, k).tobytes(), k
