@@ -231,6 +231,11 @@ def run_ours(args, rank, world):
                       algorithmic_bytes_per_launch=per_launch_bytes),
         clocks=clk.summary(),
     )
+    if os.environ.get("FB_BENCH_ADJOINT", "1") == "1":
+        del brain
+        torch.cuda.empty_cache()
+        res["adjoint"] = run_adjoint(g, idx, hz)
+        brain = None
     if os.environ.get("FB_BENCH_BATCHED", "1") == "1":
         del brain
         torch.cuda.empty_cache()
@@ -303,6 +308,73 @@ def run_batched(g, args, n_trials=256, seed=7):
                        "U{500..4000} neurons at U(50,250) Hz, 64 cell-type gains lognormal(0,0.2); "
                        "one persistent launch, uneven steps; state in HBM (no L2 flush needed: "
                        "the batch's state is ~60 GB)")
+
+
+def run_adjoint(g, idx, hz, steps=5000, seed=3):
+    """The differentiable workload: surrogate-gradient LIF (fast-sigmoid slope 25/mV, beta 0.04)
+    on the full graph, 500 ms at dt 0.1 ms, checkpoint every 100 steps; loss = MSE between 20 ms
+    low-pass rates of 1,000 seeded readout neurons and a seeded 0-80 Hz target; gradients for
+    every edge gain, every neuron's bias and 64 cell-type gains through the autograd function.
+    The adjoint is bounded with the reference's adjClip (100, the value of its loom refit) since
+    the steep surrogate's adjoint overflows on this graph otherwise. Arithmetic: float32
+    intermediates (FB_ADJ_PRECISION=f64 for the reference's double). Reports forward+backward
+    time against the plain (unrecorded) forward of the same window, and the library's own
+    forward/backward times."""
+    import torch
+    from flybrain.autograd import DiffContext, LIFDiffFunction, lowpass_rates
+    from flybrain.diff import DiffNet
+    prec = os.environ.get("FB_ADJ_PRECISION", "f32")
+    rng = np.random.default_rng(seed)
+    data = dict(N=g.N, indptr=g.indptr, indices=g.indices, weights=g.counts.astype(np.float32), sign=g.sign)
+    opts = dict(dt=0.1, vRest=-52.0, vThresh=-45.0, vReset=-52.0, tauM=20.0, tauSyn=5.0, tRef=2.2,
+                delay=1.8, wSyn=0.275, coba=False, soft=False, surrogateBeta=0.04, adjClip=100.0,
+                checkpoint=100, adaptInc=0.0, depU=0.0, precision=prec, edgeGain=np.ones(g.E, np.float32),
+                bias=np.zeros(g.N, np.float32), outScale=np.ones(g.N, np.float32))
+    net = DiffNet(data, opts, tape_cap=1 << 26)
+    for i, h in zip(idx.tolist(), hz.tolist()):
+        net.setDriveOne(i, h)
+    readout = np.sort(rng.choice(g.N, 1000, replace=False))
+    dctx = DiffContext(net, g.cell_type, readout, steps)
+    target = torch.as_tensor(rng.uniform(0, 80, (1, 1000)), dtype=torch.float32, device="cuda")
+    eg = torch.ones(g.E, device="cuda", requires_grad=True)
+    bias = torch.zeros(g.N, device="cuda", requires_grad=True)
+    tg = torch.as_tensor(rng.lognormal(0, 0.2, 64), dtype=torch.float32, device="cuda").requires_grad_()
+
+    def clock(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    net.forward(steps, record=False)  # warm-up (allocations)
+    _, plain = clock(lambda: net.forward(steps, record=False))
+    _, lib_fwd = clock(lambda: net.forward(steps, record=True))
+    dro = np.zeros((steps, readout.shape[0]), np.float32)
+    net.backward(dro, readout=readout)  # warm-up (arena allocation)
+    _, lib_bwd = clock(lambda: net.backward(dro, readout=readout))
+    for p_ in (eg, bias, tg):
+        p_.grad = None
+
+    def fwd():
+        raster = LIFDiffFunction.apply(eg, bias, tg, dctx)
+        return ((lowpass_rates(raster, 0.1) - target) ** 2).mean()
+
+    loss, fwd_s = clock(fwd)
+    _, bwd_s = clock(loss.backward)
+    sim_s = steps * 0.1 / 1000
+    ge, gb, gt = eg.grad, bias.grad, tg.grad
+    return dict(neurons=g.N, edges=g.E, steps=steps, checkpoint=100, sim_s=sim_s, precision=prec,
+                plain_forward_s=plain, library_forward_recorded_s=lib_fwd, library_backward_s=lib_bwd,
+                autograd_forward_s=fwd_s, autograd_backward_s=bwd_s,
+                fwd_bwd_per_trial_s=(fwd_s + bwd_s) / sim_s, plain_per_trial_s=plain / sim_s,
+                cost_vs_plain_forward=(fwd_s + bwd_s) / plain, loss=float(loss),
+                spikes=int(net.tape()[0][-1]),
+                grads=dict(edge_nonzero=int((ge != 0).sum()), edge_finite=bool(torch.isfinite(ge).all()),
+                           bias_nonzero=int((gb != 0).sum()), type_gain=[float(x) for x in gt[:4]]),
+                config="surrogate-gradient LIF (beta 0.04, adjClip 100), N=165,122, 500 ms at dt 0.1 ms, "
+                       "K=100; MSE of 20 ms low-pass rates of 1,000 readouts vs a 0-80 Hz target; "
+                       "gradients for every edge gain, bias and 64 type gains (autograd)")
 
 
 def run_reference(args, rank, world):

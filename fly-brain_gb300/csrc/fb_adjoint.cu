@@ -49,6 +49,7 @@ struct DiffDev {
   const float *inScale;
   const uint8_t *gate;
   const double *P;
+  const float *Pf;
   // state
   float *v, *gE, *gI, *adapt, *res, *refr, *spikeCount;
   uint8_t *isForced;
@@ -87,28 +88,42 @@ struct DiffDev {
   const uint32_t *jump;
 };
 
-__device__ __forceinline__ double d_bias(const DiffDev &D, int i, double *lam) {
-  const double l = (D.biasMask && D.biasMask[i]) ? D.laminaBias : 0.0;
+// Model constants in the arithmetic type R of a pass: double reproduces the reference's
+// arithmetic (JS numbers); float is the GB300 fast mode (the FP64 pipes are a small fraction of
+// the FP32 ones). Built on the host from the double parameters, each rounded once.
+template <typename R>
+struct DP {
+  R dt, vRest, vThresh, vReset, tRef, wSyn, adaptInc, depU, eExc, eInh, inhGain;
+  R kcThreshold, laminaBias, beta, adjClip, dE, dA, kRec, kM, dtS, cE, cI;
+};
+
+template <typename R>
+__device__ __forceinline__ R d_bias(const DiffDev &D, const DP<R> &P, int i, R *lam) {
+  const R l = (D.biasMask && D.biasMask[i]) ? P.laminaBias : R(0);
   if (lam) *lam = l;
-  return D.biasArr ? l + (double)D.biasArr[i] : l;
+  return D.biasArr ? l + (R)D.biasArr[i] : l;
 }
-__device__ __forceinline__ double d_kc(const DiffDev &D, int i) {
-  return (D.thrMask && D.thrMask[i]) ? D.kcThreshold : 0.0;
+template <typename R>
+__device__ __forceinline__ R d_kc(const DiffDev &D, const DP<R> &P, int i) {
+  return (D.thrMask && D.thrMask[i]) ? P.kcThreshold : R(0);
 }
-__device__ __forceinline__ double d_beta(const DiffDev &D, int i) {
-  return D.betaArr ? (double)D.betaArr[i] : D.beta;
+template <typename R>
+__device__ __forceinline__ R d_beta(const DiffDev &D, const DP<R> &P, int i) {
+  return D.betaArr ? (R)D.betaArr[i] : P.beta;
 }
-__device__ __forceinline__ double d_out(const DiffDev &D, int i) {
-  return D.outScale ? (double)D.outScale[i] : 1.0;
+template <typename R>
+__device__ __forceinline__ R d_out(const DiffDev &D, int i) {
+  return D.outScale ? (R)D.outScale[i] : R(1);
 }
 // u = v + (vRest - v + gE (eExc - v) cE + gI (v - eInh) cI + bias) kM   (src/lifdiff.js:327)
 // current-based: u = v + (vRest - v + gE + gI + bias) kM              (src/wasm/lif.c:67)
-__device__ __forceinline__ double d_u(const DiffDev &D, double vv, double ge, double gi, double bias) {
-  if (D.coba) return vv + (D.vRest - vv + ge * (D.eExc - vv) * D.cE + gi * (vv - D.eInh) * D.cI + bias) * D.kM;
-  return vv + (D.vRest - vv + ge + gi + bias) * D.kM;
+template <typename R>
+__device__ __forceinline__ R d_u(const DiffDev &D, const DP<R> &P, R vv, R ge, R gi, R bias) {
+  if (D.coba) return vv + (P.vRest - vv + ge * (P.eExc - vv) * P.cE + gi * (vv - P.eInh) * P.cI + bias) * P.kM;
+  return vv + (P.vRest - vv + ge + gi + bias) * P.kM;
 }
 
-// inScale, gate and P (src/lifdiff.js:158-172; P folds the first two factors of :281-282).
+// inScale (src/lifdiff.js:158-164).
 __global__ void k_prepare(DiffDev D, float *inScale, uint8_t *gate, double *P, const float *sizeLog,
                           const float *inScaleSrc, const uint8_t *sensory, double sizeAlpha,
                           double maxSizeScale, double boostCap, double minSyn) {
@@ -120,10 +135,11 @@ __global__ void k_prepare(DiffDev D, float *inScale, uint8_t *gate, double *P, c
       inScale[i] = (float)fmin(boostCap, fmax(1.0 / maxSizeScale, s));
     }
   }
-  __threadfence();
 }
 
-__global__ void k_prepare_edges(DiffDev D, const float *inScale, uint8_t *gate, double *P,
+// The gate (src/lifdiff.js:167-171) and P[j] = (count * edgeGain) * inScale[q], the first factors
+// of the delivered amount (:281-282), in double and in float.
+__global__ void k_prepare_edges(DiffDev D, const float *inScale, uint8_t *gate, double *P, float *Pf,
                                 const uint8_t *sensory, double minSyn) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
   for (int64_t j = tid; j < D.E; j += nt) {
@@ -131,6 +147,7 @@ __global__ void k_prepare_edges(DiffDev D, const float *inScale, uint8_t *gate, 
     const double c = (double)D.counts[j];
     gate[j] = (c >= minSyn && !(sensory && sensory[q])) ? 1 : 0;
     P[j] = c * (D.edgeGain ? (double)D.edgeGain[j] : 1.0) * (double)inScale[q];
+    Pf[j] = D.counts[j] * (D.edgeGain ? D.edgeGain[j] : 1.f) * inScale[q];
   }
 }
 
@@ -148,7 +165,8 @@ __global__ void k_reset(DiffDev D) {
 // Delivery of the arrivals at step t (the spikes of step t - (nslots-1)), warp per arrival
 // (src/lifdiff.js:276-283): lane 0 forms eff and depresses res; lanes push (rank, edge) per
 // gated edge into the target's bucket. resRow (replay) records res[pre] per arrival.
-__global__ void k_deliver(DiffDev D, int32_t t, float *resRow) {
+template <typename R>
+__global__ void k_deliver(DiffDev D, DP<R> P, int32_t t, float *resRow) {
   const int e = t - (D.nslots - 1);
   if (e < 0) return;
   const int64_t a0 = D.tOff[e], na = D.tOff[e + 1] - a0;
@@ -157,16 +175,16 @@ __global__ void k_deliver(DiffDev D, int32_t t, float *resRow) {
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t k = w0; k < na; k += nw) {
     const int32_t pre = D.tIdx[a0 + k];
-    const double sg = D.sign[pre];
-    double eff = 0;
+    const float sg = D.sign[pre];
     if (lane == 0) {
+      R eff = 0;
       if (sg != 0) {
-        const double r = D.res[pre];
+        const R r = D.res[pre];
         if (resRow) resRow[k] = (float)r;
-        eff = sg * D.wSyn * d_out(D, pre) * exp((double)D.logGain[pre]) * r * (double)D.tAmp[a0 + k];
-        D.res[pre] = (float)(r - D.depU * r);
+        eff = (R)sg * P.wSyn * d_out<R>(D, pre) * exp((R)D.logGain[pre]) * r * (R)D.tAmp[a0 + k];
+        D.res[pre] = (float)(r - P.depU * r);
       }
-      D.effK[k] = eff;
+      D.effK[k] = (double)eff;
     }
     if (sg == 0) continue;
     const uint32_t lo = D.indptr[pre], hi = D.indptr[pre + 1];
@@ -194,9 +212,10 @@ __global__ void k_deliver(DiffDev D, int32_t t, float *resRow) {
 }
 
 // Forced spikes of step t (src/lifdiff.js:290-297), one block. Forward: one draw per
-// non-refractory driven neuron in drivenSet order, compared in double against drive * dt/1000;
-// each spike goes to the head of step t's tape list. Replay: the tape's forced list.
-__global__ void k_forced(DiffDev D, int32_t t, int32_t replay) {
+// non-refractory driven neuron in drivenSet order, compared (in R) against drive * dt/1000; each
+// spike goes to the head of step t's tape list. Replay: the tape's forced list.
+template <typename R>
+__global__ void k_forced(DiffDev D, DP<R> P, int32_t t, int32_t replay) {
   __shared__ uint32_t sJump[32 * 128];
   __shared__ uint32_t scan[33];
   __shared__ uint32_t sh_s0;
@@ -206,8 +225,8 @@ __global__ void k_forced(DiffDev D, int32_t t, int32_t replay) {
     const int32_t nf = D.tForced[t];
     for (int k = tid; k < nf; k += blockDim.x) {
       const int32_t i = D.tIdx[base + k];
-      D.refr[i] = (float)(D.tRef + D.dt);
-      D.adapt[i] = (float)((double)D.adapt[i] + D.adaptInc);
+      D.refr[i] = (float)(P.tRef + P.dt);
+      D.adapt[i] = (float)((R)D.adapt[i] + P.adaptInc);
       D.isForced[i] = 1;
     }
     return;
@@ -221,17 +240,19 @@ __global__ void k_forced(DiffDev D, int32_t t, int32_t replay) {
     const int32_t k = r0 + tid;
     int32_t i = 0;
     uint32_t live = 0;
+    float dr = 0.f;
     if (k < D.nDriven) {
       i = D.driven[k];
       live = D.refr[i] > 0 ? 0u : 1u;
+      dr = D.drive[i];
     }
     uint32_t nlive;
     const uint32_t dpos = block_exclusive_scan(live, &nlive, scan);
     uint32_t fire = 0;
     if (live) {
       const uint32_t x = xs_jump(sJump, s0, draws + dpos + 1);
-      const double u = (double)(x >> 8) * (1.0 / 16777216.0);
-      fire = u < (double)D.drive[i] * D.dtS ? 1u : 0u;
+      const R u = (R)(x >> 8) * (R)(1.0 / 16777216.0);
+      fire = u < (R)dr * P.dtS ? 1u : 0u;
     }
     uint32_t nfire;
     const uint32_t fpos = block_exclusive_scan(fire, &nfire, scan);
@@ -243,9 +264,9 @@ __global__ void k_forced(DiffDev D, int32_t t, int32_t replay) {
       } else {
         atomicCAS(D.err, 0, FB_EOVERFLOW);
       }
-      D.refr[i] = (float)(D.tRef + D.dt);
-      D.spikeCount[i] = (float)((double)D.spikeCount[i] + 1);
-      D.adapt[i] = (float)((double)D.adapt[i] + D.adaptInc);
+      D.refr[i] = (float)(P.tRef + P.dt);
+      D.spikeCount[i] = (float)((R)D.spikeCount[i] + R(1));
+      D.adapt[i] = (float)((R)D.adapt[i] + P.adaptInc);
       D.isForced[i] = 1;
     }
     draws += nlive;
@@ -257,18 +278,20 @@ __global__ void k_forced(DiffDev D, int32_t t, int32_t replay) {
   }
 }
 
-// Adds target i's bucket in arrival-rank order: gE (or gI) = f32(f64(g) + P[j] (*inhGain) * eff).
+// Adds target i's bucket in arrival-rank order: gE (or gI) = f32(g + P[j] (*inhGain) * eff) in R.
 // Up to kDSortMax contributions are sorted in local memory; beyond that they are applied in
 // successive windows of the kDSortMax smallest ranks above the last one applied (ranks are unique
 // per target: one contribution per arrival).
-__device__ __forceinline__ void d_add(const DiffDev &D, uint2 c, float &geF, float &giF) {
-  const double eff = D.effK[c.x];
-  const double p = D.P[c.y];
-  if (eff > 0) geF = (float)((double)geF + p * eff);
-  else giF = (float)((double)giF + p * D.inhGain * eff);
+template <typename R>
+__device__ __forceinline__ void d_add(const DiffDev &D, const DP<R> &Pp, uint2 c, float &geF, float &giF) {
+  const R eff = (R)D.effK[c.x];
+  const R p = sizeof(R) == 8 ? (R)D.P[c.y] : (R)D.Pf[c.y];
+  if (eff > 0) geF = (float)((R)geF + p * eff);
+  else giF = (float)((R)giF + p * Pp.inhGain * eff);
 }
 
-__device__ void d_apply(const DiffDev &D, int i, uint32_t n, double &ge, double &gi, float &geF, float &giF) {
+template <typename R>
+__device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, float &geF, float &giF) {
   uint2 e[kDSortMax];
   const uint2 *bk = D.bucket + (int64_t)i * kDBucket;
   const uint32_t nb = n < (uint32_t)kDBucket ? n : (uint32_t)kDBucket;
@@ -297,33 +320,32 @@ __device__ void d_apply(const DiffDev &D, int i, uint32_t n, double &ge, double 
       atomicCAS(D.err, 0, FB_EOVERFLOW);
       break;
     }
-    for (uint32_t u = 0; u < m; u++) d_add(D, e[u], geF, giF);
+    for (uint32_t u = 0; u < m; u++) d_add<R>(D, Pp, e[u], geF, giF);
     last = e[m - 1].x;
     any = true;
     done += m;
   }
   if (n > (uint32_t)kDBucket) D.ovfHead[i] = kNil;
-  ge = geF;
-  gi = giF;
 }
 
 // Integrate and spike (src/lifdiff.js:313-344), one thread per neuron; with `row` >= 0 it also
 // records the replay arena (:439-456). Spikes above the tape threshold are staged per tile.
-__global__ void k_update(DiffDev D, int32_t row) {
+template <typename R>
+__global__ void k_update(DiffDev D, DP<R> P, int32_t row) {
   __shared__ uint32_t scan[33];
   const int tid = threadIdx.x, i = blockIdx.x * blockDim.x + tid;
   bool emit = false;
   float amp = 0.f;
   if (i < D.N) {
     float geF = D.gE[i], giF = D.gI[i];
-    double ge = geF, gi = giF;
     const uint32_t n = D.cnt[i];
     if (n) {
-      d_apply(D, i, n, ge, gi, geF, giF);
+      d_apply<R>(D, P, i, n, geF, giF);
       D.cnt[i] = 0;
     }
+    const R ge = geF, gi = giF;
     const int64_t off = row >= 0 ? (int64_t)row * D.N + i : 0;
-    double vi = D.v[i], s = 0;
+    R vi = D.v[i], s = 0;
     int md = 0;
     if (row >= 0) {
       D.aV[off] = D.v[i];
@@ -335,8 +357,8 @@ __global__ void k_update(DiffDev D, int32_t row) {
     if (forced) D.isForced[i] = 0;
     const bool wasRefr = refr > 0;
     if (wasRefr) {
-      refr = (float)((double)refr - D.dt);
-      vi = D.vReset;
+      refr = (float)((R)refr - P.dt);
+      vi = P.vReset;
       if (forced) {
         md = 2;
         s = 1;
@@ -344,24 +366,24 @@ __global__ void k_update(DiffDev D, int32_t row) {
         md = 1;
       }
     } else {
-      vi = d_u(D, vi, ge, gi, d_bias(D, i, nullptr));
+      vi = d_u<R>(D, P, vi, ge, gi, d_bias<R>(D, P, i, nullptr));
     }
-    geF = (float)(ge * D.dE);
-    giF = (float)(gi * D.dE);
-    float ad = (float)((double)D.adapt[i] * D.dA);
-    const double rs = D.res[i];
-    D.res[i] = (float)(rs + (1 - rs) * D.kRec);
+    geF = (float)(ge * P.dE);
+    giF = (float)(gi * P.dE);
+    float ad = (float)((R)D.adapt[i] * P.dA);
+    const R rs = D.res[i];
+    D.res[i] = (float)(rs + (R(1) - rs) * P.kRec);
     if (row >= 0) D.aAd[off] = ad;
     if (!wasRefr) {
-      const double thr = D.vThresh + (double)ad + d_kc(D, i) + (double)D.thrOffset[i];
-      s = D.soft ? 1 / (1 + exp(-(vi - thr) / d_beta(D, i))) : (vi >= thr ? 1 : 0);
+      const R thr = P.vThresh + (R)ad + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
+      s = D.soft ? R(1) / (R(1) + exp(-(vi - thr) / d_beta<R>(D, P, i))) : (vi >= thr ? R(1) : R(0));
       if (s > 0) {
-        vi = s * D.vReset + (1 - s) * vi;
-        if (!D.soft) refr = (float)D.tRef;
-        ad = (float)((double)ad + s * D.adaptInc);
+        vi = s * P.vReset + (R(1) - s) * vi;
+        if (!D.soft) refr = (float)P.tRef;
+        ad = (float)((R)ad + s * P.adaptInc);
       }
-      D.spikeCount[i] = (float)((double)D.spikeCount[i] + s);
-      if (s > (D.soft ? 1e-4 : 0.5)) {
+      D.spikeCount[i] = (float)((R)D.spikeCount[i] + s);
+      if (s > (D.soft ? R(1e-4) : R(0.5))) {
         emit = true;
         amp = (float)s;
       }
@@ -419,39 +441,40 @@ __global__ void k_emit(DiffDev D, int32_t t) {
 }
 
 // Reverse of integrate-and-spike at step t (src/lifdiff.js:555-617), with the adjoint clip
-// (:623-629) fused: one thread per neuron.
-__global__ void k_bneuron(DiffDev D, int32_t t, int32_t row, int32_t scored) {
+// (:623-629) fused: one thread per neuron. Scalar terms accumulate per neuron in double.
+template <typename R>
+__global__ void k_bneuron(DiffDev D, DP<R> P, int32_t t, int32_t row, int32_t scored) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.N) return;
   const int64_t off = (int64_t)row * D.N + i;
   float *ls = D.lsRing + (int64_t)(t % D.nslots) * D.N;
   const int md = D.aMode[off];
-  const double lpA = D.lad[i];
-  const double lE = (double)D.lgE[i] * D.dE, lI = (double)D.lgI[i] * D.dE, lA = lpA * D.dA;
-  const double lR = (double)D.lres[i] * (1 - D.kRec);
+  const R lpA = D.lad[i];
+  const R lE = (R)D.lgE[i] * P.dE, lI = (R)D.lgI[i] * P.dE, lA = lpA * P.dA;
+  const R lR = (R)D.lres[i] * (R(1) - P.kRec);
   float lvF = D.lv[i], lgEF = (float)lE, lgIF = (float)lI, ladF = (float)lA, lresF = (float)lR;
   if (md == 1) {
     lvF = 0.f;
   } else if (md == 2) {
-    D.accA[i] += lA;
+    D.accA[i] += (double)lA;
     lvF = 0.f;
     ls[i] = 0.f;
   } else {
-    const double vv = D.aV[off], gEv = D.aGE[off], gIv = D.aGI[off];
-    double lam;
-    const double bias = d_bias(D, i, &lam);
-    const double u = d_u(D, vv, gEv, gIv, bias);
-    const double thr = D.vThresh + (double)D.aAd[off] + d_kc(D, i) + (double)D.thrOffset[i];
-    const double d = u - thr;
-    const double s = D.aSp[off];
-    const double beta = d_beta(D, i);
-    double sg;
-    if (D.soft) sg = s * (1 - s) / beta;
+    const R vv = D.aV[off], gEv = D.aGE[off], gIv = D.aGI[off];
+    R lam;
+    const R bias = d_bias<R>(D, P, i, &lam);
+    const R u = d_u<R>(D, P, vv, gEv, gIv, bias);
+    const R thr = P.vThresh + (R)D.aAd[off] + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
+    const R d = u - thr;
+    const R s = D.aSp[off];
+    const R beta = d_beta<R>(D, P, i);
+    R sg;
+    if (D.soft) sg = s * (R(1) - s) / beta;
     else {
-      const double tt = 1 + fabs(d) / beta;
-      sg = 1 / (beta * tt * tt);
+      const R tt = R(1) + fabs(d) / beta;
+      sg = R(1) / (beta * tt * tt);
     }
-    double dl = 0;
+    R dl = 0;
     if (scored && D.dL) {
       if (D.roMap) {
         const int c = D.roMap[i];
@@ -460,33 +483,33 @@ __global__ void k_bneuron(DiffDev D, int32_t t, int32_t row, int32_t scored) {
         dl = D.dL[i];
       }
     }
-    const double lspike = (double)ls[i] + dl;
-    const double lvNew = lvF;
-    const double lsTot = (D.vReset - u) * lvNew + lpA * D.adaptInc + lspike;
-    const double lt = lsTot * (1 - 0.0) * sg;
-    const double lu = lvNew * (1 - s) + lt;
-    const double lthr = -lt;
-    D.accA[i] += lpA * s;
-    D.accV[i] += lthr;
-    if (D.thrMask && D.thrMask[i]) D.accKc[i] += lthr;
-    ladF = (float)(lA + lthr * D.dA);
+    const R lspike = (R)ls[i] + dl;
+    const R lvNew = lvF;
+    const R lsTot = (P.vReset - u) * lvNew + lpA * P.adaptInc + lspike;
+    const R lt = lsTot * R(1) * sg;
+    const R lu = lvNew * (R(1) - s) + lt;
+    const R lthr = -lt;
+    D.accA[i] += (double)(lpA * s);
+    D.accV[i] += (double)lthr;
+    if (D.thrMask && D.thrMask[i]) D.accKc[i] += (double)lthr;
+    ladF = (float)(lA + lthr * P.dA);
     if (D.coba) {
-      lvF = (float)(lu * (1 + D.kM * (-1 - gEv * D.cE + gIv * D.cI)));
-      lgEF = (float)(lE + lu * D.kM * (D.eExc - vv) * D.cE);
-      lgIF = (float)(lI + lu * D.kM * (vv - D.eInh) * D.cI);
-      D.accEI[i] += lu * D.kM * gIv * D.cI * (-1 + (vv - D.eInh) * D.cI);
+      lvF = (float)(lu * (R(1) + P.kM * (R(-1) - gEv * P.cE + gIv * P.cI)));
+      lgEF = (float)(lE + lu * P.kM * (P.eExc - vv) * P.cE);
+      lgIF = (float)(lI + lu * P.kM * (vv - P.eInh) * P.cI);
+      D.accEI[i] += (double)(lu * P.kM * gIv * P.cI * (R(-1) + (vv - P.eInh) * P.cI));
     } else {
-      lvF = (float)(lu * (1 - D.kM));
-      lgEF = (float)(lE + lu * D.kM);
-      lgIF = (float)(lI + lu * D.kM);
+      lvF = (float)(lu * (R(1) - P.kM));
+      lgEF = (float)(lE + lu * P.kM);
+      lgIF = (float)(lI + lu * P.kM);
     }
-    if (lam != 0) D.accLa[i] += lu * D.kM;
-    D.gBias[i] += lu * D.kM;
+    if (lam != 0) D.accLa[i] += (double)(lu * P.kM);
+    D.gBias[i] += (double)(lu * P.kM);
     ls[i] = 0.f;
   }
-  const double c = D.adjClip;
+  const R c = P.adjClip;
   if (c > 0) {
-    auto cl = [c](float x) { return (float)((double)x > c ? c : ((double)x < -c ? -c : (double)x)); };
+    auto cl = [c](float x) { return (float)((R)x > c ? c : ((R)x < -c ? -c : (R)x)); };
     lvF = cl(lvF); lgEF = cl(lgEF); lgIF = cl(lgIF); ladF = cl(ladF); lresF = cl(lresF);
   }
   D.lv[i] = lvF;
@@ -499,7 +522,8 @@ __global__ void k_bneuron(DiffDev D, int32_t t, int32_t row, int32_t scored) {
 // Reverse of the delivery at step t (src/lifdiff.js:635-666), warp per arrival: lanes gather the
 // fan-out's adjoint into lRaw (a fixed-order warp sum) and add each gated edge's
 // dLoss/dW_j = lg[q] * eff to its accumulator; lane 0 updates the presynaptic neuron's terms.
-__global__ void k_barrival(DiffDev D, int32_t t, const float *resRow) {
+template <typename R>
+__global__ void k_barrival(DiffDev D, DP<R> P, int32_t t, const float *resRow) {
   const int e = t - (D.nslots - 1);
   if (e < 0) return;
   const int64_t a0 = D.tOff[e], na = D.tOff[e + 1] - a0;
@@ -509,38 +533,36 @@ __global__ void k_barrival(DiffDev D, int32_t t, const float *resRow) {
   float *target = D.lsRing + (int64_t)(e % D.nslots) * D.N;
   for (int64_t k = w0; k < na; k += nw) {
     const int32_t pre = D.tIdx[a0 + k];
-    const double sgn = D.sign[pre];
+    const R sgn = D.sign[pre];
     if (sgn == 0) continue;
-    const double amp = D.tAmp[a0 + k];
-    const double resAtv = resRow[k];
-    const double gain = exp((double)D.logGain[pre]) * d_out(D, pre);
-    const double base = sgn * D.wSyn * gain * resAtv;
-    const double eff = base * amp;
+    const R amp = D.tAmp[a0 + k];
+    const R resAtv = resRow[k];
+    const R gain = exp((R)D.logGain[pre]) * d_out<R>(D, pre);
+    const R base = sgn * P.wSyn * gain * resAtv;
+    const R eff = base * amp;
     const bool exc = eff > 0;
     const uint32_t lo = D.indptr[pre], hi = D.indptr[pre + 1];
-    double lraw = 0;
+    R lraw = 0;
     for (uint32_t j = lo + lane; j < hi; j += 32) {
       if (!D.gate[j]) continue;
       const uint32_t q = D.indices[j];
-      const double lg = exc ? (double)D.lgE[q] : (double)D.lgI[q];
-      const double cw = (double)D.counts[j] * (D.edgeGain ? (double)D.edgeGain[j] : 1.0);
-      lraw += exc ? lg * cw * (double)D.inScale[q] : lg * cw * (double)D.inScale[q] * D.inhGain;
-      D.gEdge[j] += lg * eff;
+      const R lg = exc ? (R)D.lgE[q] : (R)D.lgI[q];
+      const R cw = (R)D.counts[j] * (D.edgeGain ? (R)D.edgeGain[j] : R(1));
+      lraw += exc ? lg * cw * (R)D.inScale[q] : lg * cw * (R)D.inScale[q] * P.inhGain;
+      D.gEdge[j] += (double)(lg * eff);
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) lraw += __shfl_xor_sync(0xffffffffu, lraw, o);
     if (lane == 0) {
-      D.accW[pre] += lraw * sgn * gain * resAtv * amp;
-      D.gLog[pre] += lraw * eff;
-      if (e >= 0) {
-        float x = (float)((double)target[pre] + lraw * base);
-        if (D.adjClip > 0) x = (float)fmin(D.adjClip, fmax(-D.adjClip, (double)x));
-        target[pre] = x;
-      }
-      const double lresAfter = D.lres[pre];
-      D.accD[pre] += -lresAfter * resAtv;
-      float y = (float)(lresAfter * (1 - D.depU) + lraw * sgn * D.wSyn * gain * amp);
-      if (D.adjClip > 0) y = (float)fmin(D.adjClip, fmax(-D.adjClip, (double)y));
+      D.accW[pre] += (double)(lraw * sgn * gain * resAtv * amp);
+      D.gLog[pre] += (double)(lraw * eff);
+      float x = (float)((R)target[pre] + lraw * base);
+      if (P.adjClip > 0) x = (float)fmin(P.adjClip, fmax(-P.adjClip, (R)x));
+      target[pre] = x;
+      const R lresAfter = D.lres[pre];
+      D.accD[pre] += (double)(-lresAfter * resAtv);
+      float y = (float)(lresAfter * (R(1) - P.depU) + lraw * sgn * P.wSyn * gain * amp);
+      if (P.adjClip > 0) y = (float)fmin(P.adjClip, fmax(-P.adjClip, (R)y));
       D.lres[pre] = y;
     }
   }
@@ -613,6 +635,10 @@ struct fb_diff {
   float *inScale = nullptr;
   uint8_t *gate = nullptr;
   double *P = nullptr;
+  float *Pf = nullptr;
+  int32_t f32 = 0;  // FB_DIFF_F32 arithmetic
+  DP<double> P64;
+  DP<float> P32;
   float *ckpt = nullptr;
   uint32_t *ckptRng = nullptr;
   int64_t ckptCap = 0;     // checkpoints allocated
@@ -662,6 +688,18 @@ extern "C" void fb_diff_default_params(fb_diff_params *p) {
   p->depTau = 200; p->minSyn = 1; p->eExc = 0; p->eInh = -70; p->inhGain = 1; p->sizeAlpha = 0;
   p->maxSizeScale = 20; p->boostCap = 1; p->kcThreshold = 0; p->laminaBias = 0;
   p->surrogateBeta = 2.0; p->adjClip = 0; p->coba = 1; p->soft = 0; p->checkpoint = 16;
+  p->precision = FB_DIFF_F64;
+}
+
+template <typename R>
+static DP<R> typed_params(const DiffDev &D) {
+  DP<R> q;
+  q.dt = (R)D.dt; q.vRest = (R)D.vRest; q.vThresh = (R)D.vThresh; q.vReset = (R)D.vReset;
+  q.tRef = (R)D.tRef; q.wSyn = (R)D.wSyn; q.adaptInc = (R)D.adaptInc; q.depU = (R)D.depU;
+  q.eExc = (R)D.eExc; q.eInh = (R)D.eInh; q.inhGain = (R)D.inhGain; q.kcThreshold = (R)D.kcThreshold;
+  q.laminaBias = (R)D.laminaBias; q.beta = (R)D.beta; q.adjClip = (R)D.adjClip; q.dE = (R)D.dE;
+  q.dA = (R)D.dA; q.kRec = (R)D.kRec; q.kM = (R)D.kM; q.dtS = (R)D.dtS; q.cE = (R)D.cE; q.cI = (R)D.cI;
+  return q;
 }
 
 extern "C" int fb_diff_create(const fb_diff_net *net, int64_t tape_cap, fb_diff **out) {
@@ -744,6 +782,7 @@ extern "C" int fb_diff_create(const fb_diff_net *net, int64_t tape_cap, fb_diff 
   int32_t *i32;
   float *f;
   if ((rc = dalloc(d, &d->inScale, N)) || (rc = dalloc(d, &d->gate, E)) || (rc = dalloc(d, &d->P, E)) ||
+      (rc = dalloc(d, &d->Pf, E)) ||
       (rc = dalloc(d, &D.v, N)) || (rc = dalloc(d, &D.gE, N)) || (rc = dalloc(d, &D.gI, N)) ||
       (rc = dalloc(d, &D.adapt, N)) || (rc = dalloc(d, &D.res, N)) || (rc = dalloc(d, &D.refr, N)) ||
       (rc = dalloc(d, &D.spikeCount, N)) || (rc = dalloc(d, &D.isForced, N)) || (rc = dalloc(d, &D.rng, 1)) ||
@@ -763,6 +802,7 @@ extern "C" int fb_diff_create(const fb_diff_net *net, int64_t tape_cap, fb_diff 
   D.inScale = d->inScale;
   D.gate = d->gate;
   D.P = d->P;
+  D.Pf = d->Pf;
   D.ovfCap = (uint32_t)std::min<int64_t>((1 << 20) + E / 8, 0x7fffffff);
   DOvf *ov;
   if ((rc = dalloc(d, &ov, D.ovfCap))) { fb_diff_destroy(d); return rc; }
@@ -818,6 +858,8 @@ static int fill_params(fb_diff *d, const fb_diff_params *p) {
   DiffDev &D = d->D;
   if (!(p->dt > 0) || !(p->tauM > 0) || !(p->tauSyn > 0) || p->checkpoint <= 0)
     return dfail(FB_EINVAL, "fb_diff: dt, tauM, tauSyn and checkpoint must be positive");
+  if (p->precision != FB_DIFF_F64 && p->precision != FB_DIFF_F32)
+    return dfail(FB_EINVAL, "fb_diff: precision must be FB_DIFF_F64 or FB_DIFF_F32 (got %d)", p->precision);
   D.nslots = (int32_t)std::max(1.0, std::floor(p->delay / p->dt + 0.5)) + 1;
   D.K = p->checkpoint;
   D.coba = p->coba ? 1 : 0;
@@ -833,6 +875,9 @@ static int fill_params(fb_diff *d, const fb_diff_params *p) {
   D.dtS = p->dt / 1000;
   D.cE = 1 / (p->eExc - p->vRest);
   D.cI = 1 / (p->vRest - p->eInh);
+  d->f32 = p->precision == FB_DIFF_F32;
+  d->P64 = typed_params<double>(D);
+  d->P32 = typed_params<float>(D);
   d->lastP = *p;
   return FB_OK;
 }
@@ -841,7 +886,7 @@ static int prepare(fb_diff *d, const fb_diff_params *p) {
   DiffDev &D = d->D;
   k_prepare<<<256, kDB, 0, d->st>>>(D, d->inScale, d->gate, d->P, d->sizeLog, d->inScaleSrc, d->sensory,
                                      p->sizeAlpha, p->maxSizeScale, p->boostCap, p->minSyn);
-  k_prepare_edges<<<1024, kDB, 0, d->st>>>(D, d->inScale, d->gate, d->P, d->sensory, p->minSyn);
+  k_prepare_edges<<<1024, kDB, 0, d->st>>>(D, d->inScale, d->gate, d->P, d->Pf, d->sensory, p->minSyn);
   DCU(cudaGetLastError());
   return FB_OK;
 }
@@ -857,14 +902,32 @@ static int check_err(fb_diff *d, const char *fn) {
   return FB_OK;
 }
 
-static void run_step(fb_diff *d, int32_t t, int32_t replay, int32_t row, float *resRow) {
+template <typename R>
+static void run_step_t(fb_diff *d, const DP<R> &P, int32_t t, int32_t replay, int32_t row, float *resRow) {
   DiffDev &D = d->D;
   const int nb = (int)((D.N + kDB - 1) / kDB);
-  k_deliver<<<304, kDB, 0, d->st>>>(D, t, resRow);
-  k_forced<<<1, 512, 0, d->st>>>(D, t, replay);
-  k_update<<<nb, kDB, 0, d->st>>>(D, row);
+  k_deliver<R><<<304, kDB, 0, d->st>>>(D, P, t, resRow);
+  k_forced<R><<<1, 512, 0, d->st>>>(D, P, t, replay);
+  k_update<R><<<nb, kDB, 0, d->st>>>(D, P, row);
   if (!replay) k_emit<<<1, 512, 0, d->st>>>(D, t);
   else cudaMemsetAsync(D.ovfTop, 0, 4, d->st);
+}
+
+static void run_step(fb_diff *d, int32_t t, int32_t replay, int32_t row, float *resRow) {
+  if (d->f32) run_step_t<float>(d, d->P32, t, replay, row, resRow);
+  else run_step_t<double>(d, d->P64, t, replay, row, resRow);
+}
+
+static void reverse_step(fb_diff *d, int32_t t, int32_t row, int32_t scored, const float *resRow) {
+  DiffDev &D = d->D;
+  const int nblk = (int)((D.N + kDB - 1) / kDB);
+  if (d->f32) {
+    k_bneuron<float><<<nblk, kDB, 0, d->st>>>(D, d->P32, t, row, scored);
+    k_barrival<float><<<304, kDB, 0, d->st>>>(D, d->P32, t, resRow);
+  } else {
+    k_bneuron<double><<<nblk, kDB, 0, d->st>>>(D, d->P64, t, row, scored);
+    k_barrival<double><<<304, kDB, 0, d->st>>>(D, d->P64, t, resRow);
+  }
 }
 
 extern "C" int fb_diff_forward(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed,
@@ -1056,7 +1119,6 @@ extern "C" int fb_diff_backward(fb_diff *d, const float *dL, int32_t nro, const 
   DCU(cudaMemsetAsync(D.lsRing, 0, (size_t)D.nslots * N * 4, d->st));
   if ((rc = prepare(d, &d->lastP))) return rc;
   const size_t nb = (size_t)N * 4;
-  const int nblk = (int)((N + kDB - 1) / kDB);
   const int nseg = (steps + K - 1) / K;
   for (int b = nseg - 1; b >= 0; b--) {
     const int32_t from = b * K, to = std::min(steps, from + K);
@@ -1075,8 +1137,7 @@ extern "C" int fb_diff_backward(fb_diff *d, const float *dL, int32_t nro, const 
         for (float *p : {D.lv, D.lgE, D.lgI, D.lad, D.lres}) cudaMemsetAsync(p, 0, nb, d->st);
         cudaMemsetAsync(D.lsRing, 0, (size_t)D.nslots * nb, d->st);
       }
-      k_bneuron<<<nblk, kDB, 0, d->st>>>(D, t, t - from, t >= loss_from ? 1 : 0);
-      k_barrival<<<304, kDB, 0, d->st>>>(D, t, D.resAt + (int64_t)(t - from) * maxArr);
+      reverse_step(d, t, t - from, t >= loss_from ? 1 : 0, D.resAt + (int64_t)(t - from) * maxArr);
     }
   }
   DCU(cudaGetLastError());

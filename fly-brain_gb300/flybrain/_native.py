@@ -50,7 +50,7 @@ class FbDiffParams(C.Structure):
         "dt", "vRest", "vThresh", "vReset", "tauM", "tauSyn", "tRef", "delay", "wSyn", "adaptInc",
         "adaptTau", "depU", "depTau", "minSyn", "eExc", "eInh", "inhGain", "sizeAlpha",
         "maxSizeScale", "boostCap", "kcThreshold", "laminaBias", "surrogateBeta", "adjClip")] + [
-        (k, C.c_int32) for k in ("coba", "soft", "checkpoint", "pad")]
+        (k, C.c_int32) for k in ("coba", "soft", "checkpoint", "precision")]
 
 
 class FbDiffNet(C.Structure):

@@ -75,12 +75,24 @@ class LIFDiffFunction(torch.autograd.Function):
 
 
 def lowpass_rates(raster: torch.Tensor, dt_ms: float, tau_ms: float = 20.0) -> torch.Tensor:
-    """Exponentially low-passed firing rates in Hz of a (steps x R) spike raster:
-    r_t = a r_{t-1} + (1 - a) s_t / dt, a = exp(-dt / tau), computed as a causal FIR convolution
-    truncated at 10 tau."""
+    """Exponentially low-passed firing rates in Hz of a (steps x R) spike raster, exactly:
+    r_t = a r_{t-1} + c s_t with a = exp(-dt / tau), c = (1 - a) / dt (dt in s), r_{-1} = 0.
+    Evaluated blockwise in float64 as r_t = a^(t+1) r_start + c a^t sum_{k<=t} a^-k s_k, with
+    blocks short enough that a^-k stays below 1e12; differentiable through torch ops."""
     a = float(np.exp(-dt_ms / tau_ms))
-    taps = int(np.ceil(10 * tau_ms / dt_ms))
-    k = (1 - a) / (dt_ms / 1000.0) * a ** torch.arange(taps, dtype=torch.float32, device=raster.device)
-    x = raster.t().unsqueeze(1)  # R x 1 x T
-    x = torch.nn.functional.pad(x, (taps - 1, 0))
-    return torch.nn.functional.conv1d(x, k.flip(0).view(1, 1, -1)).squeeze(1).t()
+    c = (1 - a) / (dt_ms / 1000.0)
+    T, R = raster.shape
+    block = max(1, min(T, int(27.0 * tau_ms / dt_ms)))
+    x = raster.to(torch.float64)
+    k = torch.arange(block, dtype=torch.float64, device=raster.device)
+    up, down = a ** (-k), a ** k
+    r = torch.zeros(R, dtype=torch.float64, device=raster.device)
+    out = []
+    for b0 in range(0, T, block):
+        xb = x[b0:b0 + block]
+        n = xb.shape[0]
+        cs = torch.cumsum(xb * up[:n, None], 0)
+        rb = (a * down[:n, None]) * r[None, :] + c * down[:n, None] * cs
+        out.append(rb)
+        r = rb[-1]
+    return torch.cat(out).to(raster.dtype)

@@ -22,7 +22,9 @@ DIFF_DEFAULTS = dict(
     wSyn=0.3, adaptInc=0.0, adaptTau=100.0, depU=0.0, depTau=200.0, minSyn=1.0, coba=True,
     eExc=0.0, eInh=-70.0, inhGain=1.0, sizeAlpha=0.0, maxSizeScale=20.0, boostCap=1.0,
     kcThreshold=0.0, laminaBias=0.0, surrogateBeta=2.0, adjClip=0.0, soft=False, checkpoint=16,
+    precision="f64",
 )
+PRECISIONS = dict(f64=0, f32=1)
 
 _ARRAYS_N = ("size_log", "in_scale", "log_gain", "out_scale", "thr_offset", "beta", "bias")
 _MASKS = ("thr_mask", "bias_mask", "sensory")
@@ -32,10 +34,13 @@ _FIELDS = dict(log_gain=0, out_scale=1, thr_offset=2, bias=3, edge_gain=4, drive
 def make_params(p: dict) -> nat.FbDiffParams:
     q = nat.FbDiffParams()
     for k, _ in nat.FbDiffParams._fields_:
-        if k in ("coba", "soft", "checkpoint", "pad"):
+        if k in ("coba", "soft", "checkpoint", "precision"):
             continue
         setattr(q, k, float(p[k]))
     q.coba, q.soft, q.checkpoint = int(bool(p["coba"])), int(bool(p["soft"])), int(p["checkpoint"])
+    if p["precision"] not in PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {p['precision']!r}")
+    q.precision = PRECISIONS[p["precision"]]
     return q
 
 

@@ -213,8 +213,16 @@ typedef struct fb_diff_params {
   double wSyn, adaptInc, adaptTau, depU, depTau, minSyn;
   double eExc, eInh, inhGain, sizeAlpha, maxSizeScale, boostCap;
   double kcThreshold, laminaBias, surrogateBeta, adjClip;
-  int32_t coba, soft, checkpoint, pad;
+  int32_t coba, soft, checkpoint;
+  int32_t precision; /* FB_DIFF_F64 (the reference's double intermediates) or FB_DIFF_F32 */
 } fb_diff_params;
+
+/* Arithmetic of the differentiable step's intermediates. FB_DIFF_F64 is LIFDiff's (JS numbers:
+ * every intermediate in double, state in float32). FB_DIFF_F32 computes the same expressions in
+ * float32 (state, tape and gradient accumulators are unchanged); it exists because GB300's FP64
+ * rate is a small fraction of its FP32 rate. Not bit-identical to the reference. */
+#define FB_DIFF_F64 0
+#define FB_DIFF_F32 1
 
 /* Fills *p with the defaults of src/lifdiff.js:86-109 (checkpoint 16, conductance-based). */
 void fb_diff_default_params(fb_diff_params *p);

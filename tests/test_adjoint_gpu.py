@@ -157,3 +157,79 @@ def test_readout_loss_truncation_clip_current_based():
     for i, a in zip(idx[off[t]:off[t + 1]], amp[off[t]:off[t + 1]]):
         if i in set(readout.tolist()):
             assert r[t, int(np.searchsorted(readout, i))] == a
+
+
+# ---- float32 arithmetic (precision="f32"): the same expressions with float intermediates ----
+
+def _rel_err(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(1e-30, float(np.max(np.abs(b)))))
+
+
+@pytest.mark.parametrize("name", ["wSyn", "vThresh", "depU", "sizeAlpha", "eInh", "laminaBias"])
+def test_f32_soft_gradient_matches_gpu_finite_difference(name):
+    """Float intermediates keep the adjoint within scripts/grad_check.mjs:98's tolerance of central
+    differences of the float forward."""
+    ins, target = grad_check_inputs()
+    _, net = _pair(ins, dict(P0, precision="f32"))
+    dL = np.zeros(ins["N"], np.float32)
+    dL[target] = 1
+    L = float(net.forward(60)[target].astype(np.float64).sum())
+    g = net.backward(dL)["params"][name]
+    h = H[name]
+    lp = float(net.forward(60, record=False, **{name: P0[name] + h})[target].astype(np.float64).sum())
+    lm = float(net.forward(60, record=False, **{name: P0[name] - h})[target].astype(np.float64).sum())
+    fd = (lp - lm) / (2 * h)
+    ok, rel = within_tolerance(g, fd, h, L)
+    assert ok, (name, g, fd, rel)
+
+
+def test_f32_soft_gradients_track_f64():
+    """Soft spikes: the float pass follows the double one; every scalar, per-neuron and per-edge
+    gradient agrees to 1e-3 of its vector's largest entry."""
+    ins, target = grad_check_inputs()
+    dL = np.zeros(ins["N"], np.float32)
+    dL[target] = 1
+    out = {}
+    for prec in ("f64", "f32"):
+        _, net = _pair(ins, dict(P0, precision=prec))
+        sc = net.forward(60)
+        out[prec] = (sc, net.backward(dL))
+    (sc64, g64), (sc32, g32) = out["f64"], out["f32"]
+    assert _rel_err(sc32, sc64) < 1e-4
+    for k in g64["params"]:
+        assert abs(g32["params"][k] - g64["params"][k]) <= 1e-3 * abs(g64["params"][k]) + 1e-9, k
+    assert _rel_err(g32["logGain"], g64["logGain"]) < 1e-3
+    assert _rel_err(g32["bias"], g64["bias"]) < 1e-3
+    assert _rel_err(g32["edge"], g64["edge"]) < 1e-3
+    assert _rel_err(g32["outScale"], g64["outScale"]) < 1e-3
+
+
+def test_f32_hard_forward_tracks_f64():
+    """Hard spikes: a threshold crossing can flip when float rounding moves v across it; over
+    400 steps of the driven subgraph the spike totals agree to 2% and the forced spikes (the
+    random draws) of the first steps are identical."""
+    ins, target, driven, hz, params = _hard_inputs()
+    tapes = {}
+    for prec in ("f64", "f32"):
+        _, net = _pair(ins, dict(params, precision=prec), driven, hz)
+        sc = net.forward(400, seed=3)
+        tapes[prec] = (sc, net.tape())
+    (sc64, (o64, i64, _)), (sc32, (o32, i32, _)) = tapes["f64"], tapes["f32"]
+    assert abs(float(sc32.sum()) - float(sc64.sum())) <= 0.02 * float(sc64.sum())
+    np.testing.assert_array_equal(i32[: o32[5]], i64[: o64[5]])
+
+
+def test_precision_is_validated():
+    from flybrain._native import FlyBrainError
+    ins, _ = grad_check_inputs()
+    _, net = _pair(ins, P0)
+    with pytest.raises(ValueError):
+        net.forward(4, precision="f16")
+    q = net.params()
+    q.precision = 7
+    import ctypes as C
+    sc = np.zeros(ins["N"], np.float32)
+    with pytest.raises(FlyBrainError):
+        from flybrain import _native as nat
+        nat.check(net.L.fb_diff_forward(net.h, C.byref(q), 4, 1, 0, sc.ctypes.data))
