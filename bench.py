@@ -236,6 +236,15 @@ def run_ours(args, rank, world):
         torch.cuda.empty_cache()
         res["adjoint"] = run_adjoint(g, idx, hz)
         brain = None
+    if os.environ.get("FB_BENCH_ADJOINT_BATCH", "1") == "1":
+        plain_per_trial_s = dev_s / sim_s
+        ab = run_adjoint_batched(g, idx, hz, n_trials=int(os.environ.get("FB_ADJ_TRIALS", "64")))
+        ab["plain_single_trial_forward_per_trial_s"] = plain_per_trial_s
+        ab["cost_vs_plain_single_trial_forward"] = ab["fwd_bwd_per_trial_s"] / plain_per_trial_s
+        res["adjoint_batched"] = ab
+        torch.cuda.empty_cache()
+        res["adjoint_uneven"] = run_adjoint_uneven(n_inst=int(os.environ.get("FB_ADJ_UNEVEN", "128")))
+        torch.cuda.empty_cache()
     if os.environ.get("FB_BENCH_BATCHED", "1") == "1":
         del brain
         torch.cuda.empty_cache()
@@ -375,6 +384,137 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3):
                 config="surrogate-gradient LIF (beta 0.04, adjClip 100), N=165,122, 500 ms at dt 0.1 ms, "
                        "K=100; MSE of 20 ms low-pass rates of 1,000 readouts vs a 0-80 Hz target; "
                        "gradients for every edge gain, bias and 64 type gains (autograd)")
+
+
+ADJ_OPTS = dict(dt=0.1, vRest=-52.0, vThresh=-45.0, vReset=-52.0, tauM=20.0, tauSyn=5.0, tRef=2.2, delay=1.8,
+                wSyn=0.275, coba=False, soft=False, surrogateBeta=0.04, adjClip=100.0, checkpoint=100,
+                adaptInc=0.0, depU=0.0)
+
+
+def _adj_loss_grads(batch, readouts, targets, dt):
+    """Rasters of every member, MSE of 20 ms low-pass rates against the member's target trace,
+    and its gradient with respect to each raster (torch autograd over the filter)."""
+    import torch
+    from flybrain.autograd import lowpass_rates
+    dls, loss = [], 0.0
+    for b in range(batch.B):
+        r = torch.zeros((batch._steps[b], readouts[b].shape[0]), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        batch.raster(b, readouts[b], out=r)
+        r.requires_grad_()
+        L = ((lowpass_rates(r, dt) - targets[b]) ** 2).mean()
+        L.backward()
+        dls.append(r.grad.detach().contiguous())
+        loss += float(L.detach())
+    torch.cuda.synchronize()
+    return dls, loss / batch.B
+
+
+def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
+    """Batched forward+adjoint: n_trials trials of the differentiable workload (surrogate slope
+    25/mV, adjClip 100, 500 ms at dt 0.1 ms, K=100, float32 intermediates) sharing the full graph
+    and its edge gains, each with its own seed and target trace, in one batch (fb_diff_batch_*);
+    gradients for every edge (summed over trials in trial order), bias and type gain. Cost per
+    trial-second against the plain single-trial forward."""
+    import torch
+    from flybrain.diff import DiffBatch, DiffNet
+    prec = os.environ.get("FB_ADJ_PRECISION", "f32")
+    rng = np.random.default_rng(seed)
+    data = dict(N=g.N, indptr=g.indptr, indices=g.indices, weights=g.counts.astype(np.float32), sign=g.sign)
+    eg = np.ones(g.E, np.float32)
+    members = []
+    for _ in range(n_trials):
+        n = DiffNet(data, dict(ADJ_OPTS, edgeGain=eg), _defer=True)
+        for i, h in zip(idx.tolist(), hz.tolist()):
+            n.setDriveOne(i, h)
+        members.append(n)
+    params = dict(ADJ_OPTS, precision=prec)
+    t0 = time.perf_counter()
+    batch = DiffBatch(members, params)
+    create_s = time.perf_counter() - t0
+    readout = np.sort(rng.choice(g.N, 1000, replace=False)).astype(np.int32)
+    readouts = [readout] * n_trials
+    targets = [torch.as_tensor(rng.uniform(0, 80, (1, 1000)), dtype=torch.float32, device="cuda")
+               for _ in range(n_trials)]
+    seeds = list(range(1, n_trials + 1))
+
+    def clock(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    batch.forward(200, seeds, counts=False)  # warm-up
+    _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
+    _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
+    (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
+    gs, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
+    ge = torch.zeros(g.E, dtype=torch.float64, device="cuda")
+    _, sum_s = clock(lambda: batch.edge_sum(out=ge))
+    trial_s = n_trials * steps * 0.1 / 1000
+    total = fwd_s + loss_s + bwd_s + sum_s
+    spikes = sum(int(batch.tape(b)[0][-1]) for b in range(min(n_trials, 4)))
+    return dict(trials=n_trials, neurons=g.N, edges=g.E, steps=steps, checkpoint=100, precision=prec,
+                create_s=create_s, plain_batch_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s,
+                backward_s=bwd_s, edge_sum_s=sum_s, trial_s=trial_s,
+                fwd_bwd_per_trial_s=total / trial_s, plain_batch_forward_per_trial_s=plain_s / trial_s,
+                trial_s_of_gradient_per_wall_s=trial_s / total, loss=loss, spikes_first4=spikes,
+                grads=dict(edge_nonzero=int((ge != 0).sum()), edge_finite=bool(torch.isfinite(ge).all()),
+                           bias_nonzero=int(sum(int((x["bias"] != 0).sum()) for x in gs))),
+                config=f"{n_trials} trials sharing the N=165,122 graph and its edge gains, own seeds and "
+                       "target traces; surrogate slope 25/mV, adjClip 100, 500 ms at dt 0.1 ms, K=100")
+
+
+def run_adjoint_uneven(n_inst=128, seed=11):
+    """Batched uneven adjoint: n_inst instances over separately seeded synthetic subgraphs of
+    5,000-60,000 neurons, each 100-400 ms (dt 0.1 ms) with its own drive (1% of neurons at
+    150 Hz) and target trace; forward+backward of the whole batch against its plain forward."""
+    import torch
+    from flybrain.diff import DiffBatch, DiffNet
+    from flybrain.synth import synth_graph
+    prec = os.environ.get("FB_ADJ_PRECISION", "f32")
+    rng = np.random.default_rng(seed)
+    members, readouts, targets, steps = [], [], [], []
+    t0 = time.perf_counter()
+    for k in range(n_inst):
+        N = int(rng.integers(5000, 60001))
+        sg = synth_graph(N, 1000 + k)
+        n = DiffNet(dict(N=N, indptr=sg.indptr, indices=sg.indices, weights=sg.counts.astype(np.float32),
+                         sign=sg.sign), dict(ADJ_OPTS), _defer=True)
+        for i in rng.choice(N, max(1, N // 100), replace=False):
+            n.setDriveOne(int(i), 150.0)
+        members.append(n)
+        steps.append(int(rng.integers(1000, 4001)))
+        ro = np.sort(rng.choice(N, min(200, N), replace=False)).astype(np.int32)
+        readouts.append(ro)
+        targets.append(torch.as_tensor(rng.uniform(0, 80, (1, ro.shape[0])), dtype=torch.float32, device="cuda"))
+    gen_s = time.perf_counter() - t0
+    batch = DiffBatch(members, dict(ADJ_OPTS, precision=prec))
+    seeds = list(range(1, n_inst + 1))
+
+    def clock(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    batch.forward([200] * n_inst, seeds, counts=False)  # warm-up
+    _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
+    _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
+    (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
+    _, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
+    trial_s = sum(steps) * 0.1 / 1000
+    total = fwd_s + loss_s + bwd_s
+    return dict(instances=n_inst, neurons_total=int(sum(batch.N)), edges_total=int(sum(batch.E)),
+                steps_min=min(steps), steps_max=max(steps), precision=prec, graph_gen_s=gen_s,
+                plain_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s, backward_s=bwd_s,
+                trial_s=trial_s, trial_s_of_gradient_per_wall_s=trial_s / total,
+                trial_s_of_plain_forward_per_wall_s=trial_s / plain_s, cost_vs_plain_forward=total / plain_s,
+                loss=loss,
+                config=f"{n_inst} instances over synthetic subgraphs of 5,000-60,000 neurons, 100-400 ms at "
+                       "dt 0.1 ms, own drive/seed/target; surrogate slope 25/mV, adjClip 100, K=100")
 
 
 def run_reference(args, rank, world):

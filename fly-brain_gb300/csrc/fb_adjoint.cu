@@ -1,11 +1,14 @@
 // The differentiable brain step and its adjoint on sm_103a: the reference's LIFDiff
-// (src/lifdiff.js:219-686). Forward with a spike tape and state checkpoints every K steps;
-// backward replays one segment from its checkpoint (forced spikes from the tape, so the RNG is
-// never redrawn), then sweeps the segment's steps in reverse.
+// (src/lifdiff.js:219-686), for a batch of independent instances (each its own network, drive,
+// seed and length; one parameter set) advanced together: every kernel runs the whole batch, the
+// instance in blockIdx.y. Forward with a spike tape and state checkpoints every K steps; backward
+// replays one segment from its checkpoint (forced spikes from the tape, so the RNG is never
+// redrawn), then sweeps the segment's steps in reverse. A single network is a batch of one.
 //
-// Arithmetic is LIFDiff's: every intermediate in double, every state word float32, operands in
-// the JS order; per-target conductance sums run in the reference's arrival order (each
-// contribution is pushed with its arrival rank into a per-target bucket and summed in rank order).
+// Arithmetic is LIFDiff's in FB_DIFF_F64 mode: every intermediate in double, every state word
+// float32, operands in the JS order; per-target conductance sums run in the reference's arrival
+// order (each contribution is pushed with its arrival rank into a per-target bucket and summed in
+// rank order). FB_DIFF_F32 evaluates the same expressions with float intermediates.
 // The backward accumulates without float atomics: within one step every edge and every
 // presynaptic neuron is touched by one arrival at most, so per-edge and per-neuron accumulators
 // have a single writer per step and are summed in time order; scalars are reduced in a fixed order.
@@ -16,7 +19,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "fb_internal.cuh"
@@ -28,24 +33,28 @@ void host_jump_tables(std::vector<uint32_t> &tab);
 constexpr int kDB = 256;      // threads per block of the per-neuron kernels
 constexpr int kDBucket = 8;   // bucket slots per target and step
 constexpr int kDSortMax = 64; // contributions per target sorted in local memory
+constexpr int kRB = 128;      // blocks per instance of the final reduction
+constexpr int kNSums = 9;     // scalar sums per instance
 
 struct DOvf {
   uint32_t k, j, next, pad;
 };
 
-// Everything the kernels see: parameters (double), graph, derived arrays, state, tape, scratch.
+// One instance as the kernels see it: sizes, graph, derived arrays, state, tape, scratch,
+// adjoint state and accumulators. Kernels copy their instance's record into shared memory.
 struct DiffDev {
-  int32_t N, nslots, K, coba, soft, nDriven, nro, pad;
+  int32_t N, nslots, K, coba, soft, nDriven, nro, nTiles;
+  int32_t steps;   // length of the current forward; the instance sits out steps t >= steps
+  uint32_t seed0;  // xorshift state after seeding
   int64_t E;
-  double dt, vRest, vThresh, vReset, tRef, wSyn, adaptInc, depU, eExc, eInh, inhGain;
-  double kcThreshold, laminaBias, beta, adjClip, dE, dA, kRec, kM, dtS, cE, cI;
   // graph and per-neuron structure
   const uint32_t *indptr, *indices;
-  const float *counts, *edgeGain, *sign, *logGain, *outScale, *thrOffset, *betaArr, *biasArr;
+  const uint32_t *cscPtr, *cscEdge, *cscSrc;  // in-edges of each target, ascending edge id
+  const float *counts, *edgeGain, *sign, *logGain, *outScale, *thrOffset, *betaArr, *biasArr, *sizeLog;
   const uint8_t *thrMask, *biasMask;
   const float *drive;
   const int32_t *driven;
-  // derived per forward: inScale, gate, P[j] = (count * edgeGain) * inScale[q]
+  // derived per forward: inScale, gate, P[j] = (count * edgeGain) * inScale[q] (double, float)
   const float *inScale;
   const uint8_t *gate;
   const double *P;
@@ -60,18 +69,19 @@ struct DiffDev {
   int64_t *tOff;
   int32_t *tForced;
   int64_t tapeCap;
+  // checkpoints: v gE gI adapt res refr every K steps, and the RNG state
+  float *ckpt;
+  uint32_t *ckptRng;
   // delivery scratch
   uint32_t *cnt;
   uint2 *bucket;
   uint32_t *ovfHead, *ovfTop;
   DOvf *ovf;
-  uint32_t ovfCap;
-  double *effK;   // per arrival of the step
+  double *effK;  // per arrival of the step
   // spike staging per tile
   int32_t *stage;
   float *stageAmp;
   int32_t *tileCnt;
-  int32_t nTiles;
   // arena of a replayed segment (row r = step - segment start) and per-arrival res
   float *aV, *aGE, *aGI, *aAd, *aSp;
   uint8_t *aMode;
@@ -82,11 +92,25 @@ struct DiffDev {
   // accumulators (double): per neuron A (adaptInc) V (vThresh) Kc La (laminaBias) EI (eInh)
   // W (wSyn) D (depU), per-neuron log-gain and bias gradients, per-edge weight gradients
   double *accA, *accV, *accKc, *accLa, *accEI, *accW, *accD, *gLog, *gBias, *gEdge;
-  const float *dL;      // flat [N], or per step over the readout set [steps][nro]
-  const int32_t *roMap; // neuron -> readout column, -1 elsewhere (per-step dL)
+  float *gLogF;  // log-gain gradient as returned (non-finite -> 0)
+  double *gOut;  // outScale gradient
+  const float *dL;       // flat [N], or per step over the readout set [steps][nro]
+  const int32_t *roMap;  // neuron -> readout column, -1 elsewhere (per-step dL)
+  int32_t *nonfinite;    // count of non-finite log-gain gradients
+  uint32_t ovfCap, pad0;
   int32_t *err;
   const uint32_t *jump;
 };
+
+static_assert(sizeof(DiffDev) % 4 == 0, "DiffDev is copied as 32-bit words");
+
+// The block's instance record into shared memory.
+__device__ __forceinline__ void load_dev(const DiffDev *Ds, DiffDev &s) {
+  const uint32_t *src = reinterpret_cast<const uint32_t *>(Ds + blockIdx.y);
+  uint32_t *dst = reinterpret_cast<uint32_t *>(&s);
+  for (int k = threadIdx.x; k < (int)(sizeof(DiffDev) / 4); k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+}
 
 // Model constants in the arithmetic type R of a pass: double reproduces the reference's
 // arithmetic (JS numbers); float is the GB300 fast mode (the FP64 pipes are a small fraction of
@@ -124,11 +148,10 @@ __device__ __forceinline__ R d_u(const DiffDev &D, const DP<R> &P, R vv, R ge, R
 }
 
 // inScale (src/lifdiff.js:158-164).
-__global__ void k_prepare(DiffDev D, float *inScale, uint8_t *gate, double *P, const float *sizeLog,
-                          const float *inScaleSrc, const uint8_t *sensory, double sizeAlpha,
-                          double maxSizeScale, double boostCap, double minSyn) {
+__global__ void k_prepare(int32_t N, float *inScale, const float *sizeLog, const float *inScaleSrc,
+                          double sizeAlpha, double maxSizeScale, double boostCap) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = tid; i < D.N; i += nt) {
+  for (int64_t i = tid; i < N; i += nt) {
     if (inScaleSrc) inScale[i] = inScaleSrc[i];
     else {
       const double s = exp(-sizeAlpha * (double)sizeLog[i]);
@@ -139,36 +162,66 @@ __global__ void k_prepare(DiffDev D, float *inScale, uint8_t *gate, double *P, c
 
 // The gate (src/lifdiff.js:167-171) and P[j] = (count * edgeGain) * inScale[q], the first factors
 // of the delivered amount (:281-282), in double and in float.
-__global__ void k_prepare_edges(DiffDev D, const float *inScale, uint8_t *gate, double *P, float *Pf,
-                                const uint8_t *sensory, double minSyn) {
+__global__ void k_prepare_edges(int64_t E, const uint32_t *indices, const float *counts, const float *edgeGain,
+                                const float *inScale, const uint8_t *sensory, double minSyn, uint8_t *gate,
+                                double *P, float *Pf) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t j = tid; j < D.E; j += nt) {
-    const uint32_t q = D.indices[j];
-    const double c = (double)D.counts[j];
+  for (int64_t j = tid; j < E; j += nt) {
+    const uint32_t q = indices[j];
+    const double c = (double)counts[j];
     gate[j] = (c >= minSyn && !(sensory && sensory[q])) ? 1 : 0;
-    P[j] = c * (D.edgeGain ? (double)D.edgeGain[j] : 1.0) * (double)inScale[q];
-    Pf[j] = D.counts[j] * (D.edgeGain ? D.edgeGain[j] : 1.f) * inScale[q];
+    P[j] = c * (edgeGain ? (double)edgeGain[j] : 1.0) * (double)inScale[q];
+    Pf[j] = counts[j] * (edgeGain ? edgeGain[j] : 1.f) * inScale[q];
   }
 }
 
-__global__ void k_reset(DiffDev D) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
-    D.v[i] = (float)D.vRest;
+// Reset (src/lifdiff.js:221-233): state, delivery scratch, RNG, tape offset 0.
+__global__ void k_reset(const DiffDev *Ds, float vRest) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (int64_t)gridDim.x * blockDim.x) {
+    D.v[i] = vRest;
     D.gE[i] = D.gI[i] = D.adapt[i] = D.refr[i] = D.spikeCount[i] = 0.f;
     D.res[i] = 1.f;
     D.isForced[i] = 0;
     D.cnt[i] = 0;
     D.ovfHead[i] = kNil;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *D.rng = D.seed0;
+    D.tOff[0] = 0;
+    *D.ovfTop = 0;
+  }
+}
+
+// Saves (save=1, at t % K == 0) or restores (save=0) the checkpoint of step t.
+__global__ void __launch_bounds__(kDB, 4) k_ckpt(const DiffDev *Ds, int32_t t, int32_t save) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
+  if (t >= D.steps || t % D.K) return;
+  const int64_t N = D.N;
+  float *c = D.ckpt + (int64_t)(t / D.K) * 6 * N;
+  float *st[6] = {D.v, D.gE, D.gI, D.adapt, D.res, D.refr};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 6; a++) {
+      if (save) c[a * N + i] = st[a][i];
+      else st[a][i] = c[a * N + i];
+    }
+  }
+  if (save && blockIdx.x == 0 && threadIdx.x == 0) D.ckptRng[t / D.K] = *D.rng;
 }
 
 // Delivery of the arrivals at step t (the spikes of step t - (nslots-1)), warp per arrival
 // (src/lifdiff.js:276-283): lane 0 forms eff and depresses res; lanes push (rank, edge) per
-// gated edge into the target's bucket. resRow (replay) records res[pre] per arrival.
+// gated edge into the target's bucket. In a replay (row >= 0) the arrival's res is recorded.
 template <typename R>
-__global__ void k_deliver(DiffDev D, DP<R> P, int32_t t, float *resRow) {
+__global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
   const int e = t - (D.nslots - 1);
-  if (e < 0) return;
+  if (t >= D.steps || e < 0) return;
+  float *resRow = row >= 0 ? D.resAt + (int64_t)row * D.maxArr : nullptr;
   const int64_t a0 = D.tOff[e], na = D.tOff[e + 1] - a0;
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -211,14 +264,18 @@ __global__ void k_deliver(DiffDev D, DP<R> P, int32_t t, float *resRow) {
   }
 }
 
-// Forced spikes of step t (src/lifdiff.js:290-297), one block. Forward: one draw per
+// Forced spikes of step t (src/lifdiff.js:290-297), one block per instance. Forward: one draw per
 // non-refractory driven neuron in drivenSet order, compared (in R) against drive * dt/1000; each
-// spike goes to the head of step t's tape list. Replay: the tape's forced list.
+// spike goes to the head of step t's tape list. Replay: the tape's forced list. Runs after the
+// step's delivery, so it also rewinds the overflow pool for the next step.
 template <typename R>
-__global__ void k_forced(DiffDev D, DP<R> P, int32_t t, int32_t replay) {
+__global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) {
+  __shared__ DiffDev D;
   __shared__ uint32_t sJump[32 * 128];
   __shared__ uint32_t scan[33];
   __shared__ uint32_t sh_s0;
+  load_dev(Ds, D);
+  if (t >= D.steps) return;
   const int tid = threadIdx.x;
   const int64_t base = D.tOff[t];
   if (replay) {
@@ -229,6 +286,7 @@ __global__ void k_forced(DiffDev D, DP<R> P, int32_t t, int32_t replay) {
       D.adapt[i] = (float)((R)D.adapt[i] + P.adaptInc);
       D.isForced[i] = 1;
     }
+    if (tid == 0) *D.ovfTop = 0;
     return;
   }
   for (int k = tid; k < 32 * 128; k += blockDim.x) sJump[k] = D.jump[k];
@@ -275,6 +333,7 @@ __global__ void k_forced(DiffDev D, DP<R> P, int32_t t, int32_t replay) {
   if (tid == 0) {
     *D.rng = xs_jump(sJump, s0, draws);
     D.tForced[t] = (int32_t)nf;
+    *D.ovfTop = 0;
   }
 }
 
@@ -328,94 +387,102 @@ __device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, fl
   if (n > (uint32_t)kDBucket) D.ovfHead[i] = kNil;
 }
 
-// Integrate and spike (src/lifdiff.js:313-344), one thread per neuron; with `row` >= 0 it also
-// records the replay arena (:439-456). Spikes above the tape threshold are staged per tile.
+// Integrate and spike (src/lifdiff.js:313-344), one thread per neuron, tiles of kDB neurons; with
+// `row` >= 0 it also records the replay arena (:439-456). In a forward pass the spikes above the
+// tape threshold are staged per tile.
 template <typename R>
-__global__ void k_update(DiffDev D, DP<R> P, int32_t row) {
+__global__ void __launch_bounds__(kDB, 4) k_update(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
+  __shared__ DiffDev D;
   __shared__ uint32_t scan[33];
-  const int tid = threadIdx.x, i = blockIdx.x * blockDim.x + tid;
-  bool emit = false;
-  float amp = 0.f;
-  if (i < D.N) {
-    float geF = D.gE[i], giF = D.gI[i];
-    const uint32_t n = D.cnt[i];
-    if (n) {
-      d_apply<R>(D, P, i, n, geF, giF);
-      D.cnt[i] = 0;
-    }
-    const R ge = geF, gi = giF;
-    const int64_t off = row >= 0 ? (int64_t)row * D.N + i : 0;
-    R vi = D.v[i], s = 0;
-    int md = 0;
-    if (row >= 0) {
-      D.aV[off] = D.v[i];
-      D.aGE[off] = geF;
-      D.aGI[off] = giF;
-    }
-    float refr = D.refr[i];
-    const bool forced = D.isForced[i] != 0;
-    if (forced) D.isForced[i] = 0;
-    const bool wasRefr = refr > 0;
-    if (wasRefr) {
-      refr = (float)((R)refr - P.dt);
-      vi = P.vReset;
-      if (forced) {
-        md = 2;
-        s = 1;
+  load_dev(Ds, D);
+  if (t >= D.steps) return;
+  const int tid = threadIdx.x;
+  for (int tl = blockIdx.x; tl < D.nTiles; tl += gridDim.x) {
+    const int i = tl * kDB + tid;
+    bool emit = false;
+    float amp = 0.f;
+    if (i < D.N) {
+      float geF = D.gE[i], giF = D.gI[i];
+      const uint32_t n = D.cnt[i];
+      if (n) {
+        d_apply<R>(D, P, i, n, geF, giF);
+        D.cnt[i] = 0;
+      }
+      const R ge = geF, gi = giF;
+      const int64_t off = row >= 0 ? (int64_t)row * D.N + i : 0;
+      R vi = D.v[i], s = 0;
+      int md = 0;
+      if (row >= 0) {
+        D.aV[off] = D.v[i];
+        D.aGE[off] = geF;
+        D.aGI[off] = giF;
+      }
+      float refr = D.refr[i];
+      const bool forced = D.isForced[i] != 0;
+      if (forced) D.isForced[i] = 0;
+      const bool wasRefr = refr > 0;
+      if (wasRefr) {
+        refr = (float)((R)refr - P.dt);
+        vi = P.vReset;
+        if (forced) {
+          md = 2;
+          s = 1;
+        } else {
+          md = 1;
+        }
       } else {
-        md = 1;
+        vi = d_u<R>(D, P, vi, ge, gi, d_bias<R>(D, P, i, nullptr));
       }
-    } else {
-      vi = d_u<R>(D, P, vi, ge, gi, d_bias<R>(D, P, i, nullptr));
-    }
-    geF = (float)(ge * P.dE);
-    giF = (float)(gi * P.dE);
-    float ad = (float)((R)D.adapt[i] * P.dA);
-    const R rs = D.res[i];
-    D.res[i] = (float)(rs + (R(1) - rs) * P.kRec);
-    if (row >= 0) D.aAd[off] = ad;
-    if (!wasRefr) {
-      const R thr = P.vThresh + (R)ad + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
-      s = D.soft ? R(1) / (R(1) + exp(-(vi - thr) / d_beta<R>(D, P, i))) : (vi >= thr ? R(1) : R(0));
-      if (s > 0) {
-        vi = s * P.vReset + (R(1) - s) * vi;
-        if (!D.soft) refr = (float)P.tRef;
-        ad = (float)((R)ad + s * P.adaptInc);
+      geF = (float)(ge * P.dE);
+      giF = (float)(gi * P.dE);
+      float ad = (float)((R)D.adapt[i] * P.dA);
+      const R rs = D.res[i];
+      D.res[i] = (float)(rs + (R(1) - rs) * P.kRec);
+      if (row >= 0) D.aAd[off] = ad;
+      if (!wasRefr) {
+        const R thr = P.vThresh + (R)ad + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
+        s = D.soft ? R(1) / (R(1) + exp(-(vi - thr) / d_beta<R>(D, P, i))) : (vi >= thr ? R(1) : R(0));
+        if (s > 0) {
+          vi = s * P.vReset + (R(1) - s) * vi;
+          if (!D.soft) refr = (float)P.tRef;
+          ad = (float)((R)ad + s * P.adaptInc);
+        }
+        D.spikeCount[i] = (float)((R)D.spikeCount[i] + s);
+        if (s > (D.soft ? R(1e-4) : R(0.5))) {
+          emit = true;
+          amp = (float)s;
+        }
       }
-      D.spikeCount[i] = (float)((R)D.spikeCount[i] + s);
-      if (s > (D.soft ? R(1e-4) : R(0.5))) {
-        emit = true;
-        amp = (float)s;
+      if (row >= 0) {
+        D.aMode[off] = (uint8_t)md;
+        D.aSp[off] = (float)s;
       }
+      D.gE[i] = geF;
+      D.gI[i] = giF;
+      D.adapt[i] = ad;
+      D.refr[i] = refr;
+      D.v[i] = (float)vi;
     }
-    if (row >= 0) {
-      D.aMode[off] = (uint8_t)md;
-      D.aSp[off] = (float)s;
+    if (row >= 0) continue;  // replay: the tape already holds the spikes
+    uint32_t tot;
+    const uint32_t pos = block_exclusive_scan(emit ? 1u : 0u, &tot, scan);
+    if (emit) {
+      D.stage[(int64_t)tl * kDB + pos] = i;
+      D.stageAmp[(int64_t)tl * kDB + pos] = amp;
     }
-    D.gE[i] = geF;
-    D.gI[i] = giF;
-    D.adapt[i] = ad;
-    D.refr[i] = refr;
-    D.v[i] = (float)vi;
+    if (tid == 0) D.tileCnt[tl] = (int32_t)tot;
   }
-  if (row >= 0) return;  // replay: the tape already holds the spikes
-  uint32_t tot;
-  const uint32_t pos = block_exclusive_scan(emit ? 1u : 0u, &tot, scan);
-  if (emit) {
-    D.stage[(int64_t)blockIdx.x * blockDim.x + pos] = i;
-    D.stageAmp[(int64_t)blockIdx.x * blockDim.x + pos] = amp;
-  }
-  if (tid == 0) D.tileCnt[blockIdx.x] = (int32_t)tot;
 }
 
-// Appends step t's threshold spikes (tile order = ascending) after its forced ones.
-__global__ void k_emit(DiffDev D, int32_t t) {
+// Appends step t's threshold spikes (tile order = ascending) after its forced ones; one block per
+// instance.
+__global__ void k_emit(const DiffDev *Ds, int32_t t) {
+  __shared__ DiffDev D;
   __shared__ uint32_t scan[33];
-  __shared__ int64_t sBase;
+  load_dev(Ds, D);
+  if (t >= D.steps) return;
   const int tid = threadIdx.x;
-  if (tid == 0) sBase = D.tOff[t] + D.tForced[t];
-  __syncthreads();
-  int64_t carry = sBase;
+  int64_t carry = D.tOff[t] + D.tForced[t];
   for (int t0 = 0; t0 < D.nTiles; t0 += blockDim.x) {
     const int tl = t0 + tid;
     const uint32_t c = tl < D.nTiles ? (uint32_t)D.tileCnt[tl] : 0u;
@@ -434,98 +501,126 @@ __global__ void k_emit(DiffDev D, int32_t t) {
     }
     carry += tot;
   }
-  if (tid == 0) {
-    D.tOff[t + 1] = carry;
-    *D.ovfTop = 0;
+  if (tid == 0) D.tOff[t + 1] = carry;
+}
+
+// Zeroes the adjoint state and accumulators of every instance (before a backward pass).
+__global__ void k_zero_adjoint(const DiffDev *Ds) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
+  const int64_t N = D.N, s0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, ns = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = s0; i < N; i += ns) {
+    D.lv[i] = D.lgE[i] = D.lgI[i] = D.lad[i] = D.lres[i] = 0.f;
+    D.accA[i] = D.accV[i] = D.accKc[i] = D.accLa[i] = D.accEI[i] = D.accW[i] = D.accD[i] = 0.0;
+    D.gLog[i] = D.gBias[i] = 0.0;
   }
+  for (int64_t i = s0; i < (int64_t)D.nslots * N; i += ns) D.lsRing[i] = 0.f;
+  for (int64_t j = s0; j < D.E; j += ns) D.gEdge[j] = 0.0;
+}
+
+// Truncated BPTT (src/lifdiff.js:541-548): the adjoint state restarts at every multiple of
+// `truncate` steps.
+__global__ void __launch_bounds__(kDB, 4) k_truncate(const DiffDev *Ds, int32_t t, int32_t truncate) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
+  if (t >= D.steps || (t + 1) % truncate) return;
+  const int64_t N = D.N, s0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, ns = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = s0; i < N; i += ns) D.lv[i] = D.lgE[i] = D.lgI[i] = D.lad[i] = D.lres[i] = 0.f;
+  for (int64_t i = s0; i < (int64_t)D.nslots * N; i += ns) D.lsRing[i] = 0.f;
 }
 
 // Reverse of integrate-and-spike at step t (src/lifdiff.js:555-617), with the adjoint clip
 // (:623-629) fused: one thread per neuron. Scalar terms accumulate per neuron in double.
 template <typename R>
-__global__ void k_bneuron(DiffDev D, DP<R> P, int32_t t, int32_t row, int32_t scored) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= D.N) return;
-  const int64_t off = (int64_t)row * D.N + i;
+__global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row, int32_t scored) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
+  if (t >= D.steps) return;
   float *ls = D.lsRing + (int64_t)(t % D.nslots) * D.N;
-  const int md = D.aMode[off];
-  const R lpA = D.lad[i];
-  const R lE = (R)D.lgE[i] * P.dE, lI = (R)D.lgI[i] * P.dE, lA = lpA * P.dA;
-  const R lR = (R)D.lres[i] * (R(1) - P.kRec);
-  float lvF = D.lv[i], lgEF = (float)lE, lgIF = (float)lI, ladF = (float)lA, lresF = (float)lR;
-  if (md == 1) {
-    lvF = 0.f;
-  } else if (md == 2) {
-    D.accA[i] += (double)lA;
-    lvF = 0.f;
-    ls[i] = 0.f;
-  } else {
-    const R vv = D.aV[off], gEv = D.aGE[off], gIv = D.aGI[off];
-    R lam;
-    const R bias = d_bias<R>(D, P, i, &lam);
-    const R u = d_u<R>(D, P, vv, gEv, gIv, bias);
-    const R thr = P.vThresh + (R)D.aAd[off] + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
-    const R d = u - thr;
-    const R s = D.aSp[off];
-    const R beta = d_beta<R>(D, P, i);
-    R sg;
-    if (D.soft) sg = s * (R(1) - s) / beta;
-    else {
-      const R tt = R(1) + fabs(d) / beta;
-      sg = R(1) / (beta * tt * tt);
-    }
-    R dl = 0;
-    if (scored && D.dL) {
-      if (D.roMap) {
-        const int c = D.roMap[i];
-        if (c >= 0) dl = D.dL[(int64_t)t * D.nro + c];
-      } else {
-        dl = D.dL[i];
-      }
-    }
-    const R lspike = (R)ls[i] + dl;
-    const R lvNew = lvF;
-    const R lsTot = (P.vReset - u) * lvNew + lpA * P.adaptInc + lspike;
-    const R lt = lsTot * R(1) * sg;
-    const R lu = lvNew * (R(1) - s) + lt;
-    const R lthr = -lt;
-    D.accA[i] += (double)(lpA * s);
-    D.accV[i] += (double)lthr;
-    if (D.thrMask && D.thrMask[i]) D.accKc[i] += (double)lthr;
-    ladF = (float)(lA + lthr * P.dA);
-    if (D.coba) {
-      lvF = (float)(lu * (R(1) + P.kM * (R(-1) - gEv * P.cE + gIv * P.cI)));
-      lgEF = (float)(lE + lu * P.kM * (P.eExc - vv) * P.cE);
-      lgIF = (float)(lI + lu * P.kM * (vv - P.eInh) * P.cI);
-      D.accEI[i] += (double)(lu * P.kM * gIv * P.cI * (R(-1) + (vv - P.eInh) * P.cI));
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
+    const int64_t off = (int64_t)row * D.N + i;
+    const int md = D.aMode[off];
+    const R lpA = D.lad[i];
+    const R lE = (R)D.lgE[i] * P.dE, lI = (R)D.lgI[i] * P.dE, lA = lpA * P.dA;
+    const R lR = (R)D.lres[i] * (R(1) - P.kRec);
+    float lvF = D.lv[i], lgEF = (float)lE, lgIF = (float)lI, ladF = (float)lA, lresF = (float)lR;
+    if (md == 1) {
+      lvF = 0.f;
+    } else if (md == 2) {
+      D.accA[i] += (double)lA;
+      lvF = 0.f;
+      ls[i] = 0.f;
     } else {
-      lvF = (float)(lu * (R(1) - P.kM));
-      lgEF = (float)(lE + lu * P.kM);
-      lgIF = (float)(lI + lu * P.kM);
+      const R vv = D.aV[off], gEv = D.aGE[off], gIv = D.aGI[off];
+      R lam;
+      const R bias = d_bias<R>(D, P, i, &lam);
+      const R u = d_u<R>(D, P, vv, gEv, gIv, bias);
+      const R thr = P.vThresh + (R)D.aAd[off] + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
+      const R d = u - thr;
+      const R s = D.aSp[off];
+      const R beta = d_beta<R>(D, P, i);
+      R sg;
+      if (D.soft) sg = s * (R(1) - s) / beta;
+      else {
+        const R tt = R(1) + fabs(d) / beta;
+        sg = R(1) / (beta * tt * tt);
+      }
+      R dl = 0;
+      if (scored && D.dL) {
+        if (D.roMap) {
+          const int c = D.roMap[i];
+          if (c >= 0) dl = D.dL[(int64_t)t * D.nro + c];
+        } else {
+          dl = D.dL[i];
+        }
+      }
+      const R lspike = (R)ls[i] + dl;
+      const R lvNew = lvF;
+      const R lsTot = (P.vReset - u) * lvNew + lpA * P.adaptInc + lspike;
+      const R lt = lsTot * R(1) * sg;
+      const R lu = lvNew * (R(1) - s) + lt;
+      const R lthr = -lt;
+      D.accA[i] += (double)(lpA * s);
+      D.accV[i] += (double)lthr;
+      if (D.thrMask && D.thrMask[i]) D.accKc[i] += (double)lthr;
+      ladF = (float)(lA + lthr * P.dA);
+      if (D.coba) {
+        lvF = (float)(lu * (R(1) + P.kM * (R(-1) - gEv * P.cE + gIv * P.cI)));
+        lgEF = (float)(lE + lu * P.kM * (P.eExc - vv) * P.cE);
+        lgIF = (float)(lI + lu * P.kM * (vv - P.eInh) * P.cI);
+        D.accEI[i] += (double)(lu * P.kM * gIv * P.cI * (R(-1) + (vv - P.eInh) * P.cI));
+      } else {
+        lvF = (float)(lu * (R(1) - P.kM));
+        lgEF = (float)(lE + lu * P.kM);
+        lgIF = (float)(lI + lu * P.kM);
+      }
+      if (lam != 0) D.accLa[i] += (double)(lu * P.kM);
+      D.gBias[i] += (double)(lu * P.kM);
+      ls[i] = 0.f;
     }
-    if (lam != 0) D.accLa[i] += (double)(lu * P.kM);
-    D.gBias[i] += (double)(lu * P.kM);
-    ls[i] = 0.f;
+    const R c = P.adjClip;
+    if (c > 0) {
+      auto cl = [c](float x) { return (float)((R)x > c ? c : ((R)x < -c ? -c : (R)x)); };
+      lvF = cl(lvF); lgEF = cl(lgEF); lgIF = cl(lgIF); ladF = cl(ladF); lresF = cl(lresF);
+    }
+    D.lv[i] = lvF;
+    D.lgE[i] = lgEF;
+    D.lgI[i] = lgIF;
+    D.lad[i] = ladF;
+    D.lres[i] = lresF;
   }
-  const R c = P.adjClip;
-  if (c > 0) {
-    auto cl = [c](float x) { return (float)((R)x > c ? c : ((R)x < -c ? -c : (R)x)); };
-    lvF = cl(lvF); lgEF = cl(lgEF); lgIF = cl(lgIF); ladF = cl(ladF); lresF = cl(lresF);
-  }
-  D.lv[i] = lvF;
-  D.lgE[i] = lgEF;
-  D.lgI[i] = lgIF;
-  D.lad[i] = ladF;
-  D.lres[i] = lresF;
 }
 
 // Reverse of the delivery at step t (src/lifdiff.js:635-666), warp per arrival: lanes gather the
 // fan-out's adjoint into lRaw (a fixed-order warp sum) and add each gated edge's
 // dLoss/dW_j = lg[q] * eff to its accumulator; lane 0 updates the presynaptic neuron's terms.
 template <typename R>
-__global__ void k_barrival(DiffDev D, DP<R> P, int32_t t, const float *resRow) {
+__global__ void __launch_bounds__(kDB, 4) k_barrival(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
   const int e = t - (D.nslots - 1);
-  if (e < 0) return;
+  if (t >= D.steps || e < 0) return;
+  const float *resRow = D.resAt + (int64_t)row * D.maxArr;
   const int64_t a0 = D.tOff[e], na = D.tOff[e + 1] - a0;
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -568,32 +663,87 @@ __global__ void k_barrival(DiffDev D, DP<R> P, int32_t t, const float *resRow) {
   }
 }
 
-// Sums the per-neuron accumulators in a fixed order: block partial sums, then one block.
-__global__ void k_reduce(const double *const *src, int nsrc, int32_t N, double *partial) {
-  __shared__ double sm[8][kDB];
+// Per instance, kRB blocks of fixed-order partial sums: the seven per-neuron accumulators
+// (W EI V Kc La A D), the sizeAlpha term through inScale (src/lifdiff.js:650-655, 676-680:
+// gInScale[q] summed over q's in-edges in edge order) and the inhibitory-gain term.
+__global__ void k_reduce(const DiffDev *Ds, double inhGain, double sizeAlpha, double boostCap,
+                         double maxSizeScale, double *partial) {
+  __shared__ DiffDev D;
+  __shared__ double sm[kNSums][kDB];
+  load_dev(Ds, D);
   const int tid = threadIdx.x;
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (int i = blockIdx.x * blockDim.x + tid; i < N; i += gridDim.x * blockDim.x)
-    for (int k = 0; k < nsrc; k++) acc[k] += src[k][i];
-  for (int k = 0; k < nsrc; k++) sm[k][tid] = acc[k];
+  double acc[kNSums];
+#pragma unroll
+  for (int k = 0; k < kNSums; k++) acc[k] = 0;
+  for (int i = blockIdx.x * blockDim.x + tid; i < D.N; i += gridDim.x * blockDim.x) {
+    acc[0] += D.accW[i];
+    acc[1] += D.accEI[i];
+    acc[2] += D.accV[i];
+    acc[3] += D.accKc[i];
+    acc[4] += D.accLa[i];
+    acc[5] += D.accA[i];
+    acc[6] += D.accD[i];
+    double gis = 0, ginh = 0;
+    for (uint32_t e = D.cscPtr[i]; e < D.cscPtr[i + 1]; e++) {
+      const uint32_t j = D.cscEdge[e];
+      if (!D.gate[j]) continue;
+      const bool inh = D.sign[D.cscSrc[e]] < 0;  // eff's sign follows the presynaptic sign
+      const double cw = (double)D.counts[j] * (D.edgeGain ? (double)D.edgeGain[j] : 1.0);
+      gis += cw * (inh ? inhGain : 1.0) * D.gEdge[j];
+      if (inh) ginh += cw * (double)D.inScale[i] * D.gEdge[j];
+    }
+    const double sl = (double)D.sizeLog[i];
+    const double raw = exp(-sizeAlpha * sl);
+    if (raw < boostCap && raw > 1 / maxSizeScale) acc[7] += gis * (-sl) * raw;
+    acc[8] += ginh;
+  }
+#pragma unroll
+  for (int k = 0; k < kNSums; k++) sm[k][tid] = acc[k];
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (tid < s)
-      for (int k = 0; k < nsrc; k++) sm[k][tid] += sm[k][tid + s];
+      for (int k = 0; k < kNSums; k++) sm[k][tid] += sm[k][tid + s];
     __syncthreads();
   }
   if (tid == 0)
-    for (int k = 0; k < nsrc; k++) partial[(int64_t)blockIdx.x * 8 + k] = sm[k][0];
+    for (int k = 0; k < kNSums; k++) partial[((int64_t)blockIdx.y * kRB + blockIdx.x) * kNSums + k] = sm[k][0];
 }
 
-// The readout raster of the recorded forward: out[t * nro + c] = amplitude of readout c at t.
-__global__ void k_raster(DiffDev D, int32_t steps, float *out) {
+// Log-gain gradient as float with non-finite values zeroed and counted (src/lifdiff.js:681-684),
+// and the outScale gradient dL/dlogGain / outScale.
+__global__ void k_finalize(const DiffDev *Ds) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
+    float x = (float)D.gLog[i];
+    if (!isfinite(x)) {
+      x = 0.f;
+      atomicAdd(D.nonfinite, 1);
+    }
+    D.gLogF[i] = x;
+    D.gOut[i] = (double)x / (D.outScale ? (double)D.outScale[i] : 1.0);
+  }
+}
+
+// The readout raster of one instance's recorded forward: out[t * nro + c] = amplitude at t.
+__global__ void k_raster(const DiffDev *Ds, int32_t steps, float *out) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
   for (int t = blockIdx.x; t < steps; t += gridDim.x) {
     const int64_t a = D.tOff[t], b = D.tOff[t + 1];
     for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) {
       const int c = D.roMap[D.tIdx[k]];
       if (c >= 0) out[(int64_t)t * D.nro + c] = D.tAmp[k];
     }
+  }
+}
+
+// out[j] = sum over the listed instances, in list order, of their per-edge gradients.
+__global__ void k_edge_sum(const double *const *g, int32_t n, int64_t E, double *out) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < E; j += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int k = 0; k < n; k++) s += g[k][j];
+    out[j] = s;
   }
 }
 
@@ -623,61 +773,408 @@ int dfail(int code, const char *fmt, ...) {
                    cudaGetErrorString(e_));                                                  \
   } while (0)
 
+// Arrays shared across instances: one device copy per (host pointer, field).
+enum Field { F_INDPTR, F_INDICES, F_COUNTS, F_EDGE_GAIN, F_SIGN, F_OUT_SCALE, F_BETA, F_BIAS, F_THR_MASK,
+             F_BIAS_MASK, F_LOG_GAIN, F_THR_OFFSET, F_SIZE_LOG, F_IN_SCALE, F_SENSORY };
+
+// The derived per-edge arrays of instances with the same graph, edge gains and input scaling.
+struct EdgeGroup {
+  const void *key[5];
+  int rep;  // instance whose arrays define the group
+  float *inScale;
+  uint8_t *gate;
+  double *P;
+  float *Pf;
+};
+
+struct Inst {
+  DiffDev D;
+  float *sizeLogSrc = nullptr, *inScaleSrc = nullptr;
+  uint8_t *sensory = nullptr;
+  int group = 0;
+  int64_t ckptCap = 0, tStepsCap = 0, dLcap = 0, resAtCap = 0, arenaRows = 0;
+  int32_t recordedSteps = 0;
+  float *dLbuf = nullptr;
+  int32_t *roMap = nullptr;
+};
+
 }  // namespace
 
-struct fb_diff {
-  DiffDev D;
+struct fb_diff_batch {
+  int32_t B = 0;
+  std::vector<Inst> in;
+  std::vector<EdgeGroup> groups;
+  std::map<std::pair<const void *, int>, std::pair<void *, size_t>> shared;
+  std::map<std::pair<const void *, const void *>, std::vector<uint32_t *>> csc;  // (indptr, indices) -> CSC
+  std::map<int64_t, float *> zeros;  // read-only zero arrays by length
+  DiffDev *dDevs = nullptr;
   cudaStream_t st = nullptr;
   std::vector<void *> allocs;
-  // inputs kept on the device
-  float *sizeLog = nullptr, *inScaleSrc = nullptr;
-  uint8_t *sensory = nullptr;
-  float *inScale = nullptr;
-  uint8_t *gate = nullptr;
-  double *P = nullptr;
-  float *Pf = nullptr;
-  int32_t f32 = 0;  // FB_DIFF_F32 arithmetic
+  fb_diff_params lastP;
+  int32_t f32 = 0, recordedK = 0, recorded = 0, maxSteps = 0, maxTiles = 1, maxN = 1;
   DP<double> P64;
   DP<float> P32;
-  float *ckpt = nullptr;
-  uint32_t *ckptRng = nullptr;
-  int64_t ckptCap = 0;     // checkpoints allocated
-  int32_t recordedSteps = 0, recordedK = 0, tStepsCap = 0;
-  uint32_t recordedSeed = 0;
-  fb_diff_params lastP;
-  int32_t *roMap = nullptr;
-  int32_t nroCap = 0;
-  float *dLbuf = nullptr;
-  int64_t dLcap = 0;
-  int64_t hostMaxArr = 0;
-  float *resAt = nullptr;
-  int64_t resAtCap = 0;
-  float *arena = nullptr;  // aV aGE aGI aAd aSp for K rows
-  uint8_t *aMode = nullptr;
-  int32_t arenaK = 0;
+  int32_t *err = nullptr, *nonfinite = nullptr;
+  uint32_t *jump = nullptr;
   double *partial = nullptr;
 };
 
-template <typename T>
-static int dalloc(fb_diff *d, T **p, size_t n) {
-  void *q = nullptr;
-  DCU(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
-  d->allocs.push_back(q);
-  *p = (T *)q;
+struct fb_diff {
+  fb_diff_batch *b = nullptr;
+};
+
+namespace {
+
+int balloc(fb_diff_batch *b, void **p, size_t bytes) {
+  *p = nullptr;
+  DCU(cudaMalloc(p, std::max<size_t>(bytes, 16)));
+  b->allocs.push_back(*p);
   return FB_OK;
 }
 
 template <typename T>
-static int dupload(fb_diff *d, T **p, const void *src, size_t n) {
-  if (!src) {
-    *p = nullptr;
+int talloc(fb_diff_batch *b, T **p, size_t n) {
+  void *q;
+  int rc = balloc(b, &q, n * sizeof(T));
+  *p = (T *)q;
+  return rc;
+}
+
+// Upload n elements of src (host or device), or reuse the copy made for the same pointer and field.
+template <typename T>
+int upload(fb_diff_batch *b, T **p, const void *src, size_t n, int field) {
+  *p = nullptr;
+  if (!src) return FB_OK;
+  auto key = std::make_pair(src, field);
+  auto it = b->shared.find(key);
+  if (it != b->shared.end() && it->second.second == n * sizeof(T)) {
+    *p = (T *)it->second.first;
     return FB_OK;
   }
-  int rc = dalloc(d, p, n);
+  int rc = talloc(b, p, n);
   if (rc) return rc;
   DCU(cudaMemcpy(*p, src, n * sizeof(T), cudaMemcpyDefault));
+  b->shared[key] = std::make_pair((void *)*p, n * sizeof(T));
   return FB_OK;
 }
+
+// Carves one allocation into aligned pieces.
+struct Carver {
+  size_t off = 0;
+  std::vector<std::pair<void **, size_t>> items;
+  template <typename T>
+  void add(T **p, size_t n) {
+    items.emplace_back((void **)p, off);
+    off += (n * sizeof(T) + 255) / 256 * 256;
+  }
+  int commit(fb_diff_batch *b) {
+    void *base;
+    int rc = balloc(b, &base, off);
+    if (rc) return rc;
+    for (auto &it : items) *it.first = (char *)base + it.second;
+    return FB_OK;
+  }
+};
+
+// In-edges of every target in ascending edge id (a stable counting sort of the CSR by target).
+int build_csc(fb_diff_batch *b, DiffDev &D) {
+  auto it = b->csc.find(std::make_pair((const void *)D.indptr, (const void *)D.indices));
+  if (it != b->csc.end()) {
+    D.cscPtr = it->second[0];
+    D.cscEdge = it->second[1];
+    D.cscSrc = it->second[2];
+    return FB_OK;
+  }
+  const int64_t N = D.N, E = D.E;
+  std::vector<uint32_t> ip(N + 1), ix(E), cp(N + 1, 0), ce(E), cs(E);
+  DCU(cudaMemcpy(ip.data(), D.indptr, (N + 1) * 4, cudaMemcpyDeviceToHost));
+  if (E) DCU(cudaMemcpy(ix.data(), D.indices, E * 4, cudaMemcpyDeviceToHost));
+  if (ip[0] != 0 || (int64_t)ip[N] != E)
+    return dfail(FB_EINVAL, "fb_diff: indptr[0]=%u, indptr[N]=%u, E=%lld", ip[0], ip[N], (long long)E);
+  for (int64_t i = 0; i < N; i++)
+    if (ip[i + 1] < ip[i]) return dfail(FB_EINVAL, "fb_diff: indptr decreases at %lld", (long long)i);
+  for (int64_t j = 0; j < E; j++)
+    if (ix[j] >= (uint32_t)N) return dfail(FB_EINVAL, "fb_diff: indices[%lld]=%u >= N", (long long)j, ix[j]);
+  for (int64_t j = 0; j < E; j++) cp[ix[j] + 1]++;
+  for (int64_t q = 0; q < N; q++) cp[q + 1] += cp[q];
+  std::vector<uint32_t> fill(cp.begin(), cp.end() - 1);
+  for (int64_t s = 0; s < N; s++)
+    for (uint32_t j = ip[s]; j < ip[s + 1]; j++) {
+      const uint32_t o = fill[ix[j]]++;
+      ce[o] = j;
+      cs[o] = (uint32_t)s;
+    }
+  uint32_t *a, *e, *s;
+  int rc;
+  if ((rc = talloc(b, &a, N + 1)) || (rc = talloc(b, &e, E)) || (rc = talloc(b, &s, E))) return rc;
+  DCU(cudaMemcpy(a, cp.data(), (N + 1) * 4, cudaMemcpyHostToDevice));
+  if (E) {
+    DCU(cudaMemcpy(e, ce.data(), E * 4, cudaMemcpyHostToDevice));
+    DCU(cudaMemcpy(s, cs.data(), E * 4, cudaMemcpyHostToDevice));
+  }
+  b->csc[std::make_pair((const void *)D.indptr, (const void *)D.indices)] = {a, e, s};
+  D.cscPtr = a;
+  D.cscEdge = e;
+  D.cscSrc = s;
+  return FB_OK;
+}
+
+int create_instance(fb_diff_batch *b, Inst &I, const fb_diff_net *net, int64_t tape_cap) {
+  DiffDev &D = I.D;
+  memset(&D, 0, sizeof D);
+  if (net->N <= 0 || net->E < 0 || !net->indptr || (net->E && (!net->indices || !net->counts)) || !net->sign ||
+      net->nDriven < 0 || net->nDriven > net->N || (net->nDriven && (!net->driven || !net->drive)))
+    return dfail(FB_EINVAL, "fb_diff: bad network description (N=%d E=%lld nDriven=%d)", net->N,
+                 (long long)net->E, net->nDriven);
+  const int64_t N = net->N, E = net->E;
+  D.N = net->N;
+  D.E = net->E;
+  D.nDriven = net->nDriven;
+  D.nTiles = (int32_t)((N + kDB - 1) / kDB);
+  int rc;
+  float *f;
+#define UP(dst, src, n, fld, T)                           \
+  do {                                                    \
+    T *p_;                                                \
+    if ((rc = upload(b, &p_, (src), (n), (fld)))) return rc; \
+    dst = p_;                                             \
+  } while (0)
+  UP(D.indptr, net->indptr, N + 1, F_INDPTR, uint32_t);
+  UP(D.indices, net->indices, E, F_INDICES, uint32_t);
+  UP(D.counts, net->counts, E, F_COUNTS, float);
+  UP(D.edgeGain, net->edge_gain, E, F_EDGE_GAIN, float);
+  UP(D.sign, net->sign, N, F_SIGN, float);
+  UP(D.outScale, net->out_scale, N, F_OUT_SCALE, float);
+  UP(D.betaArr, net->beta, N, F_BETA, float);
+  UP(D.biasArr, net->bias, N, F_BIAS, float);
+  UP(D.thrMask, net->thr_mask, N, F_THR_MASK, uint8_t);
+  UP(D.biasMask, net->bias_mask, N, F_BIAS_MASK, uint8_t);
+  UP(I.inScaleSrc, net->in_scale, N, F_IN_SCALE, float);
+  UP(I.sensory, net->sensory, N, F_SENSORY, uint8_t);
+#undef UP
+  if ((rc = build_csc(b, D))) return rc;
+  // arrays that default to zeros get their own copy when not given (they can be set later)
+  {
+    std::vector<float> z(N, 0.f);
+    auto own = [&](const float *src, int fld, const float **dst) -> int {
+      float *p;
+      int r = src ? upload(b, &p, src, N, fld) : talloc(b, &p, N);
+      if (r) return r;
+      if (!src) {
+        DCU(cudaMemcpy(p, z.data(), N * 4, cudaMemcpyHostToDevice));
+      }
+      *dst = p;
+      return FB_OK;
+    };
+    if ((rc = own(net->log_gain, F_LOG_GAIN, &D.logGain)) || (rc = own(net->thr_offset, F_THR_OFFSET, &D.thrOffset)))
+      return rc;
+    float *sl;
+    if (net->size_log) {
+      if ((rc = upload(b, &sl, net->size_log, N, F_SIZE_LOG))) return rc;
+    } else if (b->zeros.count(N)) {
+      sl = b->zeros[N];
+    } else {  // sizeLog cannot be set later: instances of one size share a zero array
+      if ((rc = talloc(b, &sl, N))) return rc;
+      DCU(cudaMemcpy(sl, z.data(), N * 4, cudaMemcpyHostToDevice));
+      b->zeros[N] = sl;
+    }
+    D.sizeLog = sl;
+    I.sizeLogSrc = sl;
+  }
+  // the drive: validated on the host, one copy per instance
+  {
+    std::vector<float> dr(N, 0.f);
+    std::vector<int32_t> dv(std::max<int32_t>(net->nDriven, 1), 0);
+    if (net->nDriven) {
+      DCU(cudaMemcpy(dv.data(), net->driven, 4 * (size_t)net->nDriven, cudaMemcpyDefault));
+      DCU(cudaMemcpy(dr.data(), net->drive, 4 * (size_t)N, cudaMemcpyDefault));
+      for (int32_t k = 0; k < net->nDriven; k++)
+        if (dv[k] < 0 || dv[k] >= N) return dfail(FB_EINVAL, "fb_diff: driven[%d]=%d", k, dv[k]);
+    }
+    int32_t *dvD;
+    if ((rc = talloc(b, &f, N)) || (rc = talloc(b, &dvD, dv.size()))) return rc;
+    DCU(cudaMemcpy(f, dr.data(), N * 4, cudaMemcpyHostToDevice));
+    DCU(cudaMemcpy(dvD, dv.data(), dv.size() * 4, cudaMemcpyHostToDevice));
+    D.drive = f;
+    D.driven = dvD;
+  }
+  // per-instance state, scratch, adjoint state and accumulators in one allocation
+  D.ovfCap = (uint32_t)std::min<int64_t>(std::min<int64_t>(E + 1, (1 << 20) + E / 8), 0x7fffffff);
+  D.tapeCap = tape_cap > 0 ? tape_cap : std::max<int64_t>(1 << 20, 64 * N);
+  Carver c;
+  c.add(&D.v, N); c.add(&D.gE, N); c.add(&D.gI, N); c.add(&D.adapt, N); c.add(&D.res, N);
+  c.add(&D.refr, N); c.add(&D.spikeCount, N); c.add(&D.isForced, N); c.add(&D.rng, 1);
+  c.add(&D.cnt, N); c.add(&D.bucket, N * kDBucket); c.add(&D.ovfHead, N); c.add(&D.ovfTop, 1);
+  c.add(&D.ovf, D.ovfCap); c.add(&D.effK, N);
+  c.add(&D.stage, (size_t)D.nTiles * kDB); c.add(&D.stageAmp, (size_t)D.nTiles * kDB); c.add(&D.tileCnt, D.nTiles);
+  c.add(&D.lv, N); c.add(&D.lgE, N); c.add(&D.lgI, N); c.add(&D.lad, N); c.add(&D.lres, N);
+  c.add(&D.accA, N); c.add(&D.accV, N); c.add(&D.accKc, N); c.add(&D.accLa, N); c.add(&D.accEI, N);
+  c.add(&D.accW, N); c.add(&D.accD, N); c.add(&D.gLog, N); c.add(&D.gBias, N); c.add(&D.gEdge, E);
+  c.add(&D.gLogF, N); c.add(&D.gOut, N); c.add(&D.nonfinite, 1);
+  c.add(&D.tIdx, D.tapeCap); c.add(&D.tAmp, D.tapeCap);
+  if ((rc = c.commit(b))) return rc;
+  DCU(cudaMemset(D.ovfTop, 0, 4));
+  DCU(cudaMemset(D.cnt, 0, N * 4));
+  DCU(cudaMemset(D.ovfHead, 0xff, N * 4));
+  D.err = b->err;
+  D.jump = b->jump;
+  return FB_OK;
+}
+
+// Edge groups: instances sharing graph, edge gains and input scaling share inScale/gate/P.
+int build_groups(fb_diff_batch *b) {
+  for (int k = 0; k < b->B; k++) {
+    Inst &I = b->in[k];
+    const void *key[5] = {I.D.indptr, I.D.edgeGain, I.sizeLogSrc, I.inScaleSrc, I.sensory};
+    int g = -1;
+    for (size_t q = 0; q < b->groups.size(); q++)
+      if (!memcmp(b->groups[q].key, key, sizeof key)) g = (int)q;
+    if (g < 0) {
+      EdgeGroup G;
+      memcpy(G.key, key, sizeof key);
+      G.rep = k;
+      const int64_t N = I.D.N, E = I.D.E;
+      int rc;
+      Carver c;
+      c.add(&G.inScale, N); c.add(&G.gate, E); c.add(&G.P, E); c.add(&G.Pf, E);
+      if ((rc = c.commit(b))) return rc;
+      b->groups.push_back(G);
+      g = (int)b->groups.size() - 1;
+    }
+    I.group = g;
+    I.D.inScale = b->groups[g].inScale;
+    I.D.gate = b->groups[g].gate;
+    I.D.P = b->groups[g].P;
+    I.D.Pf = b->groups[g].Pf;
+  }
+  return FB_OK;
+}
+
+template <typename R>
+DP<R> typed_params(const fb_diff_params *p) {
+  DP<R> q;
+  q.dt = (R)p->dt; q.vRest = (R)p->vRest; q.vThresh = (R)p->vThresh; q.vReset = (R)p->vReset;
+  q.tRef = (R)p->tRef; q.wSyn = (R)p->wSyn; q.adaptInc = (R)p->adaptInc; q.depU = (R)p->depU;
+  q.eExc = (R)p->eExc; q.eInh = (R)p->eInh; q.inhGain = (R)p->inhGain; q.kcThreshold = (R)p->kcThreshold;
+  q.laminaBias = (R)p->laminaBias; q.beta = (R)p->surrogateBeta; q.adjClip = (R)p->adjClip;
+  q.dE = (R)std::exp(-p->dt / p->tauSyn);
+  q.dA = (R)std::exp(-p->dt / p->adaptTau);
+  q.kRec = (R)(p->dt / p->depTau);
+  q.kM = (R)(p->dt / p->tauM);
+  q.dtS = (R)(p->dt / 1000);
+  q.cE = (R)(1 / (p->eExc - p->vRest));
+  q.cI = (R)(1 / (p->vRest - p->eInh));
+  return q;
+}
+
+int fill_params(fb_diff_batch *b, const fb_diff_params *p) {
+  if (!(p->dt > 0) || !(p->tauM > 0) || !(p->tauSyn > 0) || p->checkpoint <= 0)
+    return dfail(FB_EINVAL, "fb_diff: dt, tauM, tauSyn and checkpoint must be positive");
+  if (p->precision != FB_DIFF_F64 && p->precision != FB_DIFF_F32)
+    return dfail(FB_EINVAL, "fb_diff: precision must be FB_DIFF_F64 or FB_DIFF_F32 (got %d)", p->precision);
+  const int32_t nslots = (int32_t)std::max(1.0, std::floor(p->delay / p->dt + 0.5)) + 1;
+  for (Inst &I : b->in) {
+    if (I.D.nslots && I.D.nslots != nslots && I.D.lsRing) I.D.lsRing = nullptr;  // ring depth changed
+    I.D.nslots = nslots;
+    I.D.K = p->checkpoint;
+    I.D.coba = p->coba ? 1 : 0;
+    I.D.soft = p->soft ? 1 : 0;
+  }
+  b->f32 = p->precision == FB_DIFF_F32;
+  b->P64 = typed_params<double>(p);
+  b->P32 = typed_params<float>(p);
+  b->lastP = *p;
+  return FB_OK;
+}
+
+int push_devs(fb_diff_batch *b) {
+  std::vector<DiffDev> h(b->B);
+  for (int k = 0; k < b->B; k++) h[k] = b->in[k].D;
+  DCU(cudaMemcpyAsync(b->dDevs, h.data(), sizeof(DiffDev) * b->B, cudaMemcpyHostToDevice, b->st));
+  DCU(cudaStreamSynchronize(b->st));
+  return FB_OK;
+}
+
+int prepare(fb_diff_batch *b, const fb_diff_params *p) {
+  for (const EdgeGroup &G : b->groups) {
+    const Inst &I = b->in[G.rep];
+    k_prepare<<<256, kDB, 0, b->st>>>(I.D.N, G.inScale, I.sizeLogSrc, I.inScaleSrc, p->sizeAlpha,
+                                       p->maxSizeScale, p->boostCap);
+    k_prepare_edges<<<1024, kDB, 0, b->st>>>(I.D.E, I.D.indices, I.D.counts, I.D.edgeGain, G.inScale, I.sensory,
+                                              p->minSyn, G.gate, G.P, G.Pf);
+  }
+  DCU(cudaGetLastError());
+  return FB_OK;
+}
+
+int check_err(fb_diff_batch *b, const char *fn) {
+  int32_t err = 0;
+  DCU(cudaMemcpyAsync(&err, b->err, 4, cudaMemcpyDeviceToHost, b->st));
+  DCU(cudaStreamSynchronize(b->st));
+  if (err) {
+    cudaMemset(b->err, 0, 4);
+    return dfail(err, "%s: %s", fn, err == FB_EOVERFLOW ? "tape or delivery scratch overflow" : "device error");
+  }
+  return FB_OK;
+}
+
+// Launch shapes: per-neuron kernels one tile per block for a single instance, about four waves of
+// 256-thread blocks over the whole batch otherwise; warp-per-arrival kernels 304 blocks over the
+// batch (at least two per instance).
+dim3 neuron_grid(const fb_diff_batch *b) {
+  const int gx = b->B == 1 ? b->maxTiles : std::max(1, std::min(b->maxTiles, 1216 / b->B));
+  return dim3(gx, b->B);
+}
+dim3 arrival_grid(const fb_diff_batch *b) { return dim3(std::max(2, 304 / b->B), b->B); }
+
+template <typename R>
+void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int32_t row) {
+  k_deliver<R><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, P, t, row);
+  k_forced<R><<<dim3(1, b->B), 512, 0, b->st>>>(b->dDevs, P, t, replay);
+  k_update<R><<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, P, t, row);
+  if (!replay) k_emit<<<dim3(1, b->B), 512, 0, b->st>>>(b->dDevs, t);
+}
+
+void run_step(fb_diff_batch *b, int32_t t, int32_t replay, int32_t row) {
+  if (b->f32) run_step_t<float>(b, b->P32, t, replay, row);
+  else run_step_t<double>(b, b->P64, t, replay, row);
+}
+
+void reverse_step(fb_diff_batch *b, int32_t t, int32_t row, int32_t scored) {
+  if (b->f32) {
+    k_bneuron<float><<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P32, t, row, scored);
+    k_barrival<float><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P32, t, row);
+  } else {
+    k_bneuron<double><<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P64, t, row, scored);
+    k_barrival<double><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P64, t, row);
+  }
+}
+
+int set_readout(fb_diff_batch *b, Inst &I, int32_t nro, const int32_t *ro) {
+  DiffDev &D = I.D;
+  if (!I.roMap) {
+    int rc = talloc(b, &I.roMap, D.N);
+    if (rc) return rc;
+  }
+  std::vector<int32_t> map(D.N, -1), h(std::max(nro, 1));
+  if (nro) DCU(cudaMemcpy(h.data(), ro, (size_t)nro * 4, cudaMemcpyDefault));
+  for (int32_t c = 0; c < nro; c++) {
+    if (h[c] < 0 || h[c] >= D.N) return dfail(FB_EINVAL, "readout[%d]=%d out of range", c, h[c]);
+    map[h[c]] = c;
+  }
+  DCU(cudaMemcpy(I.roMap, map.data(), (size_t)D.N * 4, cudaMemcpyHostToDevice));
+  D.roMap = I.roMap;
+  D.nro = nro;
+  return FB_OK;
+}
+
+uint32_t seed_state(uint32_t seed) {
+  // (seed * 2654435761) >>> 0 || 1, the product in double (src/lifdiff.js:221)
+  uint32_t s0 = (uint32_t)std::fmod(std::floor((double)seed * 2654435761.0), 4294967296.0);
+  return s0 ? s0 : 1;
+}
+
+}  // namespace
 
 extern "C" void fb_diff_default_params(fb_diff_params *p) {
   if (!p) return;
@@ -691,358 +1188,153 @@ extern "C" void fb_diff_default_params(fb_diff_params *p) {
   p->precision = FB_DIFF_F64;
 }
 
-template <typename R>
-static DP<R> typed_params(const DiffDev &D) {
-  DP<R> q;
-  q.dt = (R)D.dt; q.vRest = (R)D.vRest; q.vThresh = (R)D.vThresh; q.vReset = (R)D.vReset;
-  q.tRef = (R)D.tRef; q.wSyn = (R)D.wSyn; q.adaptInc = (R)D.adaptInc; q.depU = (R)D.depU;
-  q.eExc = (R)D.eExc; q.eInh = (R)D.eInh; q.inhGain = (R)D.inhGain; q.kcThreshold = (R)D.kcThreshold;
-  q.laminaBias = (R)D.laminaBias; q.beta = (R)D.beta; q.adjClip = (R)D.adjClip; q.dE = (R)D.dE;
-  q.dA = (R)D.dA; q.kRec = (R)D.kRec; q.kM = (R)D.kM; q.dtS = (R)D.dtS; q.cE = (R)D.cE; q.cI = (R)D.cI;
-  return q;
+extern "C" int fb_diff_batch_destroy(fb_diff_batch *b) {
+  if (!b) return FB_OK;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (void *p : b->allocs) cudaFree(p);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return FB_OK;
 }
 
-extern "C" int fb_diff_create(const fb_diff_net *net, int64_t tape_cap, fb_diff **out) {
-  if (!net || !out) return dfail(FB_EINVAL, "fb_diff_create: null argument");
+extern "C" int fb_diff_batch_create(const fb_diff_net *nets, int32_t B, int64_t tape_cap, fb_diff_batch **out) {
+  if (!nets || !out || B <= 0) return dfail(FB_EINVAL, "fb_diff_batch_create: bad arguments (B=%d)", B);
   *out = nullptr;
-  if (net->N <= 0 || net->E < 0 || !net->indptr || (net->E && (!net->indices || !net->counts)) || !net->sign ||
-      net->nDriven < 0 || net->nDriven > net->N || (net->nDriven && (!net->driven || !net->drive)))
-    return dfail(FB_EINVAL, "fb_diff_create: bad network description (N=%d E=%lld nDriven=%d)", net->N,
-                 (long long)net->E, net->nDriven);
-  fb_diff *d = new fb_diff;
-  memset(&d->D, 0, sizeof d->D);
-  DiffDev &D = d->D;
-  const int64_t N = net->N, E = net->E;
-  D.N = net->N;
-  D.E = net->E;
-  D.nDriven = net->nDriven;
-  int rc = 0;
-  auto up_u32 = [&](const uint32_t **dst, const uint32_t *src, size_t n) {
-    uint32_t *p;
-    int r = dupload(d, &p, src, n);
-    *dst = p;
+  fb_diff_batch *b = new fb_diff_batch;
+  b->B = B;
+  b->in.resize(B);
+  int rc;
+  auto bail = [&](int r) {
+    fb_diff_batch_destroy(b);
     return r;
   };
-  auto up_f = [&](const float **dst, const float *src, size_t n) {
-    float *p;
-    int r = dupload(d, &p, src, n);
-    *dst = p;
-    return r;
-  };
-  auto up_u8 = [&](const uint8_t **dst, const uint8_t *src, size_t n) {
-    uint8_t *p;
-    int r = dupload(d, &p, src, n);
-    *dst = p;
-    return r;
-  };
-  if ((rc = up_u32(&D.indptr, net->indptr, N + 1)) || (rc = up_u32(&D.indices, net->indices, E)) ||
-      (rc = up_f(&D.counts, net->counts, E)) || (rc = up_f(&D.edgeGain, net->edge_gain, E)) ||
-      (rc = up_f(&D.sign, net->sign, N)) || (rc = up_f(&D.outScale, net->out_scale, N)) ||
-      (rc = up_f(&D.betaArr, net->beta, N)) || (rc = up_f(&D.biasArr, net->bias, N)) ||
-      (rc = up_u8(&D.thrMask, net->thr_mask, N)) || (rc = up_u8(&D.biasMask, net->bias_mask, N))) {
-    fb_diff_destroy(d);
-    return rc;
-  }
-  {
-    float *p;
-    std::vector<float> z(N, 0.f);
-    if ((rc = dupload(d, &p, net->log_gain ? (const void *)net->log_gain : z.data(), N))) { fb_diff_destroy(d); return rc; }
-    D.logGain = p;
-    if ((rc = dupload(d, &p, net->thr_offset ? (const void *)net->thr_offset : z.data(), N))) { fb_diff_destroy(d); return rc; }
-    D.thrOffset = p;
-    if ((rc = dupload(d, &d->sizeLog, net->size_log ? (const void *)net->size_log : z.data(), N))) { fb_diff_destroy(d); return rc; }
-    if ((rc = dupload(d, &d->inScaleSrc, net->in_scale, N)) || (rc = dupload(d, &d->sensory, net->sensory, N))) {
-      fb_diff_destroy(d);
-      return rc;
-    }
-    std::vector<float> dr(N, 0.f);
-    std::vector<int32_t> dv(net->nDriven);
-    if (net->nDriven) {
-      std::vector<int32_t> hv(net->nDriven);
-      std::vector<float> hd(N);
-      if (cudaMemcpy(hv.data(), net->driven, 4 * net->nDriven, cudaMemcpyDefault) != cudaSuccess ||
-          cudaMemcpy(hd.data(), net->drive, 4 * N, cudaMemcpyDefault) != cudaSuccess) {
-        fb_diff_destroy(d);
-        return dfail(FB_ECUDA, "fb_diff_create: reading the drive failed");
-      }
-      for (int32_t k = 0; k < net->nDriven; k++) {
-        if (hv[k] < 0 || hv[k] >= N) { fb_diff_destroy(d); return dfail(FB_EINVAL, "fb_diff_create: driven[%d]=%d", k, hv[k]); }
-        dv[k] = hv[k];
-      }
-      dr = hd;
-    }
-    if ((rc = dupload(d, &p, dr.data(), N))) { fb_diff_destroy(d); return rc; }
-    D.drive = p;
-    int32_t *q;
-    if ((rc = dupload(d, &q, dv.data(), std::max<int32_t>(net->nDriven, 1)))) { fb_diff_destroy(d); return rc; }
-    D.driven = q;
-  }
-  // derived arrays, state, scratch, tape, adjoint state
-  D.nTiles = (int32_t)((N + kDB - 1) / kDB);
-  int32_t *i32;
-  float *f;
-  if ((rc = dalloc(d, &d->inScale, N)) || (rc = dalloc(d, &d->gate, E)) || (rc = dalloc(d, &d->P, E)) ||
-      (rc = dalloc(d, &d->Pf, E)) ||
-      (rc = dalloc(d, &D.v, N)) || (rc = dalloc(d, &D.gE, N)) || (rc = dalloc(d, &D.gI, N)) ||
-      (rc = dalloc(d, &D.adapt, N)) || (rc = dalloc(d, &D.res, N)) || (rc = dalloc(d, &D.refr, N)) ||
-      (rc = dalloc(d, &D.spikeCount, N)) || (rc = dalloc(d, &D.isForced, N)) || (rc = dalloc(d, &D.rng, 1)) ||
-      (rc = dalloc(d, &D.cnt, N)) || (rc = dalloc(d, &D.bucket, N * kDBucket)) || (rc = dalloc(d, &D.ovfHead, N)) ||
-      (rc = dalloc(d, &D.ovfTop, 1)) || (rc = dalloc(d, &D.effK, N)) ||
-      (rc = dalloc(d, &D.stage, (size_t)D.nTiles * kDB)) || (rc = dalloc(d, &D.stageAmp, (size_t)D.nTiles * kDB)) ||
-      (rc = dalloc(d, &D.tileCnt, D.nTiles)) || (rc = dalloc(d, &D.err, 1)) ||
-      (rc = dalloc(d, &D.lv, N)) || (rc = dalloc(d, &D.lgE, N)) || (rc = dalloc(d, &D.lgI, N)) ||
-      (rc = dalloc(d, &D.lad, N)) || (rc = dalloc(d, &D.lres, N)) ||
-      (rc = dalloc(d, &D.accA, N)) || (rc = dalloc(d, &D.accV, N)) || (rc = dalloc(d, &D.accKc, N)) ||
-      (rc = dalloc(d, &D.accLa, N)) || (rc = dalloc(d, &D.accEI, N)) || (rc = dalloc(d, &D.accW, N)) ||
-      (rc = dalloc(d, &D.accD, N)) || (rc = dalloc(d, &D.gLog, N)) || (rc = dalloc(d, &D.gBias, N)) ||
-      (rc = dalloc(d, &D.gEdge, E)) || (rc = dalloc(d, &d->partial, 8 * 256))) {
-    fb_diff_destroy(d);
-    return rc;
-  }
-  D.inScale = d->inScale;
-  D.gate = d->gate;
-  D.P = d->P;
-  D.Pf = d->Pf;
-  D.ovfCap = (uint32_t)std::min<int64_t>((1 << 20) + E / 8, 0x7fffffff);
-  DOvf *ov;
-  if ((rc = dalloc(d, &ov, D.ovfCap))) { fb_diff_destroy(d); return rc; }
-  D.ovf = ov;
-  D.tapeCap = tape_cap > 0 ? tape_cap : std::max<int64_t>(1 << 20, 64 * N);
-  if ((rc = dalloc(d, &i32, D.tapeCap)) || (rc = dalloc(d, &f, D.tapeCap))) { fb_diff_destroy(d); return rc; }
-  D.tIdx = i32;
-  D.tAmp = f;
   std::vector<uint32_t> tab;
   host_jump_tables(tab);
-  uint32_t *jt;
-  if ((rc = dupload(d, &jt, tab.data(), tab.size()))) { fb_diff_destroy(d); return rc; }
-  D.jump = jt;
-  cudaMemset(D.err, 0, 4);
-  cudaMemset(D.ovfTop, 0, 4);
-  if (cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking) != cudaSuccess) {
-    fb_diff_destroy(d);
-    return dfail(FB_ECUDA, "fb_diff_create: stream creation failed");
+  if ((rc = talloc(b, &b->err, 1)) || (rc = talloc(b, &b->jump, tab.size())) ||
+      (rc = talloc(b, &b->partial, (size_t)B * kRB * kNSums)) || (rc = talloc(b, &b->dDevs, B)))
+    return bail(rc);
+  if (cudaMemcpy(b->jump, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(b->err, 0, 4) != cudaSuccess)
+    return bail(dfail(FB_ECUDA, "fb_diff_batch_create: device setup failed"));
+  for (int k = 0; k < B; k++) {
+    if ((rc = create_instance(b, b->in[k], nets + k, tape_cap))) return bail(rc);
+    b->maxTiles = std::max(b->maxTiles, b->in[k].D.nTiles);
+    b->maxN = std::max(b->maxN, b->in[k].D.N);
   }
-  *out = d;
+  if ((rc = build_groups(b))) return bail(rc);
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(dfail(FB_ECUDA, "fb_diff_batch_create: stream creation failed"));
+  *out = b;
   return FB_OK;
 }
 
-extern "C" int fb_diff_destroy(fb_diff *d) {
-  if (!d) return FB_OK;
-  if (d->st) cudaStreamSynchronize(d->st);
-  for (void *p : d->allocs) cudaFree(p);
-  if (d->st) cudaStreamDestroy(d->st);
-  delete d;
-  return FB_OK;
-}
-
-extern "C" int fb_diff_set(fb_diff *d, int32_t field, const float *values) {
-  if (!d || !values) return dfail(FB_EINVAL, "fb_diff_set: null argument");
+extern "C" int fb_diff_batch_set(fb_diff_batch *b, int32_t inst, int32_t field, const float *values) {
+  if (!b || !values || inst < 0 || inst >= b->B) return dfail(FB_EINVAL, "fb_diff_set: bad arguments");
+  const DiffDev &D = b->in[inst].D;
   const float *dst;
-  size_t n = (size_t)d->D.N;
+  size_t n = (size_t)D.N;
   switch (field) {
-    case FB_DIFF_LOG_GAIN: dst = d->D.logGain; break;
-    case FB_DIFF_OUT_SCALE: dst = d->D.outScale; break;
-    case FB_DIFF_THR_OFFSET: dst = d->D.thrOffset; break;
-    case FB_DIFF_BIAS: dst = d->D.biasArr; break;
-    case FB_DIFF_EDGE_GAIN: dst = d->D.edgeGain; n = (size_t)d->D.E; break;
-    case FB_DIFF_DRIVE: dst = d->D.drive; break;
+    case FB_DIFF_LOG_GAIN: dst = D.logGain; break;
+    case FB_DIFF_OUT_SCALE: dst = D.outScale; break;
+    case FB_DIFF_THR_OFFSET: dst = D.thrOffset; break;
+    case FB_DIFF_BIAS: dst = D.biasArr; break;
+    case FB_DIFF_EDGE_GAIN: dst = D.edgeGain; n = (size_t)D.E; break;
+    case FB_DIFF_DRIVE: dst = D.drive; break;
     default: return dfail(FB_EINVAL, "fb_diff_set: unknown field %d", field);
   }
   if (!dst) return dfail(FB_ESTATE, "fb_diff_set: field %d was not given at creation", field);
-  DCU(cudaMemcpyAsync((void *)dst, values, n * 4, cudaMemcpyDefault, d->st));
-  DCU(cudaStreamSynchronize(d->st));
+  DCU(cudaMemcpyAsync((void *)dst, values, n * 4, cudaMemcpyDefault, b->st));
+  DCU(cudaStreamSynchronize(b->st));
   return FB_OK;
 }
 
-static int fill_params(fb_diff *d, const fb_diff_params *p) {
-  DiffDev &D = d->D;
-  if (!(p->dt > 0) || !(p->tauM > 0) || !(p->tauSyn > 0) || p->checkpoint <= 0)
-    return dfail(FB_EINVAL, "fb_diff: dt, tauM, tauSyn and checkpoint must be positive");
-  if (p->precision != FB_DIFF_F64 && p->precision != FB_DIFF_F32)
-    return dfail(FB_EINVAL, "fb_diff: precision must be FB_DIFF_F64 or FB_DIFF_F32 (got %d)", p->precision);
-  D.nslots = (int32_t)std::max(1.0, std::floor(p->delay / p->dt + 0.5)) + 1;
-  D.K = p->checkpoint;
-  D.coba = p->coba ? 1 : 0;
-  D.soft = p->soft ? 1 : 0;
-  D.dt = p->dt; D.vRest = p->vRest; D.vThresh = p->vThresh; D.vReset = p->vReset; D.tRef = p->tRef;
-  D.wSyn = p->wSyn; D.adaptInc = p->adaptInc; D.depU = p->depU; D.eExc = p->eExc; D.eInh = p->eInh;
-  D.inhGain = p->inhGain; D.kcThreshold = p->kcThreshold; D.laminaBias = p->laminaBias;
-  D.beta = p->surrogateBeta; D.adjClip = p->adjClip;
-  D.dE = std::exp(-p->dt / p->tauSyn);
-  D.dA = std::exp(-p->dt / p->adaptTau);
-  D.kRec = p->dt / p->depTau;
-  D.kM = p->dt / p->tauM;
-  D.dtS = p->dt / 1000;
-  D.cE = 1 / (p->eExc - p->vRest);
-  D.cI = 1 / (p->vRest - p->eInh);
-  d->f32 = p->precision == FB_DIFF_F32;
-  d->P64 = typed_params<double>(D);
-  d->P32 = typed_params<float>(D);
-  d->lastP = *p;
-  return FB_OK;
-}
-
-static int prepare(fb_diff *d, const fb_diff_params *p) {
-  DiffDev &D = d->D;
-  k_prepare<<<256, kDB, 0, d->st>>>(D, d->inScale, d->gate, d->P, d->sizeLog, d->inScaleSrc, d->sensory,
-                                     p->sizeAlpha, p->maxSizeScale, p->boostCap, p->minSyn);
-  k_prepare_edges<<<1024, kDB, 0, d->st>>>(D, d->inScale, d->gate, d->P, d->Pf, d->sensory, p->minSyn);
-  DCU(cudaGetLastError());
-  return FB_OK;
-}
-
-static int check_err(fb_diff *d, const char *fn) {
-  int32_t err = 0;
-  DCU(cudaMemcpyAsync(&err, d->D.err, 4, cudaMemcpyDeviceToHost, d->st));
-  DCU(cudaStreamSynchronize(d->st));
-  if (err) {
-    cudaMemset(d->D.err, 0, 4);
-    return dfail(err, "%s: %s", fn, err == FB_EOVERFLOW ? "tape or delivery scratch overflow" : "device error");
-  }
-  return FB_OK;
-}
-
-template <typename R>
-static void run_step_t(fb_diff *d, const DP<R> &P, int32_t t, int32_t replay, int32_t row, float *resRow) {
-  DiffDev &D = d->D;
-  const int nb = (int)((D.N + kDB - 1) / kDB);
-  k_deliver<R><<<304, kDB, 0, d->st>>>(D, P, t, resRow);
-  k_forced<R><<<1, 512, 0, d->st>>>(D, P, t, replay);
-  k_update<R><<<nb, kDB, 0, d->st>>>(D, P, row);
-  if (!replay) k_emit<<<1, 512, 0, d->st>>>(D, t);
-  else cudaMemsetAsync(D.ovfTop, 0, 4, d->st);
-}
-
-static void run_step(fb_diff *d, int32_t t, int32_t replay, int32_t row, float *resRow) {
-  if (d->f32) run_step_t<float>(d, d->P32, t, replay, row, resRow);
-  else run_step_t<double>(d, d->P64, t, replay, row, resRow);
-}
-
-static void reverse_step(fb_diff *d, int32_t t, int32_t row, int32_t scored, const float *resRow) {
-  DiffDev &D = d->D;
-  const int nblk = (int)((D.N + kDB - 1) / kDB);
-  if (d->f32) {
-    k_bneuron<float><<<nblk, kDB, 0, d->st>>>(D, d->P32, t, row, scored);
-    k_barrival<float><<<304, kDB, 0, d->st>>>(D, d->P32, t, resRow);
-  } else {
-    k_bneuron<double><<<nblk, kDB, 0, d->st>>>(D, d->P64, t, row, scored);
-    k_barrival<double><<<304, kDB, 0, d->st>>>(D, d->P64, t, resRow);
-  }
-}
-
-extern "C" int fb_diff_forward(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed,
-                               int32_t record, float *spike_count) {
-  if (!d || !p || steps < 0) return dfail(FB_EINVAL, "fb_diff_forward: bad arguments");
-  int rc = fill_params(d, p);
+extern "C" int fb_diff_batch_forward(fb_diff_batch *b, const fb_diff_params *p, const int32_t *steps,
+                                     const uint32_t *seeds, int32_t record, float *spike_counts) {
+  if (!b || !p || !steps || !seeds) return dfail(FB_EINVAL, "fb_diff_forward: bad arguments");
+  int rc = fill_params(b, p);
   if (rc) return rc;
-  DiffDev &D = d->D;
-  const int64_t N = D.N;
-  if (record) {
-    const int64_t nck = (steps + D.K - 1) / D.K;
-    if (nck > d->ckptCap) {
-      void *q = nullptr, *r = nullptr;
-      if (cudaMalloc(&q, (size_t)std::max<int64_t>(nck, 1) * 6 * N * 4) != cudaSuccess ||
-          cudaMalloc(&r, (size_t)std::max<int64_t>(nck, 1) * 4) != cudaSuccess) {
-        cudaFree(q);
-        return dfail(FB_ENOMEM, "fb_diff_forward: %lld checkpoints of %lld neurons", (long long)nck, (long long)N);
+  int32_t maxSteps = 0;
+  for (int k = 0; k < b->B; k++) {
+    if (steps[k] < 0) return dfail(FB_EINVAL, "fb_diff_forward: steps[%d]=%d", k, steps[k]);
+    maxSteps = std::max(maxSteps, steps[k]);
+  }
+  for (int k = 0; k < b->B; k++) {
+    Inst &I = b->in[k];
+    DiffDev &D = I.D;
+    const int64_t N = D.N;
+    D.steps = steps[k];
+    D.seed0 = seed_state(seeds[k]);
+    if (record) {
+      const int64_t nck = std::max<int64_t>(1, (steps[k] + D.K - 1) / D.K);
+      if (nck > I.ckptCap) {
+        if ((rc = talloc(b, &D.ckpt, (size_t)nck * 6 * N)) || (rc = talloc(b, &D.ckptRng, (size_t)nck))) return rc;
+        I.ckptCap = nck;
       }
-      d->allocs.push_back(q);
-      d->allocs.push_back(r);
-      d->ckpt = (float *)q;
-      d->ckptRng = (uint32_t *)r;
-      d->ckptCap = nck;
+    }
+    if (steps[k] + 1 > I.tStepsCap || !D.tOff) {
+      const int64_t cap = std::max<int64_t>(steps[k] + 1, 2);
+      if ((rc = talloc(b, &D.tOff, cap)) || (rc = talloc(b, &D.tForced, cap))) return rc;
+      I.tStepsCap = cap;
     }
   }
-  if (steps > d->tStepsCap || !D.tOff) {  // per-step tape offsets and forced counts
-    int64_t *o;
-    int32_t *fz;
-    if ((rc = dalloc(d, &o, (size_t)steps + 1)) || (rc = dalloc(d, &fz, (size_t)std::max(steps, 1)))) return rc;
-    D.tOff = o;
-    D.tForced = fz;
-    d->tStepsCap = steps;
-  }
-  if ((rc = prepare(d, p))) return rc;
-  k_reset<<<256, kDB, 0, d->st>>>(D);
-  // (seed * 2654435761) >>> 0 || 1, the product in double (src/lifdiff.js:221)
-  uint32_t s0 = (uint32_t)std::fmod(std::floor((double)seed * 2654435761.0), 4294967296.0);
-  if (!s0) s0 = 1;
-  DCU(cudaMemcpyAsync(D.rng, &s0, 4, cudaMemcpyHostToDevice, d->st));
-  DCU(cudaMemsetAsync(D.tOff, 0, 8, d->st));
-  DCU(cudaMemsetAsync(D.ovfTop, 0, 4, d->st));
-  const size_t nb = (size_t)N * 4;
-  for (int32_t t = 0; t < steps; t++) {
-    if (record && t % D.K == 0) {
-      float *c = d->ckpt + (int64_t)(t / D.K) * 6 * N;
-      cudaMemcpyAsync(c, D.v, nb, cudaMemcpyDeviceToDevice, d->st);
-      cudaMemcpyAsync(c + N, D.gE, nb, cudaMemcpyDeviceToDevice, d->st);
-      cudaMemcpyAsync(c + 2 * N, D.gI, nb, cudaMemcpyDeviceToDevice, d->st);
-      cudaMemcpyAsync(c + 3 * N, D.adapt, nb, cudaMemcpyDeviceToDevice, d->st);
-      cudaMemcpyAsync(c + 4 * N, D.res, nb, cudaMemcpyDeviceToDevice, d->st);
-      cudaMemcpyAsync(c + 5 * N, D.refr, nb, cudaMemcpyDeviceToDevice, d->st);
-      cudaMemcpyAsync(d->ckptRng + t / D.K, D.rng, 4, cudaMemcpyDeviceToDevice, d->st);
-    }
-    run_step(d, t, 0, -1, nullptr);
+  if ((rc = push_devs(b)) || (rc = prepare(b, p))) return rc;
+  k_reset<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, (float)p->vRest);
+  for (int32_t t = 0; t < maxSteps; t++) {
+    if (record && t % p->checkpoint == 0) k_ckpt<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, t, 1);
+    run_step(b, t, 0, -1);
   }
   DCU(cudaGetLastError());
-  if ((rc = check_err(d, "fb_diff_forward"))) return rc;
-  if (spike_count) DCU(cudaMemcpy(spike_count, D.spikeCount, nb, cudaMemcpyDefault));
-  if (record) {
-    d->recordedSteps = steps;
-    d->recordedK = D.K;
-    d->recordedSeed = seed;
-  } else {
-    d->recordedSteps = 0;
+  if ((rc = check_err(b, "fb_diff_forward"))) return rc;
+  if (spike_counts) {
+    int64_t o = 0;
+    for (int k = 0; k < b->B; k++) {
+      DCU(cudaMemcpyAsync(spike_counts + o, b->in[k].D.spikeCount, (size_t)b->in[k].D.N * 4, cudaMemcpyDefault, b->st));
+      o += b->in[k].D.N;
+    }
+    DCU(cudaStreamSynchronize(b->st));
   }
+  b->recorded = record ? 1 : 0;
+  b->recordedK = p->checkpoint;
+  b->maxSteps = maxSteps;
+  for (int k = 0; k < b->B; k++) b->in[k].recordedSteps = record ? steps[k] : 0;
   return FB_OK;
 }
 
-extern "C" int fb_diff_tape(fb_diff *d, int64_t *offsets, int32_t *idx, float *amp, int64_t cap, int64_t *len) {
-  if (!d || !d->recordedSteps) return dfail(FB_ESTATE, "fb_diff_tape: no recorded forward pass");
-  const int32_t steps = d->recordedSteps;
+extern "C" int fb_diff_batch_tape(fb_diff_batch *b, int32_t inst, int64_t *offsets, int32_t *idx, float *amp,
+                                  int64_t cap, int64_t *len) {
+  if (!b || inst < 0 || inst >= b->B) return dfail(FB_EINVAL, "fb_diff_tape: bad arguments");
+  if (!b->recorded) return dfail(FB_ESTATE, "fb_diff_tape: no recorded forward pass");
+  const Inst &I = b->in[inst];
+  const int32_t steps = I.recordedSteps;
   std::vector<int64_t> off(steps + 1);
-  DCU(cudaMemcpy(off.data(), d->D.tOff, (steps + 1) * 8, cudaMemcpyDeviceToHost));
+  DCU(cudaMemcpy(off.data(), I.D.tOff, (size_t)(steps + 1) * 8, cudaMemcpyDeviceToHost));
   if (len) *len = off[steps];
-  if (offsets) memcpy(offsets, off.data(), (steps + 1) * 8);
+  if (offsets) memcpy(offsets, off.data(), (size_t)(steps + 1) * 8);
   const int64_t n = std::min<int64_t>(cap, off[steps]);
-  if (idx && n > 0) DCU(cudaMemcpy(idx, d->D.tIdx, n * 4, cudaMemcpyDefault));
-  if (amp && n > 0) DCU(cudaMemcpy(amp, d->D.tAmp, n * 4, cudaMemcpyDefault));
+  if (idx && n > 0) DCU(cudaMemcpy(idx, I.D.tIdx, n * 4, cudaMemcpyDefault));
+  if (amp && n > 0) DCU(cudaMemcpy(amp, I.D.tAmp, n * 4, cudaMemcpyDefault));
   return FB_OK;
 }
 
-static int set_readout(fb_diff *d, int32_t nro, const int32_t *ro) {
-  DiffDev &D = d->D;
-  if (!d->roMap) {
-    int rc = dalloc(d, &d->roMap, D.N);
-    if (rc) return rc;
-  }
-  std::vector<int32_t> map(D.N, -1), h(nro);
-  if (nro) DCU(cudaMemcpy(h.data(), ro, nro * 4, cudaMemcpyDefault));
-  for (int32_t c = 0; c < nro; c++) {
-    if (h[c] < 0 || h[c] >= D.N) return dfail(FB_EINVAL, "readout[%d]=%d out of range", c, h[c]);
-    map[h[c]] = c;
-  }
-  DCU(cudaMemcpy(d->roMap, map.data(), D.N * 4, cudaMemcpyHostToDevice));
-  D.nro = nro;
-  return FB_OK;
-}
-
-extern "C" int fb_diff_raster(fb_diff *d, int32_t nro, const int32_t *readout, float *out) {
-  if (!d || nro <= 0 || !readout || !out) return dfail(FB_EINVAL, "fb_diff_raster: bad arguments");
-  if (!d->recordedSteps) return dfail(FB_ESTATE, "fb_diff_raster: no recorded forward pass");
-  int rc = set_readout(d, nro, readout);
-  if (rc) return rc;
-  const int32_t steps = d->recordedSteps;
+extern "C" int fb_diff_batch_raster(fb_diff_batch *b, int32_t inst, int32_t nro, const int32_t *readout, float *out) {
+  if (!b || inst < 0 || inst >= b->B || nro <= 0 || !readout || !out)
+    return dfail(FB_EINVAL, "fb_diff_raster: bad arguments");
+  if (!b->recorded) return dfail(FB_ESTATE, "fb_diff_raster: no recorded forward pass");
+  Inst &I = b->in[inst];
+  int rc = set_readout(b, I, nro, readout);
+  if (rc || (rc = push_devs(b))) return rc;
+  const int32_t steps = I.recordedSteps;
+  if (steps == 0) return FB_OK;
   float *dev = nullptr;
   cudaPointerAttributes at;
   const bool onDev = cudaPointerGetAttributes(&at, out) == cudaSuccess && at.type == cudaMemoryTypeDevice;
   cudaGetLastError();
   if (onDev) dev = out;
   else DCU(cudaMalloc(&dev, (size_t)steps * nro * 4));
-  DCU(cudaMemsetAsync(dev, 0, (size_t)steps * nro * 4, d->st));
-  d->D.roMap = d->roMap;
-  k_raster<<<std::min(steps, 4096), 256, 0, d->st>>>(d->D, steps, dev);
+  DCU(cudaMemsetAsync(dev, 0, (size_t)steps * nro * 4, b->st));
+  k_raster<<<std::min(steps, 4096), 256, 0, b->st>>>(b->dDevs + inst, steps, dev);
   DCU(cudaGetLastError());
-  DCU(cudaStreamSynchronize(d->st));
+  DCU(cudaStreamSynchronize(b->st));
   if (!onDev) {
     DCU(cudaMemcpy(out, dev, (size_t)steps * nro * 4, cudaMemcpyDeviceToHost));
     cudaFree(dev);
@@ -1050,162 +1342,193 @@ extern "C" int fb_diff_raster(fb_diff *d, int32_t nro, const int32_t *readout, f
   return FB_OK;
 }
 
-extern "C" int fb_diff_backward(fb_diff *d, const float *dL, int32_t nro, const int32_t *readout,
-                                int32_t truncate, int32_t loss_from, fb_diff_grads *g) {
-  if (!d || !dL || !g) return dfail(FB_EINVAL, "fb_diff_backward: null argument");
-  if (!d->recordedSteps) return dfail(FB_ESTATE, "fb_diff_backward: no recorded forward pass (record=1)");
-  DiffDev &D = d->D;
-  const int32_t steps = d->recordedSteps, K = d->recordedK;
-  const int64_t N = D.N, E = D.E;
-  int rc = fill_params(d, &d->lastP);
+extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, const int32_t *nro,
+                                      const int32_t *const *readout, int32_t truncate, int32_t loss_from,
+                                      fb_diff_grads *g) {
+  if (!b || !dL || !g) return dfail(FB_EINVAL, "fb_diff_backward: null argument");
+  if (!b->recorded) return dfail(FB_ESTATE, "fb_diff_backward: no recorded forward pass (record=1)");
+  const int32_t K = b->recordedK;
+  int rc = fill_params(b, &b->lastP);
   if (rc) return rc;
-  // the loss gradient: flat over N, or per step over a readout set
-  const int64_t dLn = nro > 0 ? (int64_t)steps * nro : N;
-  if (dLn > d->dLcap) {
-    float *q;
-    if ((rc = dalloc(d, &q, dLn))) return rc;
-    d->dLbuf = q;
-    d->dLcap = dLn;
+  for (int k = 0; k < b->B; k++) {
+    Inst &I = b->in[k];
+    DiffDev &D = I.D;
+    const int64_t N = D.N, steps = I.recordedSteps;
+    const int32_t m = nro ? nro[k] : 0;
+    if (!dL[k]) return dfail(FB_EINVAL, "fb_diff_backward: dL[%d] missing", k);
+    // the loss gradient: flat over N, or per step over a readout set
+    const int64_t dLn = m > 0 ? std::max<int64_t>(steps * m, 1) : N;
+    if (dLn > I.dLcap) {
+      if ((rc = talloc(b, &I.dLbuf, dLn))) return rc;
+      I.dLcap = dLn;
+    }
+    if (m > 0 ? steps * m > 0 : true) DCU(cudaMemcpyAsync(I.dLbuf, dL[k], (m > 0 ? steps * m : N) * 4, cudaMemcpyDefault, b->st));
+    D.dL = I.dLbuf;
+    if (m > 0) {
+      if (!readout || !readout[k]) return dfail(FB_EINVAL, "fb_diff_backward: readout indices missing");
+      if ((rc = set_readout(b, I, m, readout[k]))) return rc;
+    } else {
+      D.roMap = nullptr;
+    }
+    // arena and per-arrival res for one segment
+    std::vector<int64_t> off(steps + 1);
+    DCU(cudaMemcpy(off.data(), D.tOff, (size_t)(steps + 1) * 8, cudaMemcpyDeviceToHost));
+    int64_t maxArr = 1;
+    for (int64_t t = 0; t < steps; t++) {
+      const int64_t e = t - (D.nslots - 1);
+      if (e >= 0) maxArr = std::max<int64_t>(maxArr, off[e + 1] - off[e]);
+    }
+    if (K > I.arenaRows) {
+      float *a;
+      uint8_t *md;
+      if ((rc = talloc(b, &a, (size_t)5 * K * N)) || (rc = talloc(b, &md, (size_t)K * N))) return rc;
+      D.aV = a;
+      D.aGE = a + (size_t)K * N;
+      D.aGI = a + (size_t)2 * K * N;
+      D.aAd = a + (size_t)3 * K * N;
+      D.aSp = a + (size_t)4 * K * N;
+      D.aMode = md;
+      I.arenaRows = K;
+    }
+    if (maxArr * K > I.resAtCap) {
+      if ((rc = talloc(b, &D.resAt, maxArr * K))) return rc;
+      I.resAtCap = maxArr * K;
+    }
+    D.maxArr = maxArr;
+    if (!D.lsRing) {
+      if ((rc = talloc(b, &D.lsRing, (size_t)D.nslots * N))) return rc;
+    }
+    D.steps = (int32_t)steps;
   }
-  DCU(cudaMemcpyAsync(d->dLbuf, dL, dLn * 4, cudaMemcpyDefault, d->st));
-  D.dL = d->dLbuf;
-  if (nro > 0) {
-    if (!readout) return dfail(FB_EINVAL, "fb_diff_backward: readout indices missing");
-    if ((rc = set_readout(d, nro, readout))) return rc;
-    D.roMap = d->roMap;
-  } else {
-    D.roMap = nullptr;
-  }
-  // arena and per-arrival res for one segment
-  std::vector<int64_t> off(steps + 1);
-  DCU(cudaMemcpy(off.data(), D.tOff, (steps + 1) * 8, cudaMemcpyDeviceToHost));
-  int64_t maxArr = 1;
-  for (int32_t t = 0; t < steps; t++) {
-    const int e = t - (D.nslots - 1);
-    if (e >= 0) maxArr = std::max<int64_t>(maxArr, off[e + 1] - off[e]);
-  }
-  if (K > d->arenaK) {
-    float *a;
-    uint8_t *m;
-    if ((rc = dalloc(d, &a, (size_t)5 * K * N)) || (rc = dalloc(d, &m, (size_t)K * N))) return rc;
-    d->arena = a;
-    d->aMode = m;
-    d->arenaK = K;
-  }
-  if (maxArr * K > d->resAtCap) {
-    float *r;
-    if ((rc = dalloc(d, &r, maxArr * K))) return rc;
-    d->resAt = r;
-    d->resAtCap = maxArr * K;
-  }
-  D.aV = d->arena;
-  D.aGE = d->arena + (size_t)K * N;
-  D.aGI = d->arena + (size_t)2 * K * N;
-  D.aAd = d->arena + (size_t)3 * K * N;
-  D.aSp = d->arena + (size_t)4 * K * N;
-  D.aMode = d->aMode;
-  D.resAt = d->resAt;
-  D.maxArr = maxArr;
-  // zero the adjoint state and accumulators
-  for (float *p : {D.lv, D.lgE, D.lgI, D.lad, D.lres}) DCU(cudaMemsetAsync(p, 0, N * 4, d->st));
-  for (double *p : {D.accA, D.accV, D.accKc, D.accLa, D.accEI, D.accW, D.accD, D.gLog, D.gBias})
-    DCU(cudaMemsetAsync(p, 0, N * 8, d->st));
-  DCU(cudaMemsetAsync(D.gEdge, 0, std::max<int64_t>(E, 1) * 8, d->st));
-  float *lsRing;
-  if (!D.lsRing) {
-    if ((rc = dalloc(d, &lsRing, (size_t)D.nslots * N))) return rc;
-    D.lsRing = lsRing;
-  }
-  DCU(cudaMemsetAsync(D.lsRing, 0, (size_t)D.nslots * N * 4, d->st));
-  if ((rc = prepare(d, &d->lastP))) return rc;
-  const size_t nb = (size_t)N * 4;
+  if ((rc = push_devs(b))) return rc;
+  const dim3 ng = neuron_grid(b);
+  k_zero_adjoint<<<ng, kDB, 0, b->st>>>(b->dDevs);
+  for (int k = 0; k < b->B; k++) DCU(cudaMemsetAsync(b->in[k].D.nonfinite, 0, 4, b->st));
+  if ((rc = prepare(b, &b->lastP))) return rc;
+  const int32_t steps = b->maxSteps;
   const int nseg = (steps + K - 1) / K;
-  for (int b = nseg - 1; b >= 0; b--) {
-    const int32_t from = b * K, to = std::min(steps, from + K);
+  for (int sg = nseg - 1; sg >= 0; sg--) {
+    const int32_t from = sg * K, to = std::min(steps, from + K);
     // replay the segment from its checkpoint (src/lifdiff.js:390-464)
-    const float *c = d->ckpt + (int64_t)b * 6 * N;
-    cudaMemcpyAsync(D.v, c, nb, cudaMemcpyDeviceToDevice, d->st);
-    cudaMemcpyAsync(D.gE, c + N, nb, cudaMemcpyDeviceToDevice, d->st);
-    cudaMemcpyAsync(D.gI, c + 2 * N, nb, cudaMemcpyDeviceToDevice, d->st);
-    cudaMemcpyAsync(D.adapt, c + 3 * N, nb, cudaMemcpyDeviceToDevice, d->st);
-    cudaMemcpyAsync(D.res, c + 4 * N, nb, cudaMemcpyDeviceToDevice, d->st);
-    cudaMemcpyAsync(D.refr, c + 5 * N, nb, cudaMemcpyDeviceToDevice, d->st);
-    for (int32_t t = from; t < to; t++) run_step(d, t, 1, t - from, D.resAt + (int64_t)(t - from) * maxArr);
+    k_ckpt<<<ng, kDB, 0, b->st>>>(b->dDevs, from, 0);
+    for (int32_t t = from; t < to; t++) run_step(b, t, 1, t - from);
     // reverse sweep of the segment (src/lifdiff.js:540-667)
     for (int32_t t = to - 1; t >= from; t--) {
-      if (truncate > 0 && (t + 1) % truncate == 0) {
-        for (float *p : {D.lv, D.lgE, D.lgI, D.lad, D.lres}) cudaMemsetAsync(p, 0, nb, d->st);
-        cudaMemsetAsync(D.lsRing, 0, (size_t)D.nslots * nb, d->st);
-      }
-      reverse_step(d, t, t - from, t >= loss_from ? 1 : 0, D.resAt + (int64_t)(t - from) * maxArr);
+      if (truncate > 0) k_truncate<<<ng, kDB, 0, b->st>>>(b->dDevs, t, truncate);
+      reverse_step(b, t, t - from, t >= loss_from ? 1 : 0);
     }
   }
   DCU(cudaGetLastError());
-  if ((rc = check_err(d, "fb_diff_backward"))) return rc;
-  // fixed-order reductions of the scalar accumulators
-  const double *srcs[7] = {D.accW, D.accEI, D.accV, D.accKc, D.accLa, D.accA, D.accD};
-  const double **dsrc;
-  DCU(cudaMalloc(&dsrc, sizeof srcs));
-  DCU(cudaMemcpy(dsrc, srcs, sizeof srcs, cudaMemcpyHostToDevice));
-  k_reduce<<<256, kDB, 0, d->st>>>(dsrc, 7, D.N, d->partial);
-  std::vector<double> part(256 * 8);
-  DCU(cudaMemcpyAsync(part.data(), d->partial, part.size() * 8, cudaMemcpyDeviceToHost, d->st));
-  DCU(cudaStreamSynchronize(d->st));
-  cudaFree(dsrc);
-  double s[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int blk = 0; blk < 256; blk++)
-    for (int k = 0; k < 7; k++) s[k] += part[blk * 8 + k];
-  // per-edge gradient -> gInScale per target and the inhibitory-gain term, on the host in
-  // edge order (the reference accumulates them per arrival, src/lifdiff.js:650-655)
-  std::vector<double> gEdge(E), gIS(N, 0.0);
-  std::vector<float> counts(E), eg(D.edgeGain ? E : 0), sign(N), inS(N), sizeLog(N), lg(N), outs(N);
-  std::vector<uint32_t> ip(N + 1), ix(E);
-  std::vector<uint8_t> gate(E);
-  DCU(cudaMemcpy(gEdge.data(), D.gEdge, E * 8, cudaMemcpyDeviceToHost));
-  DCU(cudaMemcpy(counts.data(), D.counts, E * 4, cudaMemcpyDeviceToHost));
-  if (D.edgeGain) DCU(cudaMemcpy(eg.data(), D.edgeGain, E * 4, cudaMemcpyDeviceToHost));
-  DCU(cudaMemcpy(sign.data(), D.sign, N * 4, cudaMemcpyDeviceToHost));
-  DCU(cudaMemcpy(inS.data(), D.inScale, N * 4, cudaMemcpyDeviceToHost));
-  DCU(cudaMemcpy(sizeLog.data(), d->sizeLog, N * 4, cudaMemcpyDeviceToHost));
-  DCU(cudaMemcpy(ip.data(), D.indptr, (N + 1) * 4, cudaMemcpyDeviceToHost));
-  DCU(cudaMemcpy(ix.data(), D.indices, E * 4, cudaMemcpyDeviceToHost));
-  DCU(cudaMemcpy(gate.data(), D.gate, E, cudaMemcpyDeviceToHost));
-  double gInh = 0;
-  const fb_diff_params &P = d->lastP;
-  for (int64_t j0 = 0; j0 < N; j0++) {
-    const bool inh = sign[j0] < 0;  // eff's sign follows the presynaptic sign (wSyn, gains > 0)
-    for (uint32_t j = ip[j0]; j < ip[j0 + 1]; j++) {
-      if (!gate[j]) continue;
-      const double cw = (double)counts[j] * (D.edgeGain ? (double)eg[j] : 1.0);
-      gIS[ix[j]] += cw * (inh ? P.inhGain : 1.0) * gEdge[j];
-      if (inh) gInh += cw * (double)inS[ix[j]] * gEdge[j];
+  if ((rc = check_err(b, "fb_diff_backward"))) return rc;
+  // fixed-order reductions of the scalar terms
+  const fb_diff_params &P = b->lastP;
+  k_reduce<<<dim3(kRB, b->B), kDB, 0, b->st>>>(b->dDevs, P.inhGain, P.sizeAlpha, P.boostCap, P.maxSizeScale,
+                                                b->partial);
+  k_finalize<<<ng, kDB, 0, b->st>>>(b->dDevs);
+  DCU(cudaGetLastError());
+  std::vector<double> part((size_t)b->B * kRB * kNSums);
+  std::vector<int32_t> nonfin(b->B);
+  DCU(cudaMemcpyAsync(part.data(), b->partial, part.size() * 8, cudaMemcpyDeviceToHost, b->st));
+  for (int k = 0; k < b->B; k++)
+    DCU(cudaMemcpyAsync(&nonfin[k], b->in[k].D.nonfinite, 4, cudaMemcpyDeviceToHost, b->st));
+  DCU(cudaStreamSynchronize(b->st));
+  for (int k = 0; k < b->B; k++) {
+    const DiffDev &D = b->in[k].D;
+    double s[kNSums] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int blk = 0; blk < kRB; blk++)
+      for (int q = 0; q < kNSums; q++) s[q] += part[((size_t)k * kRB + blk) * kNSums + q];
+    // src/lifdiff.js:75 order: wSyn sizeAlpha inhGain eInh vThresh kcThreshold laminaBias adaptInc depU
+    double vals[9] = {s[0], s[7], s[8], s[1], s[2], s[3], s[4], s[5], s[6]};
+    fb_diff_grads &G = g[k];
+    G.clamped_params = 0;
+    for (int q = 0; q < 9; q++) {
+      if (!std::isfinite(vals[q])) { vals[q] = 0; G.clamped_params++; }
+      G.params[q] = vals[q];
     }
+    G.clamped_log_gain = nonfin[k];
+    if (G.log_gain) DCU(cudaMemcpyAsync(G.log_gain, D.gLogF, (size_t)D.N * 4, cudaMemcpyDefault, b->st));
+    if (G.out_scale) DCU(cudaMemcpyAsync(G.out_scale, D.gOut, (size_t)D.N * 8, cudaMemcpyDefault, b->st));
+    if (G.bias) DCU(cudaMemcpyAsync(G.bias, D.gBias, (size_t)D.N * 8, cudaMemcpyDefault, b->st));
+    if (G.edge && D.E) DCU(cudaMemcpyAsync(G.edge, D.gEdge, (size_t)D.E * 8, cudaMemcpyDefault, b->st));
   }
-  double gSize = 0;
-  for (int64_t i = 0; i < N; i++) {
-    const double raw = std::exp(-P.sizeAlpha * (double)sizeLog[i]);
-    if (raw < P.boostCap && raw > 1 / P.maxSizeScale) gSize += gIS[i] * (-(double)sizeLog[i]) * raw;
-  }
-  // src/lifdiff.js:75 order: wSyn sizeAlpha inhGain eInh vThresh kcThreshold laminaBias adaptInc depU
-  double vals[9] = {s[0], gSize, gInh, s[1], s[2], s[3], s[4], s[5], s[6]};
-  g->clamped_params = g->clamped_log_gain = 0;
-  for (int k = 0; k < 9; k++) {
-    if (!std::isfinite(vals[k])) { vals[k] = 0; g->clamped_params++; }
-    g->params[k] = vals[k];
-  }
-  std::vector<double> glog(N);
-  DCU(cudaMemcpy(glog.data(), D.gLog, N * 8, cudaMemcpyDeviceToHost));
-  if (g->log_gain || g->out_scale) {
-    std::vector<float> os(N, 1.f);
-    if (D.outScale) DCU(cudaMemcpy(os.data(), D.outScale, N * 4, cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < N; i++) {
-      float x = (float)glog[i];
-      if (!std::isfinite(x)) { x = 0; g->clamped_log_gain++; }
-      if (g->log_gain) g->log_gain[i] = x;
-      if (g->out_scale) g->out_scale[i] = (double)x / (double)os[i];
-    }
-  }
-  if (g->edge) memcpy(g->edge, gEdge.data(), E * 8);
-  if (g->bias) DCU(cudaMemcpy(g->bias, D.gBias, N * 8, cudaMemcpyDefault));
+  DCU(cudaStreamSynchronize(b->st));
   return FB_OK;
+}
+
+extern "C" int fb_diff_batch_edge_sum(fb_diff_batch *b, int32_t n, const int32_t *insts, double *out) {
+  if (!b || n <= 0 || !insts || !out) return dfail(FB_EINVAL, "fb_diff_batch_edge_sum: bad arguments");
+  std::vector<const double *> ptrs(n);
+  int64_t E = -1;
+  for (int k = 0; k < n; k++) {
+    if (insts[k] < 0 || insts[k] >= b->B) return dfail(FB_EINVAL, "fb_diff_batch_edge_sum: instance %d", insts[k]);
+    const DiffDev &D = b->in[insts[k]].D;
+    if (E >= 0 && D.E != E) return dfail(FB_EINVAL, "fb_diff_batch_edge_sum: instances differ in edge count");
+    E = D.E;
+    ptrs[k] = D.gEdge;
+  }
+  const double **dp;
+  DCU(cudaMalloc(&dp, n * sizeof(double *)));
+  cudaMemcpy(dp, ptrs.data(), n * sizeof(double *), cudaMemcpyHostToDevice);
+  cudaPointerAttributes at;
+  const bool onDev = cudaPointerGetAttributes(&at, out) == cudaSuccess && at.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  double *dev = out;
+  if (!onDev && cudaMalloc(&dev, std::max<int64_t>(E, 1) * 8) != cudaSuccess) {
+    cudaFree(dp);
+    return dfail(FB_ENOMEM, "fb_diff_batch_edge_sum: %lld edges", (long long)E);
+  }
+  k_edge_sum<<<1024, kDB, 0, b->st>>>(dp, n, E, dev);
+  cudaError_t e = cudaStreamSynchronize(b->st);
+  if (e == cudaSuccess && !onDev) e = cudaMemcpy(out, dev, E * 8, cudaMemcpyDeviceToHost);
+  if (!onDev) cudaFree(dev);
+  cudaFree(dp);
+  if (e != cudaSuccess) return dfail(FB_ECUDA, "fb_diff_batch_edge_sum: %s", cudaGetErrorString(e));
+  return FB_OK;
+}
+
+// ---- the single-network API: a batch of one -------------------------------------------------
+
+extern "C" int fb_diff_create(const fb_diff_net *net, int64_t tape_cap, fb_diff **out) {
+  if (!net || !out) return dfail(FB_EINVAL, "fb_diff_create: null argument");
+  *out = nullptr;
+  fb_diff_batch *b = nullptr;
+  int rc = fb_diff_batch_create(net, 1, tape_cap, &b);
+  if (rc) return rc;
+  *out = new fb_diff;
+  (*out)->b = b;
+  return FB_OK;
+}
+
+extern "C" int fb_diff_destroy(fb_diff *d) {
+  if (!d) return FB_OK;
+  fb_diff_batch_destroy(d->b);
+  delete d;
+  return FB_OK;
+}
+
+extern "C" int fb_diff_set(fb_diff *d, int32_t field, const float *values) {
+  if (!d) return dfail(FB_EINVAL, "fb_diff_set: null argument");
+  return fb_diff_batch_set(d->b, 0, field, values);
+}
+
+extern "C" int fb_diff_forward(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed, int32_t record,
+                               float *spike_count) {
+  if (!d || !p || steps < 0) return dfail(FB_EINVAL, "fb_diff_forward: bad arguments");
+  return fb_diff_batch_forward(d->b, p, &steps, &seed, record, spike_count);
+}
+
+extern "C" int fb_diff_tape(fb_diff *d, int64_t *offsets, int32_t *idx, float *amp, int64_t cap, int64_t *len) {
+  if (!d) return dfail(FB_EINVAL, "fb_diff_tape: null argument");
+  return fb_diff_batch_tape(d->b, 0, offsets, idx, amp, cap, len);
+}
+
+extern "C" int fb_diff_raster(fb_diff *d, int32_t nro, const int32_t *readout, float *out) {
+  if (!d) return dfail(FB_EINVAL, "fb_diff_raster: null argument");
+  return fb_diff_batch_raster(d->b, 0, nro, readout, out);
+}
+
+extern "C" int fb_diff_backward(fb_diff *d, const float *dL, int32_t nro, const int32_t *readout, int32_t truncate,
+                                int32_t loss_from, fb_diff_grads *g) {
+  if (!d || !dL || !g) return dfail(FB_EINVAL, "fb_diff_backward: null argument");
+  return fb_diff_batch_backward(d->b, &dL, &nro, &readout, truncate, loss_from, g);
 }

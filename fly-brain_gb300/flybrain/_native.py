@@ -108,6 +108,14 @@ SIGNATURES = {
     "fb_diff_tape": (C.c_int, [P, P, P, P, I64, PI64]),
     "fb_diff_raster": (C.c_int, [P, I32, P, P]),
     "fb_diff_backward": (C.c_int, [P, P, I32, P, I32, I32, C.POINTER(FbDiffGrads)]),
+    "fb_diff_batch_create": (C.c_int, [C.POINTER(FbDiffNet), I32, I64, C.POINTER(P)]),
+    "fb_diff_batch_destroy": (C.c_int, [P]),
+    "fb_diff_batch_set": (C.c_int, [P, I32, I32, P]),
+    "fb_diff_batch_forward": (C.c_int, [P, C.POINTER(FbDiffParams), P, P, I32, P]),
+    "fb_diff_batch_tape": (C.c_int, [P, I32, P, P, P, I64, PI64]),
+    "fb_diff_batch_raster": (C.c_int, [P, I32, I32, P, P]),
+    "fb_diff_batch_backward": (C.c_int, [P, P, P, P, I32, I32, C.POINTER(FbDiffGrads)]),
+    "fb_diff_batch_edge_sum": (C.c_int, [P, I32, P, P]),
 }
 
 

@@ -21,7 +21,8 @@ class DiffContext:
 
     def __init__(self, net: DiffNet, cell_type, readout, steps: int, seed: int = 1, **over):
         self.net = net
-        self.cell_type = torch.as_tensor(np.asarray(cell_type, np.int64), device="cuda")
+        self.cell_type_np = np.asarray(cell_type, np.int64)
+        self.cell_type = torch.as_tensor(self.cell_type_np, device="cuda")
         self.readout = np.ascontiguousarray(readout, np.int32)
         self.steps = int(steps)
         self.seed = int(seed)
@@ -65,12 +66,14 @@ class LIFDiffFunction(torch.autograd.Function):
         dctx = ctx.dctx
         gr = g_raster.detach().float().contiguous()
         torch.cuda.synchronize()
-        g = dctx.net.backward(gr, readout=dctx.readout)
         dev = g_raster.device
-        g_edge = torch.as_tensor(g["edge"], device=dev) * dctx.dW_dgain
-        g_bias = torch.as_tensor(g["bias"], device=dev)
-        g_type = torch.zeros(ctx.ntypes, dtype=torch.float64, device=dev)
-        g_type.index_add_(0, dctx.cell_type, torch.as_tensor(g["outScale"], device=dev))
+        g = dctx.net.backward(gr, readout=dctx.readout, device=dev)
+        g_edge = g["edge"] * dctx.dW_dgain
+        g_bias = g["bias"]
+        # per-type sums in neuron order on the host (a deterministic order; device scatter-adds
+        # are not)
+        g_type = torch.as_tensor(np.bincount(dctx.cell_type_np, weights=g["outScale"].cpu().numpy(),
+                                             minlength=ctx.ntypes), device=dev)
         return g_edge.float(), g_bias.float(), g_type.float(), None
 
 

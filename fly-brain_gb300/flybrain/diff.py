@@ -44,13 +44,80 @@ def make_params(p: dict) -> nat.FbDiffParams:
     return q
 
 
+class _Desc:
+    """Builds fb_diff_net records; the same array object given for the same field of several
+    networks yields the same pointer, so the library uploads it once."""
+
+    def __init__(self):
+        self.keep = []
+        self._cache = {}
+
+    def arr(self, x, dt):
+        if x is None:
+            return None
+        key = (id(x), np.dtype(dt).str)
+        hit = self._cache.get(key)
+        if hit is not None and hit[0] is x:
+            return hit[1].ctypes.data
+        a = np.ascontiguousarray(x, dt)
+        self.keep += [a, x]
+        self._cache[key] = (x, a)
+        return a.ctypes.data
+
+    def net(self, n: "DiffNet", out: nat.FbDiffNet):
+        out.N, out.E = n.N, n.E
+        out.indptr, out.indices = self.arr(n.indptr, np.uint32), self.arr(n.indices, np.uint32)
+        out.counts, out.sign = self.arr(n.counts, np.float32), self.arr(n.sign, np.float32)
+        for k in _ARRAYS_N + ("edge_gain",):
+            setattr(out, k, self.arr(n.arrays[k], np.float32))
+        for k in _MASKS:
+            setattr(out, k, self.arr(n.arrays[k], np.uint8))
+        driven = np.array(list(n.drivenSet), np.int32)
+        out.nDriven = int(driven.shape[0])
+        out.drive = self.arr(n.drive.copy(), np.float32)
+        out.driven = self.arr(driven if driven.shape[0] else np.zeros(1, np.int32), np.int32)
+
+
+def _grads(N, E, edge=True, device=None):
+    """An FbDiffGrads with its output arrays (numpy, or torch tensors on `device`)."""
+    g = nat.FbDiffGrads()
+    if device is None:
+        lg, gb, go = np.zeros(N, np.float32), np.zeros(N, np.float64), np.zeros(N, np.float64)
+        ge = np.zeros(E, np.float64) if edge else None
+        ptr = lambda a: a.ctypes.data  # noqa: E731
+    else:
+        import torch
+        lg = torch.zeros(N, dtype=torch.float32, device=device)
+        gb, go = (torch.zeros(N, dtype=torch.float64, device=device) for _ in range(2))
+        ge = torch.zeros(E, dtype=torch.float64, device=device) if edge else None
+        ptr = lambda a: a.data_ptr()  # noqa: E731
+    g.log_gain, g.bias, g.out_scale = ptr(lg), ptr(gb), ptr(go)
+    g.edge = None if ge is None else ptr(ge)
+    return g, dict(logGain=lg, edge=ge, bias=gb, outScale=go)
+
+
+def _grad_dict(g, arrays, truncate):
+    return dict(params=dict(zip(DIFF_PARAMS, list(g.params))),
+                clamped=dict(params=g.clamped_params, logGain=g.clamped_log_gain),
+                truncate=truncate, **arrays)
+
+
+def _dl_ptr(x):
+    if x is None:
+        return None, None
+    if hasattr(x, "data_ptr"):
+        return C.c_void_p(x.data_ptr()).value, x
+    a = np.ascontiguousarray(x, np.float32)
+    return a.ctypes.data, a
+
+
 class DiffNet:
     """LIFDiff on the device. data: {N, indptr, indices, weights (raw counts), nt} as the
     reference takes it (or sign= for preSign); opts: model parameters and per-neuron structure
     (sizeLog, thrMask, biasMask, logGain, outScale, thrOffset, sensoryMask, edgeGain, inScale,
     surrogateBeta as an array, bias)."""
 
-    def __init__(self, data: dict, opts: dict | None = None, tape_cap: int = 0):
+    def __init__(self, data: dict, opts: dict | None = None, tape_cap: int = 0, _defer: bool = False):
         self.L = nat.load()
         opts = dict(opts or {})
         self.N = int(data["N"])
@@ -77,32 +144,15 @@ class DiffNet:
             edge_gain=opts.get("edgeGain"))
         self.drive = np.zeros(self.N, np.float32)
         self.drivenSet: dict[int, None] = {}
-        self._keep = []
         self.h = None
-        self._create(tape_cap)
+        self._tape_cap = tape_cap
+        if not _defer:
+            self._create(tape_cap)
 
     def _create(self, tape_cap):
+        desc = _Desc()
         net = nat.FbDiffNet()
-        net.N, net.E = self.N, self.E
-        keep = []
-
-        def arr(x, dt):
-            if x is None:
-                return None
-            a = np.ascontiguousarray(x, dt)
-            keep.append(a)
-            return a.ctypes.data
-
-        net.indptr, net.indices = arr(self.indptr, np.uint32), arr(self.indices, np.uint32)
-        net.counts, net.sign = arr(self.counts, np.float32), arr(self.sign, np.float32)
-        for k in _ARRAYS_N + ("edge_gain",):
-            setattr(net, k, arr(self.arrays[k], np.float32))
-        for k in _MASKS:
-            setattr(net, k, arr(self.arrays[k], np.uint8))
-        driven = np.array(list(self.drivenSet), np.int32)
-        net.nDriven = int(driven.shape[0])
-        net.drive = arr(self.drive, np.float32)
-        net.driven = arr(driven if driven.shape[0] else np.zeros(1, np.int32), np.int32)
+        desc.net(self, net)
         h = C.c_void_p()
         nat.check(self.L.fb_diff_create(C.byref(net), int(tape_cap), C.byref(h)))
         if self.h:
@@ -178,25 +228,125 @@ class DiffNet:
         nat.check(self.L.fb_diff_raster(self.h, ro.shape[0], ro.ctypes.data, C.c_void_p(out.data_ptr())))
         return out
 
-    def backward(self, dLdSpike, truncate: int = 0, lossFrom: int = 0, readout=None, edge: bool = True):
+    def backward(self, dLdSpike, truncate: int = 0, lossFrom: int = 0, readout=None, edge: bool = True,
+                 device=None):
         """src/lifdiff.js:494: dLdSpike f32[N] (every scored step), or f32[steps][len(readout)]
-        with readout indices. Returns {params, logGain, clamped, edge, bias, outScale}."""
-        g = nat.FbDiffGrads()
-        lg = np.zeros(self.N, np.float32)
-        ge = np.zeros(self.E, np.float64) if edge else None
-        gb = np.zeros(self.N, np.float64)
-        go = np.zeros(self.N, np.float64)
-        g.log_gain, g.bias, g.out_scale = lg.ctypes.data, gb.ctypes.data, go.ctypes.data
-        g.edge = None if ge is None else ge.ctypes.data
-        if hasattr(dLdSpike, "data_ptr"):
-            dptr = C.c_void_p(dLdSpike.data_ptr())
-        else:
-            dl = np.ascontiguousarray(dLdSpike, np.float32)
-            dptr = dl.ctypes.data
+        with readout indices. Returns {params, logGain, clamped, edge, bias, outScale} (numpy, or
+        torch tensors on `device`)."""
+        g, arrays = _grads(self.N, self.E, edge, device)
+        dptr, _keep = _dl_ptr(dLdSpike)
         ro = None if readout is None else np.ascontiguousarray(readout, np.int32)
         nat.check(self.L.fb_diff_backward(self.h, dptr, 0 if ro is None else ro.shape[0],
                                           None if ro is None else ro.ctypes.data, int(truncate),
                                           int(lossFrom), C.byref(g)))
-        return dict(params=dict(zip(DIFF_PARAMS, list(g.params))), logGain=lg,
-                    clamped=dict(params=g.clamped_params, logGain=g.clamped_log_gain),
-                    edge=ge, bias=gb, outScale=go, truncate=truncate)
+        return _grad_dict(g, arrays, truncate)
+
+
+class DiffBatch:
+    """B independent differentiable brains advanced together by one set of launches
+    (fb_diff_batch_*): each member is a DiffNet built with DiffNet(..., _defer=True) (its graph,
+    per-neuron arrays and driven set); the model parameters are the batch's. Arrays that are the
+    same object in several members are uploaded once and shared."""
+
+    def __init__(self, members, params: dict | None = None, tape_cap: int = 0):
+        self.L = nat.load()
+        self.members = list(members)
+        self.B = len(self.members)
+        self.p = dict(DIFF_DEFAULTS, **(params or {}))
+        self.N = [m.N for m in self.members]
+        self.E = [m.E for m in self.members]
+        desc = _Desc()
+        nets = (nat.FbDiffNet * self.B)()
+        for b, m in enumerate(self.members):
+            desc.net(m, nets[b])
+        h = C.c_void_p()
+        nat.check(self.L.fb_diff_batch_create(nets, self.B, int(tape_cap), C.byref(h)))
+        self.h = h
+        self._steps = [0] * self.B
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.L.fb_diff_batch_destroy(h)
+            self.h = None
+
+    def set_array(self, inst: int, name: str, values):
+        key = {"logGain": "log_gain", "outScale": "out_scale", "thrOffset": "thr_offset",
+               "bias": "bias", "edgeGain": "edge_gain", "drive": "drive"}.get(name, name)
+        if hasattr(values, "data_ptr"):
+            ptr = C.c_void_p(values.data_ptr())
+        else:
+            v = np.ascontiguousarray(values, np.float32)
+            ptr = v.ctypes.data
+        nat.check(self.L.fb_diff_batch_set(self.h, int(inst), _FIELDS[key], ptr))
+
+    def forward(self, steps, seeds=1, record: bool = True, counts: bool = True, **over):
+        """Every member from reset for steps[b] steps with seeds[b]; returns the members' spike
+        counts (or None with counts=False)."""
+        st = np.broadcast_to(np.asarray(steps, np.int32), (self.B,)).copy()
+        sd = np.broadcast_to(np.asarray(seeds, np.uint32), (self.B,)).copy()
+        sc = np.zeros(sum(self.N), np.float32) if counts else None
+        nat.check(self.L.fb_diff_batch_forward(self.h, C.byref(make_params(dict(self.p, **over))),
+                                               st.ctypes.data, sd.ctypes.data, 1 if record else 0,
+                                               None if sc is None else sc.ctypes.data))
+        self._steps = st.tolist()
+        if sc is None:
+            return None
+        return np.split(sc, np.cumsum(self.N)[:-1])
+
+    def tape(self, inst: int):
+        steps = self._steps[inst]
+        off = np.zeros(steps + 1, np.int64)
+        n = C.c_int64()
+        nat.check(self.L.fb_diff_batch_tape(self.h, int(inst), off.ctypes.data, None, None, 0, C.byref(n)))
+        idx = np.zeros(max(1, n.value), np.int32)
+        amp = np.zeros(max(1, n.value), np.float32)
+        nat.check(self.L.fb_diff_batch_tape(self.h, int(inst), off.ctypes.data, idx.ctypes.data, amp.ctypes.data,
+                                            n.value, C.byref(n)))
+        return off, idx[: n.value], amp[: n.value]
+
+    def raster(self, inst: int, readout, out=None):
+        ro = np.ascontiguousarray(readout, np.int32)
+        if out is None:
+            out = np.zeros((self._steps[inst], ro.shape[0]), np.float32)
+            nat.check(self.L.fb_diff_batch_raster(self.h, int(inst), ro.shape[0], ro.ctypes.data, out.ctypes.data))
+            return out
+        nat.check(self.L.fb_diff_batch_raster(self.h, int(inst), ro.shape[0], ro.ctypes.data,
+                                              C.c_void_p(out.data_ptr())))
+        return out
+
+    def backward(self, dLs, readouts=None, truncate: int = 0, lossFrom: int = 0, edge: bool = True, device=None):
+        """Per member: dLs[b] as DiffNet.backward's dLdSpike (readouts[b] its readout set or None).
+        Returns one gradient dict per member."""
+        B = self.B
+        ptrs = (C.c_void_p * B)()
+        nro = np.zeros(B, np.int32)
+        ros = (C.c_void_p * B)()
+        keep = []
+        for b in range(B):
+            ptrs[b], k = _dl_ptr(dLs[b])
+            keep.append(k)
+            ro = None if readouts is None or readouts[b] is None else np.ascontiguousarray(readouts[b], np.int32)
+            if ro is not None:
+                keep.append(ro)
+                nro[b] = ro.shape[0]
+                ros[b] = ro.ctypes.data
+        gs = (nat.FbDiffGrads * B)()
+        arrays = []
+        for b in range(B):
+            g, a = _grads(self.N[b], self.E[b], edge, device)
+            gs[b] = g
+            arrays.append(a)
+        nat.check(self.L.fb_diff_batch_backward(self.h, ptrs, nro.ctypes.data, ros, int(truncate), int(lossFrom), gs))
+        return [_grad_dict(gs[b], arrays[b], truncate) for b in range(B)]
+
+    def edge_sum(self, insts=None, out=None):
+        """Per-edge gradients of the listed members (all by default) summed in list order."""
+        ii = np.ascontiguousarray(range(self.B) if insts is None else insts, np.int32)
+        E = self.E[int(ii[0])]
+        if out is None:
+            out = np.zeros(E, np.float64)
+            nat.check(self.L.fb_diff_batch_edge_sum(self.h, ii.shape[0], ii.ctypes.data, out.ctypes.data))
+            return out
+        nat.check(self.L.fb_diff_batch_edge_sum(self.h, ii.shape[0], ii.ctypes.data, C.c_void_p(out.data_ptr())))
+        return out

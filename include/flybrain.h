@@ -296,6 +296,37 @@ int fb_diff_raster(fb_diff *d, int32_t nro, const int32_t *readout, float *out);
 int fb_diff_backward(fb_diff *d, const float *dL, int32_t nro, const int32_t *readout, int32_t truncate,
                      int32_t loss_from, fb_diff_grads *g);
 
+/* ---- batches of differentiable brains ------------------------------------------------------
+ * No counterpart in the reference, which trains one LIFDiff at a time: B independent instances
+ * (each its own network, drive, seed and length; one parameter set) advanced together, every
+ * kernel launch covering the whole batch. Arrays passed by the same pointer for the same field
+ * of several instances are uploaded once and shared (fb_diff_batch_set on one of them sets it for
+ * all). Each instance's results are those of fb_diff_* on that instance alone. */
+typedef struct fb_diff_batch fb_diff_batch; /* opaque */
+
+int fb_diff_batch_create(const fb_diff_net *nets, int32_t B, int64_t tape_cap, fb_diff_batch **out);
+int fb_diff_batch_destroy(fb_diff_batch *b);
+int fb_diff_batch_set(fb_diff_batch *b, int32_t inst, int32_t field, const float *values);
+
+/* Forward of every instance from reset: steps[B] and seeds[B]; spike_counts (may be null)
+ * receives the instances' f32[N_b] spike totals back to back. */
+int fb_diff_batch_forward(fb_diff_batch *b, const fb_diff_params *p, const int32_t *steps,
+                          const uint32_t *seeds, int32_t record, float *spike_counts);
+int fb_diff_batch_tape(fb_diff_batch *b, int32_t inst, int64_t *offsets, int32_t *idx, float *amp,
+                       int64_t cap, int64_t *len);
+int fb_diff_batch_raster(fb_diff_batch *b, int32_t inst, int32_t nro, const int32_t *readout, float *out);
+
+/* Backward of every instance over its recorded forward: dL[b], nro[b] (null: all 0) and
+ * readout[b] as in fb_diff_backward; g[b] receives instance b's gradients (host or device
+ * pointers). */
+int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, const int32_t *nro,
+                           const int32_t *const *readout, int32_t truncate, int32_t loss_from,
+                           fb_diff_grads *g);
+
+/* out f64[E] (host or device) = the per-edge gradients of instances insts[0..n) of the last
+ * backward, summed in list order (the instances must have the same edge count). */
+int fb_diff_batch_edge_sum(fb_diff_batch *b, int32_t n, const int32_t *insts, double *out);
+
 /* ---- allocation-free step ----------------------------------------------------------------- */
 
 /* A caller-owned brain for fb_lif_step_noalloc: the fields of the reference's Brain header
