@@ -475,11 +475,18 @@ def run_adjoint_uneven(n_inst=128, seed=11):
     from flybrain.synth import synth_graph
     prec = os.environ.get("FB_ADJ_PRECISION", "f32")
     rng = np.random.default_rng(seed)
+    import concurrent.futures as cf
+    import multiprocessing as mp
     members, readouts, targets, steps = [], [], [], []
     t0 = time.perf_counter()
+    sizes = [int(rng.integers(5000, 60001)) for _ in range(n_inst)]
+    # the graphs are generated on the host cores by spawned workers (this process holds a CUDA
+    # context, so it is not forked)
+    with cf.ProcessPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)),
+                                mp_context=mp.get_context("spawn")) as ex:
+        graphs = list(ex.map(synth_graph, sizes, [1000 + k for k in range(n_inst)]))
     for k in range(n_inst):
-        N = int(rng.integers(5000, 60001))
-        sg = synth_graph(N, 1000 + k)
+        N, sg = sizes[k], graphs[k]
         n = DiffNet(dict(N=N, indptr=sg.indptr, indices=sg.indices, weights=sg.counts.astype(np.float32),
                          sign=sg.sign), dict(ADJ_OPTS), _defer=True)
         for i in rng.choice(N, max(1, N // 100), replace=False):

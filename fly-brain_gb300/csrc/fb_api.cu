@@ -13,8 +13,10 @@
 #include <vector>
 
 #include "fb_internal.cuh"
+#include "fb_lagged.cuh"
 
 namespace fb {
+cudaError_t launch_rebuild_slots(Trial *Td, int nslots, int32_t *err, cudaStream_t st);
 int step_kernel_blocks_per_sm(size_t smem);
 size_t step_smem_bytes(int B);
 cudaError_t launch_step(const StepArgs &a, int grid, size_t smem, cudaStream_t st);
@@ -354,18 +356,21 @@ struct DrivenSet {
   std::vector<int32_t> order;  // neuron or -1
   std::vector<int32_t> pos;    // index in order, or -1
   bool dirty = true;
-  void init(int N) { order.clear(); pos.assign(N, -1); dirty = true; }
+  uint64_t version = 0;  // changes with the set (ownership of the delay-scheduled kernel)
+  void init(int N) { order.clear(); pos.assign(N, -1); dirty = true; version++; }
   void add(int32_t i) {
     if (pos[i] >= 0) return;
     pos[i] = (int32_t)order.size();
     order.push_back(i);
     dirty = true;
+    version++;
   }
   void remove(int32_t i) {
     if (pos[i] < 0) return;
     order[pos[i]] = -1;
     pos[i] = -1;
     dirty = true;
+    version++;
   }
   void compact() {
     size_t n = 0;
@@ -377,6 +382,24 @@ struct DrivenSet {
       }
     order.resize(n);
   }
+};
+
+// Device resources of the delay-scheduled kernel (fb_lagged.cu) for a single brain, allocated
+// at its first use at the largest sizes the brain can need.
+struct LagRes {
+  bool ready = false;
+  int D = 0, S = 0, nTB = 0, capMax = 0, nDmax = 0, bgCap = 0, grid = 0;
+  uint64_t drivenVersion = ~0ull;
+  std::vector<void *> allocs;
+  uint32_t *inOff = nullptr, *cnt = nullptr, *pend0 = nullptr, *sync = nullptr, *bgList = nullptr;
+  uint32_t *jumpHex = nullptr;
+  uint4 *edgeRec = nullptr;
+  uint2 *buf = nullptr;
+  uint4 *dbList = nullptr;
+  int32_t *bgCount = nullptr, *dbCnt = nullptr, *dbNF = nullptr, *tStage = nullptr, *tCnt = nullptr;
+  int32_t *ndIds = nullptr, *ndLo = nullptr, *drvPosOf = nullptr;
+  int cap = 1, nD = 0;
+  size_t smem = 0;
 };
 
 struct fb_brains {
@@ -408,6 +431,8 @@ struct fb_brains {
   int logging = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float lastMs = 0.f;
+  int32_t schedule = FB_SCHEDULE_AUTO, lastSchedule = FB_SCHEDULE_GRID;
+  LagRes lag;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -597,10 +622,24 @@ extern "C" int fb_brains_destroy(fb_brains *br) {
   cudaFree(br->d_phase);
   cudaFree(br->d_dbg);
   cudaFree(br->d_ovf[0]); cudaFree(br->d_ovf[1]);
+  for (void *p : br->lag.allocs) cudaFree(p);
   if (br->ev0) cudaEventDestroy(br->ev0);
   if (br->ev1) cudaEventDestroy(br->ev1);
   if (br->stream) cudaStreamDestroy(br->stream);
   delete br;
+  return FB_OK;
+}
+
+extern "C" int fb_brains_set_schedule(fb_brains *br, int32_t schedule) {
+  if (!br || schedule < FB_SCHEDULE_AUTO || schedule > FB_SCHEDULE_LAGGED)
+    return fail(FB_EINVAL, "fb_brains_set_schedule: bad schedule %d", schedule);
+  br->schedule = schedule;
+  return FB_OK;
+}
+
+extern "C" int fb_last_schedule(fb_brains *br, int32_t *schedule) {
+  if (!br || !schedule) return fail(FB_EINVAL, "fb_last_schedule: null argument");
+  *schedule = br->lastSchedule;
   return FB_OK;
 }
 
@@ -744,10 +783,199 @@ extern "C" int fb_set_background(fb_brains *br, int32_t b, double rate_hz, doubl
   return FB_OK;
 }
 
+// ---- the delay-scheduled kernel ----------------------------------------------------------------
+
+constexpr int kLagMinSteps = 16;  // AUTO: shorter launches take the grid kernel
+
+// Whether the delay-scheduled kernel applies to this launch (why not, in *why).
+static bool lag_applies(fb_brains *br, int32_t steps, const char **why) {
+  const Trial &T = br->host[0];
+  *why = nullptr;
+  if (br->B != 1) *why = "a batch of more than one brain";
+  else if (T.mode != FB_DELIVER_EXACT || (T.flags & kHasPreInh)) *why = "a delivery mode other than exact without presynaptic inhibition";
+  else if (br->profiling && br->schedule != FB_SCHEDULE_LAGGED) *why = "phase profiling";
+  else if (br->logging && steps > kLagRing) *why = "per-step logging of a launch longer than 64 steps";
+  else if (T.nslots - 1 < kHelp + 1 || T.nslots - 1 > 32) *why = "a ring depth outside 4..33 slots";
+  else if (T.bgEvents > (float)(1 << 20)) *why = "more than 2^20 background events per step";
+  return *why == nullptr;
+}
+
+template <typename X>
+static int lag_alloc(fb_brains *br, X **p, size_t n) {
+  void *q = nullptr;
+  if (cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(X)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(FB_ENOMEM, "fb_step: %zu bytes for the delay-scheduled kernel", n * sizeof(X));
+  }
+  br->lag.allocs.push_back(q);
+  *p = (X *)q;
+  return FB_OK;
+}
+
+// Allocates the kernel's resources and (when the driven set changed) the neuron ownership.
+static int lag_setup(fb_brains *br) {
+  LagRes &R = br->lag;
+  Trial &T = br->host[0];
+  const int N = T.N;
+  const int64_t E = T.E;
+  int rc;
+  if (!R.ready) {
+    int sms = 0, optin = 0;
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, br->dev));
+    CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, br->dev));
+    R.grid = sms;
+    R.nTB = sms - 1;
+    R.D = T.nslots - 1;
+    R.S = 2 * R.D;
+    R.capMax = std::max(1, (N + R.nTB - 1) / R.nTB);
+    R.nDmax = 0;
+    for (int nd = 32; nd <= 8192; nd += 32)
+      if (lagged_smem_bytes(R.capMax, nd) <= (size_t)optin) R.nDmax = nd;
+    if (R.nDmax == 0) return fail(FB_EINVAL, "fb_step: the delay-scheduled kernel does not fit in shared memory");
+    // in-degree prefix: each target's bucket entries start at inOff[q]
+    std::vector<uint32_t> ix(E), off(N + 1, 0);
+    if (E) CU(cudaMemcpy(ix.data(), T.indices, E * 4, cudaMemcpyDeviceToHost));
+    for (int64_t j = 0; j < E; j++) off[ix[j] + 1]++;
+    for (int q = 0; q < N; q++) off[q + 1] += off[q];
+    if ((rc = lag_alloc(br, &R.inOff, N + 1)) || (rc = lag_alloc(br, &R.cnt, (size_t)R.S * (N + R.nDmax))) ||
+        (rc = lag_alloc(br, &R.buf, (size_t)R.S * std::max<int64_t>(E, 1))) || (rc = lag_alloc(br, &R.pend0, N)) ||
+        (rc = lag_alloc(br, &R.sync, 256)) || (rc = lag_alloc(br, &R.bgCount, kLagRing)) ||
+        (rc = lag_alloc(br, &R.dbList, (size_t)kLagRing * R.nDmax * 2)) || (rc = lag_alloc(br, &R.dbCnt, kLagRing)) ||
+        (rc = lag_alloc(br, &R.dbNF, kLagRing)) || (rc = lag_alloc(br, &R.tStage, (size_t)kLagRing * R.nTB * R.capMax)) ||
+        (rc = lag_alloc(br, &R.tCnt, (size_t)kLagRing * R.nTB)) || (rc = lag_alloc(br, &R.ndIds, N)) ||
+        (rc = lag_alloc(br, &R.ndLo, R.nTB + 1)) || (rc = lag_alloc(br, &R.drvPosOf, N)) || (rc = lag_alloc(br, &R.edgeRec, std::max<int64_t>(E, 1))))
+      return rc;
+    CU(cudaMemcpy(R.inOff, off.data(), (N + 1) * 4, cudaMemcpyHostToDevice));
+    std::vector<uint32_t> tab;
+    lagged_jump_tables(tab);
+    if ((rc = lag_alloc(br, &R.jumpHex, tab.size()))) return rc;
+    CU(cudaMemcpyAsync(R.jumpHex, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, br->stream));
+    CU(cudaStreamSynchronize(br->stream));
+    R.ready = true;
+  }
+  const int bgNeed = T.bgEvents > 0 ? (int)std::ceil((double)T.bgEvents) + 1 : 1;
+  if (bgNeed > R.bgCap) {
+    if ((rc = lag_alloc(br, &R.bgList, (size_t)kLagRing * bgNeed))) return rc;
+    R.bgCap = bgNeed;
+  }
+  const DrivenSet &ds = br->driven[0];
+  if (ds.version != R.drivenVersion) {
+    const int nD = (int)ds.order.size();
+    if (nD > R.nDmax) return fail(FB_EINVAL, "fb_step: %d driven neurons exceed the delay-scheduled kernel's %d", nD, R.nDmax);
+    if ((int64_t)nD + R.bgCap + 64 >= 65536)
+      return fail(FB_EINVAL, "fb_step: %d draws per step exceed the delay-scheduled kernel's jump tables", nD + R.bgCap);
+    std::vector<uint8_t> isD(N, 0);
+    for (int32_t i : ds.order) isD[i] = 1;
+    std::vector<int32_t> nd;
+    nd.reserve(N - nD);
+    for (int i = 0; i < N; i++)
+      if (!isD[i]) nd.push_back(i);
+    const int64_t Nnd = (int64_t)nd.size();
+    std::vector<int32_t> lo(R.nTB + 1);
+    for (int t = 0; t <= R.nTB; t++) lo[t] = (int32_t)(Nnd * t / R.nTB);
+    std::vector<int32_t> posOf(N, -1);
+    for (int k = 0; k < nD; k++) posOf[ds.order[k]] = k;
+    if (Nnd) CU(cudaMemcpyAsync(R.ndIds, nd.data(), Nnd * 4, cudaMemcpyHostToDevice, br->stream));
+    CU(cudaMemcpyAsync(R.ndLo, lo.data(), (R.nTB + 1) * 4, cudaMemcpyHostToDevice, br->stream));
+    CU(cudaMemcpyAsync(R.drvPosOf, posOf.data(), (size_t)N * 4, cudaMemcpyHostToDevice, br->stream));
+    CU(launch_edge_records(T.indices, R.inOff, R.drvPosOf, N, E, R.edgeRec, br->stream));
+    CU(cudaStreamSynchronize(br->stream));
+    R.nD = nD;
+    R.cap = std::max<int>(1, (int)((Nnd + R.nTB - 1) / R.nTB));
+    if (R.cap > kLagPer * kLagThreads || nD > kLagPer * kLagThreads)
+      return fail(FB_EINVAL, "fb_step: %d neurons per block or %d driven neurons exceed the delay-scheduled kernel's %d",
+                  R.cap, nD, kLagPer * kLagThreads);
+    const int nDcap = std::max(32, (nD + 31) / 32 * 32);
+    R.smem = lagged_smem_bytes(R.cap, nDcap);
+    if (lagged_blocks_per_sm(R.smem) < 1)
+      return fail(FB_EINVAL, "fb_step: the delay-scheduled kernel does not fit on an SM (%zu bytes)", R.smem);
+    R.drivenVersion = ds.version;
+  }
+  return FB_OK;
+}
+
+static int run_lagged(fb_brains *br, int32_t steps) {
+  LagRes &R = br->lag;
+  Trial &T = br->host[0];
+  const int N = T.N;
+  CU(cudaMemsetAsync(R.sync, 0, 256 * 4, br->stream));
+  CU(cudaMemsetAsync(R.cnt, 0, (size_t)R.S * (N + R.nDmax) * 4, br->stream));
+  CU(cudaMemsetAsync(R.pend0, 0, (size_t)N * 4, br->stream));
+  LagArgs a;
+  memset(&a, 0, sizeof a);
+  a.G = br->trials;
+  a.N = N;
+  a.E = T.E;
+  a.T = steps;
+  a.D = R.D;
+  a.S = R.S;
+  a.L = R.D - kHelp;
+  a.nTB = R.nTB;
+  a.cap = R.cap;
+  a.nD = R.nD;
+  a.nDcap = std::max(32, (R.nD + 31) / 32 * 32);
+  a.m = (R.nD + kLagThreads - 1) / kLagThreads;
+  a.hasBg = T.bgEvents > 0 ? 1 : 0;
+  a.bgCap = R.bgCap;
+  a.dt = T.dt; a.vRest = T.vRest; a.vThresh = T.vThresh; a.vReset = T.vReset; a.tRef = T.tRef;
+  a.adaptInc = T.adaptInc; a.depU = T.depU; a.dE = T.dE; a.dTr = T.dTr; a.dA = T.dA; a.kRec = T.kRec;
+  a.kM = T.kM; a.dtS = T.dtS; a.eExc = T.eExc; a.eInh = T.eInh; a.cE = T.cE; a.cI = T.cI;
+  a.bgEvents = T.bgEvents; a.bgAmp = T.bgAmp; a.coba = T.coba;
+  a.indptr = T.indptr; a.indices = T.indices; a.W = T.W; a.sign = T.sign; a.inOff = R.inOff;
+  a.v = T.v; a.gE = T.gE; a.gI = T.gI; a.refr = T.refr; a.trace = T.trace; a.adapt = T.adapt; a.res = T.res;
+  a.bias = T.bias; a.thr = T.thr; a.drive = T.drive; a.spikeCount = T.spikeCount;
+  a.ring = T.ring; a.ringCount = T.ringCount; a.driven = T.driven;
+  a.ndIds = R.ndIds; a.ndLo = R.ndLo; a.drvPosOf = R.drvPosOf;
+  a.cnt = R.cnt; a.cntStride = N + R.nDmax; a.buf = R.buf; a.pend0 = R.pend0;
+  a.done = R.sync; a.dbDone = R.sync + 64; a.bgReady = R.sync + 65; a.barCount = R.sync + 128;
+  a.stepTot = (int32_t *)(R.sync + 192);
+  a.bgList = R.bgList; a.bgCount = R.bgCount; a.dbList = R.dbList; a.dbCnt = R.dbCnt;
+  a.tStage = R.tStage; a.tCnt = R.tCnt;
+  a.log = br->logging;
+  a.logCount = T.logCount; a.logRaster = T.logRaster; a.logCap = T.logCap; a.logRasterCap = T.logRasterCap;
+  a.prof = br->profiling ? br->d_phase : nullptr;
+  a.jumpHex = R.jumpHex;
+  a.edgeRec = R.edgeRec;
+  a.err = br->d_err;
+  a.timeoutNs = 5000000000LL;
+  CU(cudaEventRecord(br->ev0, br->stream));
+  CU(launch_lagged(a, R.grid, R.smem, br->stream));
+  CU(launch_rebuild_slots(br->trials, T.nslots, br->d_err, br->stream));
+  CU(cudaEventRecord(br->ev1, br->stream));
+  br->lastSchedule = FB_SCHEDULE_LAGGED;
+  return FB_OK;
+}
+
 static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
   int rc = flush(br);
   if (rc) return rc;
-  if (maxSteps > 0) {
+  bool lagged = false;
+  if (maxSteps > 0 && br->schedule != FB_SCHEDULE_GRID) {
+    const char *why = nullptr;
+    const bool applies = lag_applies(br, maxSteps, &why);
+    if (br->schedule == FB_SCHEDULE_LAGGED) {
+      if (!applies) return fail(FB_EINVAL, "fb_step: the delay-scheduled kernel does not apply to %s", why);
+      if ((rc = lag_setup(br))) return rc;
+      lagged = true;
+    } else if (applies && maxSteps >= kLagMinSteps) {
+      lagged = lag_setup(br) == FB_OK;
+      if (!lagged) g_err.clear();
+    }
+  }
+  if (lagged) {
+    if ((rc = run_lagged(br, maxSteps))) return rc;
+    int32_t err = 0;
+    CU(cudaMemcpyAsync(&err, br->d_err, 4, cudaMemcpyDeviceToHost, br->stream));
+    CU(cudaStreamSynchronize(br->stream));
+    cudaEventElapsedTime(&br->lastMs, br->ev0, br->ev1);
+    if (err) {
+      cudaMemsetAsync(br->d_err, 0, 4, br->stream);
+      cudaStreamSynchronize(br->stream);
+      return fail(err, err == FB_ETIMEOUT ? "fb_step: a device-side wait timed out; the step was abandoned"
+                                          : "fb_step: delay-scheduled kernel error %d", err);
+    }
+  } else if (maxSteps > 0) {
+    br->lastSchedule = FB_SCHEDULE_GRID;
     CU(cudaMemcpyAsync(br->d_steps, br->stepsHost.data(), sizeof(int32_t) * br->B, cudaMemcpyHostToDevice, br->stream));
     StepArgs a;
     memset(&a, 0, sizeof a);

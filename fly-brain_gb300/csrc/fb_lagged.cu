@@ -1,0 +1,983 @@
+// The brain step without a per-step grid barrier, for one brain advanced by many steps: the exact
+// semantics of lif_step (src/wasm/lif.c:29-80), scheduled by the synaptic delay.
+//
+// A spike emitted at step s arrives D = nslots - 1 steps later (lif.c:44-45, 77-79). Its
+// contributions are known at emission, so they are pushed then into per-arrival-step buckets;
+// a block updating step t only needs every block to have finished step t - D (plus the helper
+// delay below), not step t - 1. Blocks therefore advance on their own and synchronise through
+// per-step completion counters with up to L = D - kHelp steps of slack.
+//
+//  - Tile blocks (all but block 0) own fixed sets of non-driven neurons (contiguous ascending id
+//    ranges), their state held in shared memory for the whole launch.
+//  - The driven block (block 0) owns every Poisson-driven neuron and the generator: the
+//    background draws and one draw per non-refractory driven neuron in list order (lif.c:46-52),
+//    then those neurons' updates. Its spikes are pushed by the tile blocks kHelp steps later.
+//  - The summation order of lif.c is kept per target: each contribution carries its arrival's
+//    rank in the fired list (forced spikes first in list order, then threshold spikes by
+//    ascending id, lif.c:51-52, 73-76), and the target adds them in rank order.
+//  - The amplitude sign*res of an arrival (lif.c:37) is fixed at emission by replaying the
+//    presynaptic neuron's own depression and recovery up to the arrival step (its earlier spikes
+//    in flight are known to its owner); the result is the value lif.c reads at delivery.
+//  - At launch start the spikes already in flight (the ring) are pushed the same way; at the end
+//    the last D fired lists are written back into the ring, so either kernel can continue.
+//
+// Not covered (the two-phase kernel runs these): presynaptic inhibition (its amplitude depends on
+// the target state at delivery), sequential and fast delivery modes, batches, per-step logging.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "fb_internal.cuh"
+#include "fb_lagged.cuh"
+
+namespace fb {
+
+constexpr int kLB = kLagThreads;
+constexpr int kBgChunk = 1024;
+constexpr int kHexLevels = 3;           // hexadecimal digits by table; beyond, M^4096 repeated
+constexpr int kHexWords = (kHexLevels * 15 + 1) * 128;
+constexpr int kOffWords = 32 * 128;
+
+__device__ __forceinline__ void red_release(uint32_t *p, uint32_t v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr int kMaxPer = kLagPer;
+
+struct LagShared {
+  int32_t nLocal;  // neurons owned by this block
+  int32_t idLo, idHi;
+  int32_t stop;
+  uint32_t rng;
+  float bgAcc;
+  int32_t nbg;
+  int32_t known;   // highest step known finished by every block
+  int32_t head0;   // ring head at launch
+  int64_t steps0;  // steps done before the launch
+  int64_t logBase;
+  uint32_t scan[33];
+  uint64_t scan64[33];
+  uint32_t wfirst[kMaxPer * 32];  // driven block: first live rank of each warp and round
+  uint32_t wstate[kMaxPer * 32];  // ... and the generator state there
+  uint32_t dbCount;               // driven block: spikes of the step
+};
+
+__device__ __forceinline__ bool lag_timeout(const LagArgs &a, uint64_t t0, uint32_t &it) {
+  if ((++it & 63u) == 0) {
+    if (ld_volatile(a.err) != 0) return true;
+    if (global_ns() - t0 > (uint64_t)a.timeoutNs || it > (1u << 30)) {
+      atomicCAS(a.err, 0, FB_ETIMEOUT);
+      return true;
+    }
+  }
+  return false;
+}
+
+// Grid barrier of a cooperative launch (same scheme as grid_sync).
+__device__ bool lag_grid_sync(const LagArgs &a) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const uint32_t add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
+    __threadfence();
+    const uint32_t old = atomicAdd(a.barCount, add);
+    const uint64_t t0 = global_ns();
+    uint32_t it = 0;
+    while (((ld_relaxed(a.barCount) ^ old) & 0x80000000u) == 0)
+      if (lag_timeout(a, t0, it)) {
+        ok = 0;
+        break;
+      }
+    __threadfence();
+    if (ok && ld_volatile(a.err) != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Waits (thread 0) until *p >= target (acquire); false on timeout or a recorded error. *seen
+// (optional) receives the value observed.
+__device__ __forceinline__ bool wait_geq(const LagArgs &a, const uint32_t *p, uint32_t target,
+                                         uint32_t *seen = nullptr) {
+  uint32_t v = ld_acquire(p);
+  if (v < target) {
+    const uint64_t t0 = global_ns();
+    uint32_t it = 0;
+    while ((v = ld_acquire(p)) < target)
+      if (lag_timeout(a, t0, it)) return false;
+  }
+  if (seen) *seen = v;
+  return true;
+}
+
+// Jump-ahead for the driven block. hex[(i * 15 + v - 1) * 128 ...] holds M^(v * 16^i) (v = 1..15,
+// i = 0..2) as 8 nibble tables, followed by M^4096; for a warp-uniform d every lane reads the same
+// words (broadcast). d < 65536.
+__device__ __forceinline__ uint32_t xs_jump_hex(const uint32_t *hex, uint32_t s, uint32_t d) {
+#pragma unroll
+  for (int i = 0; i < kHexLevels; i++) {
+    const uint32_t v = (d >> (4 * i)) & 15u;
+    if (v) s = xs_apply(hex + (i * 15 + v - 1) * 128, s);
+  }
+  for (uint32_t q = d >> (4 * kHexLevels); q; q--) s = xs_apply(hex + kHexLevels * 15 * 128, s);
+  return s;
+}
+// off holds M^l (l = 0..31) interleaved by lane: word (n * 16 + nibble) * 32 + l, so lane l
+// applying M^l reads bank l only.
+__device__ __forceinline__ uint32_t xs_apply_lane(const uint32_t *off, uint32_t lane, uint32_t x) {
+  uint32_t y = 0;
+#pragma unroll
+  for (int n = 0; n < 8; n++) y ^= off[((uint32_t)n * 16 + ((x >> (4 * n)) & 15u)) * 32 + lane];
+  return y;
+}
+
+// Phase timer: thread 0 of blocks 0 and 1 adds the time since its last lap to slot k.
+__device__ __forceinline__ void lap(const LagArgs &a, int k, uint64_t &tp) {
+  if (a.prof != nullptr && blockIdx.x < 2 && threadIdx.x == 0) {
+    const uint64_t now = global_ns();
+    atomicAdd(a.prof + k, (unsigned long long)(now - tp));
+    tp = now;
+  }
+}
+
+// Every block has finished step `s`: its completion counter reached grid * (epoch + 1).
+__device__ __forceinline__ uint32_t done_target(int s, int grid) { return (uint32_t)grid * (uint32_t)(s / kLagRing + 1); }
+
+// Amplitude sign*res that lif.c reads when this neuron's spike arrives, replayed from its state
+// now: `r` is res after this step's update, bit w of `pend` marks an earlier spike of the neuron
+// arriving w+1 steps from now; `steps` steps of delivery (depression, lif.c:37-39) and
+// recovery (lif.c:71) precede the arrival.
+__device__ __forceinline__ float predict_amp(const LagArgs &a, float sign, float r, uint32_t pend, int steps) {
+  if (sign == 0.f) return 0.f;
+  if (a.depU == 0.f && r == 1.f) return sign;
+  for (int w = 0; w < steps; w++) {
+    if ((pend >> w) & 1u)
+      if (__fmul_rn(sign, r) != 0.f) r = __fsub_rn(r, __fmul_rn(a.depU, r));
+    r = __fadd_rn(r, __fmul_rn(__fsub_rn(1.f, r), a.kRec));
+  }
+  return __fmul_rn(sign, r);
+}
+
+// One warp pushes the contributions W[j]*amp (lif.c:41-42) of edges [lo, hi) of one presynaptic
+// neuron into the buckets of arrival slot `slot`, keyed by (rank << 1) | inhibitory. Each edge's
+// record holds its target's count slot, its first bucket entry and their end. Up to kPushChunks
+// edges per lane are in flight at once: their loads, then their slot claims, then their stores.
+constexpr int kPushChunks = 1;
+__device__ __forceinline__ void push_edges(const LagArgs &a, uint32_t lo, uint32_t hi, uint32_t rank, float amp,
+                                           int slot) {
+  if (amp == 0.f) return;  // lif.c:37: nothing delivered, no depression
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t key = (rank << 1) | (amp > 0 ? 0u : 1u);
+  uint32_t *cnt = a.cnt + (int64_t)slot * a.cntStride;
+  uint2 *buf = a.buf + (int64_t)slot * a.E;
+  for (uint32_t j0 = lo; j0 < hi; j0 += 32 * kPushChunks) {
+    uint4 er[kPushChunks];
+    float w[kPushChunks];
+    uint32_t pos[kPushChunks];
+#pragma unroll
+    for (int c = 0; c < kPushChunks; c++) {
+      const uint32_t j = j0 + lane + 32 * c;
+      if (j < hi) {
+        er[c] = __ldg(a.edgeRec + j);
+        w[c] = __ldg(a.W + j);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < kPushChunks; c++)
+      if (j0 + lane + 32 * c < hi) pos[c] = atomicAdd(cnt + er[c].x, 1u);
+#pragma unroll
+    for (int c = 0; c < kPushChunks; c++) {
+      if (j0 + lane + 32 * c < hi) {
+        if (er[c].y + pos[c] < er[c].z) buf[er[c].y + pos[c]] = make_uint2(key, __float_as_uint(__fmul_rn(w[c], amp)));
+        else atomicCAS(a.err, 0, FB_EOVERFLOW);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void push_row(const LagArgs &a, int32_t pre, uint32_t rank, float amp, int slot) {
+  if (amp == 0.f) return;
+  push_edges(a, __ldg(a.indptr + pre), __ldg(a.indptr + pre + 1), rank, amp, slot);
+}
+
+// Adds target i's n contributions of a slot in ascending key order (lif.c's order); up to
+// kSortMax are sorted in registers at a time, in windows of ascending keys beyond that.
+__device__ void apply_slot(const LagArgs &a, const uint2 *e0, uint32_t n, float &ge, float &gi) {
+  if (n == 1) {
+    const uint2 x = ldcg(e0);
+    if (x.x & 1u) gi = __fadd_rn(gi, __uint_as_float(x.y));
+    else ge = __fadd_rn(ge, __uint_as_float(x.y));
+    return;
+  }
+  uint2 e[kSortMax];
+  bool any = false;
+  uint32_t last = 0;
+  for (uint32_t done = 0; done < n;) {
+    uint32_t m = 0;
+    for (uint32_t u = 0; u < n; u++) {
+      const uint2 x = ldcg(e0 + u);
+      if (any && x.x <= last) continue;
+      if (m == (uint32_t)kSortMax && x.x >= e[m - 1].x) continue;
+      uint32_t w = m < (uint32_t)kSortMax ? m++ : m - 1;
+      while (w > 0 && e[w - 1].x > x.x) {
+        e[w] = e[w - 1];
+        w--;
+      }
+      e[w] = x;
+    }
+    if (m == 0) {
+      atomicCAS(a.err, 0, FB_EOVERFLOW);
+      break;
+    }
+    for (uint32_t u = 0; u < m; u++) {
+      if (e[u].x & 1u) gi = __fadd_rn(gi, __uint_as_float(e[u].y));
+      else ge = __fadd_rn(ge, __uint_as_float(e[u].y));
+    }
+    last = e[m - 1].x;
+    any = true;
+    done += m;
+  }
+}
+
+// Shared-memory state of the block's neurons (structure of arrays, `cap` entries each): the
+// model state, launch constants (bias, thr, drive, sign, bucket offset and in-degree), the
+// amplitude of a spike of this step, the in-flight arrival mask and background hit counts.
+constexpr int kStateWords = 20;
+struct LagState {
+  float *v, *ge, *gi, *r, *tr, *ad, *rs, *bias, *thr, *drive, *amp, *sign;
+  uint32_t *sc, *pend, *hits, *off, *deg, *row0, *row1;
+  int32_t *id;
+};
+
+__device__ __forceinline__ LagState carve(unsigned char *sm, int cap) {
+  LagState s;
+  float *f = (float *)sm;
+  s.v = f; f += cap;
+  s.ge = f; f += cap;
+  s.gi = f; f += cap;
+  s.r = f; f += cap;
+  s.tr = f; f += cap;
+  s.ad = f; f += cap;
+  s.rs = f; f += cap;
+  s.bias = f; f += cap;
+  s.thr = f; f += cap;
+  s.drive = f; f += cap;
+  s.amp = f; f += cap;
+  s.sign = f; f += cap;
+  s.sc = (uint32_t *)f; f += cap;
+  s.pend = (uint32_t *)f; f += cap;
+  s.hits = (uint32_t *)f; f += cap;
+  s.off = (uint32_t *)f; f += cap;
+  s.deg = (uint32_t *)f; f += cap;
+  s.row0 = (uint32_t *)f; f += cap;
+  s.row1 = (uint32_t *)f; f += cap;
+  s.id = (int32_t *)f;
+  return s;
+}
+
+// Delivery side of one step for local neuron k with n contributions in slot `slot`: the
+// contributions, then background hits (lif.c:48), then the neuron's own depression if its spike
+// arrives now (lif.c:37-39).
+__device__ __forceinline__ void receive(const LagArgs &a, const LagState &S, int k, uint32_t n, uint32_t ci,
+                                        int slot) {
+  float ge = S.ge[k], gi = S.gi[k];
+  if (n) {
+    const uint32_t deg = S.deg[k];
+    if (n > deg) {  // cannot happen with one contribution per presynaptic neuron and step
+      atomicCAS(a.err, 0, FB_EOVERFLOW);
+      n = deg;
+    }
+    apply_slot(a, a.buf + (int64_t)slot * a.E + S.off[k], n, ge, gi);
+    a.cnt[(int64_t)slot * a.cntStride + ci] = 0;
+  }
+  const uint32_t h = S.hits[k];
+  if (h) {
+    for (uint32_t u = 0; u < h; u++) ge = __fadd_rn(ge, a.bgAmp);
+    S.hits[k] = 0;
+  }
+  S.ge[k] = ge;
+  S.gi[k] = gi;
+  if (S.pend[k] & 1u) {
+    const float rs = S.rs[k];
+    if (!(__fmul_rn(S.sign[k], rs) == 0.f)) S.rs[k] = __fsub_rn(rs, __fmul_rn(a.depU, rs));
+  }
+}
+
+// lif.c:53-76 for local neuron k: membrane, decays, threshold. Returns whether it crossed the
+// threshold; pend advances one step and, on a spike, marks the new arrival D steps ahead.
+__device__ __forceinline__ bool integrate(const LagArgs &a, const LagState &S, int k) {
+  float v = S.v[k], r = S.r[k], ge = S.ge[k], gi = S.gi[k];
+  float acc = __fsub_rn(a.vRest, v);
+  if (a.coba) {
+    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(ge, __fsub_rn(a.eExc, v)), a.cE));
+    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(gi, __fsub_rn(v, a.eInh)), a.cI));
+  } else {
+    acc = __fadd_rn(acc, ge);
+    acc = __fadd_rn(acc, gi);
+  }
+  acc = __fadd_rn(acc, S.bias[k]);
+  const float dv = __fmul_rn(acc, a.kM);
+  const bool refractory = r > 0;
+  v = refractory ? a.vReset : __fadd_rn(v, dv);
+  r = refractory ? __fsub_rn(r, a.dt) : r;
+  S.ge[k] = __fmul_rn(ge, a.dE);
+  S.gi[k] = __fmul_rn(gi, a.dE);
+  float tr = __fmul_rn(S.tr[k], a.dTr);
+  float ad = __fmul_rn(S.ad[k], a.dA);
+  const float rs0 = S.rs[k];
+  S.rs[k] = __fadd_rn(rs0, __fmul_rn(__fsub_rn(1.f, rs0), a.kRec));
+  bool fired = false;
+  if (v >= __fadd_rn(__fadd_rn(a.vThresh, ad), S.thr[k]) && r <= 0) {
+    v = a.vReset;
+    r = a.tRef;
+    tr = 1.f;
+    ad = __fadd_rn(ad, a.adaptInc);
+    S.sc[k] += 1u;
+    fired = true;
+  }
+  S.v[k] = v;
+  S.r[k] = r;
+  S.tr[k] = tr;
+  S.ad[k] = ad;
+  return fired;
+}
+
+// After a step: the arrival mask shifts; a spike of this step arrives D steps ahead (bit D-1)
+// and its amplitude is fixed now.
+__device__ __forceinline__ void emit(const LagArgs &a, const LagState &S, int k, bool spiked) {
+  const uint32_t p = S.pend[k] >> 1;
+  if (spiked) S.amp[k] = predict_amp(a, S.sign[k], S.rs[k], p, a.D - 1);
+  S.pend[k] = spiked ? p | (1u << (a.D - 1)) : p;
+}
+
+// Background targets of the step that fall on this block's neurons: a hit count per neuron.
+__device__ void collect_bg(const LagArgs &a, LagShared &sh, const LagState &S, uint32_t *sBg, int s,
+                           bool driven) {
+  const int nbg = ldcg(a.bgCount + (s & (kLagRing - 1)));
+  const uint32_t *list = a.bgList + (int64_t)(s & (kLagRing - 1)) * a.bgCap;
+  for (int c0 = 0; c0 < nbg; c0 += kBgChunk) {
+    const int m = min(kBgChunk, nbg - c0);
+    for (int k = threadIdx.x; k < m; k += blockDim.x) sBg[k] = ldcg(list + c0 + k);
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+      const int32_t x = (int32_t)sBg[k];
+      if (driven) {  // the target's place in the driven list, if driven
+        const int32_t p = __ldg(a.drvPosOf + x);
+        if (p >= 0) atomicAdd(S.hits + p, 1u);
+        continue;
+      }
+      if (x < sh.idLo || x > sh.idHi) continue;
+      int lo = 0, hi = sh.nLocal;
+      while (lo < hi) {  // first entry >= x
+        const int mid = (lo + hi) >> 1;
+        if (S.id[mid] < x) lo = mid + 1;
+        else hi = mid;
+      }
+      if (lo < sh.nLocal && S.id[lo] == x) atomicAdd(S.hits + lo, 1u);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ LagShared sh;
+  const int tid = threadIdx.x;
+  const bool drivenBlock = blockIdx.x == 0;
+  const int cap = drivenBlock ? a.nDcap : a.cap;
+  LagState S = carve(smraw, cap);
+  unsigned char *tail = smraw + (size_t)kStateWords * 4 * cap;
+  uint32_t *sBg = (uint32_t *)tail;
+  uint32_t *sHex = sBg + kBgChunk;
+  uint32_t *sOff = sHex + kHexWords;
+  int32_t *sThr = (int32_t *)(sOff + kOffWords);  // driven block: threshold spikes of a step
+  const int b = blockIdx.x - 1;        // tile index of a tile block
+
+  // ---------------- prologue: own state into shared memory ----------------
+  if (tid == 0) {
+    sh.stop = 0;
+    sh.known = -1;
+    sh.dbCount = 0;
+    sh.head0 = ldcg(&a.G->head);
+    sh.steps0 = ldcg(&a.G->stepsDone);
+    if (drivenBlock) {
+      sh.nLocal = a.nD;
+      sh.idLo = 0;
+      sh.idHi = -1;
+      sh.rng = ldcg(&a.G->rngP[sh.steps0 & 1]);
+      sh.bgAcc = ldcg(&a.G->bgAccP[sh.steps0 & 1]);
+    } else {
+      const int lo = a.ndLo[b], hi = a.ndLo[b + 1];
+      sh.nLocal = hi - lo;
+      sh.idLo = hi > lo ? a.ndIds[lo] : 0;
+      sh.idHi = hi > lo ? a.ndIds[hi - 1] : -1;
+    }
+  }
+  __syncthreads();
+  const int nLocal = sh.nLocal;
+  const int head0 = sh.head0;
+  const int64_t steps0 = sh.steps0;
+  for (int k = tid; k < nLocal; k += blockDim.x) {
+    const int32_t i = drivenBlock ? a.driven[k] : a.ndIds[a.ndLo[b] + k];
+    S.id[k] = i;
+    S.v[k] = a.v[i];
+    S.ge[k] = a.gE[i];
+    S.gi[k] = a.gI[i];
+    S.r[k] = a.refr[i];
+    S.tr[k] = a.trace[i];
+    S.ad[k] = a.adapt[i];
+    S.rs[k] = a.res[i];
+    S.bias[k] = a.bias[i];
+    S.thr[k] = a.thr[i];
+    S.drive[k] = drivenBlock ? a.drive[i] : 0.f;
+    S.sc[k] = a.spikeCount[i];
+    S.hits[k] = 0;
+    S.sign[k] = a.sign[i];
+    const uint32_t o = a.inOff[i];
+    S.off[k] = o;
+    S.deg[k] = a.inOff[i + 1] - o;
+    S.row0[k] = a.indptr[i];
+    S.row1[k] = a.indptr[i + 1];
+  }
+  if (drivenBlock) {
+    for (int k = tid; k < kHexWords + kOffWords; k += blockDim.x) sHex[k] = a.jumpHex[k];
+  }
+  // spikes in flight at launch: mark each presynaptic neuron's arrival steps
+  const int ns = a.D + 1;
+  for (int u = 0; u < a.D; u++) {
+    const int rslot = (head0 + u) % ns;
+    const int32_t na = min(max(a.ringCount[rslot], 0), a.N);
+    for (int k = blockIdx.x * blockDim.x + tid; k < na; k += gridDim.x * blockDim.x) {
+      const int32_t pre = a.ring[(int64_t)rslot * a.N + k];
+      if (pre >= 0 && pre < a.N) atomicOr(a.pend0 + pre, 1u << u);
+      else atomicCAS(a.err, 0, FB_EINVAL);
+    }
+  }
+  if (!lag_grid_sync(a)) return;
+  for (int k = tid; k < nLocal; k += blockDim.x) S.pend[k] = ldcg(a.pend0 + S.id[k]);
+  // push them: one warp per in-flight arrival, ranked by its place in the ring list
+  {
+    int32_t *sPre = (int32_t *)sBg;  // prefix of the in-flight counts over arrival steps
+    if (tid == 0) {
+      int32_t c = 0;
+      for (int u = 0; u < a.D; u++) {
+        sPre[u] = c;
+        c += min(max(a.ringCount[(head0 + u) % ns], 0), a.N);
+      }
+      sPre[a.D] = c;
+    }
+    __syncthreads();
+    const int lane = tid & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t f = ((int64_t)blockIdx.x * blockDim.x + tid) >> 5; f < sPre[a.D]; f += nw) {
+      int u = 0;
+      while (sPre[u + 1] <= f) u++;
+      const int64_t w = f - sPre[u];
+      const int32_t pre = a.ring[(int64_t)((head0 + u) % ns) * a.N + w];
+      if (pre < 0 || pre >= a.N) continue;  // recorded in the marking pass above
+      float amp = 0.f;
+      if (lane == 0) {
+        const float sg = __ldg(a.sign + pre);
+        if (sg != 0.f) {
+          float r = a.res[pre];
+          const uint32_t p = ldcg(a.pend0 + pre);
+          if (a.depU == 0.f && r == 1.f) {
+            amp = sg;
+          } else {  // u steps of delivery and recovery before the arrival
+            for (int x = 0; x < u; x++) {
+              if ((p >> x) & 1u)
+                if (__fmul_rn(sg, r) != 0.f) r = __fsub_rn(r, __fmul_rn(a.depU, r));
+              r = __fadd_rn(r, __fmul_rn(__fsub_rn(1.f, r), a.kRec));
+            }
+            amp = __fmul_rn(sg, r);
+          }
+        }
+      }
+      amp = __shfl_sync(0xffffffffu, amp, 0);
+      push_row(a, pre, (uint32_t)w, amp, u % a.S);
+    }
+  }
+  if (!lag_grid_sync(a)) return;
+
+  // ---------------- the steps ----------------
+  // this thread's neurons: k = tid + r * kLB (r < per); for the driven block the list in order,
+  // round by round
+  const int per = drivenBlock ? a.m : (nLocal + kLB - 1) / kLB;
+  auto kOf = [&](int r) { return tid + r * kLB; };
+  // count slot of local neuron k: driven neurons have their own slots after the N neuron ids
+  auto cOf = [&](int k) { return drivenBlock ? (uint32_t)(a.N + k) : (uint32_t)S.id[k]; };
+  uint32_t nNext[kMaxPer];  // contribution counts of the next step, loaded one step ahead
+  bool haveNext = false;
+  uint32_t dbKnown = 0;     // tile blocks: driven-block steps known finished (thread 0)
+  uint64_t tp = a.prof != nullptr ? global_ns() : 0;
+  const int pb = drivenBlock ? 0 : 5;  // phase slots of this block
+  for (int s = 0; s < a.T; s++) {
+    const int slot = s % a.S;
+    const int ring = s & (kLagRing - 1);
+    // lag: every block has finished step s - L (and, for the background, the driven block has
+    // published this step's draws)
+    if (tid == 0) {
+      bool ok = true;
+      const int need = s - a.L;
+      if (need >= 0 && sh.known < need) {
+        ok = wait_geq(a, a.done + (need & (kLagRing - 1)), done_target(need, gridDim.x));
+        if (ok) sh.known = need;
+      }
+      if (ok && !drivenBlock && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s + 1));
+      sh.stop = ok ? 0 : 1;
+    }
+    __syncthreads();
+    if (sh.stop) break;
+    lap(a, pb + 0, tp);
+    // this step's counts (prefetched when the lag allowed it), and the next step's
+    uint32_t nCur[kMaxPer];
+#pragma unroll
+    for (int r = 0; r < kMaxPer; r++) {
+      const int k = kOf(r);
+      nCur[r] = haveNext ? nNext[r]
+                         : ((r < per && k < nLocal) ? ldcg(a.cnt + (int64_t)slot * a.cntStride + cOf(k)) : 0u);
+    }
+    haveNext = s + 1 < a.T && sh.known >= s + 1 - a.L;
+    if (haveNext) {
+      const int slot1 = (s + 1) % a.S;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        const int k = kOf(r);
+        nNext[r] = (r < per && k < nLocal) ? ldcg(a.cnt + (int64_t)slot1 * a.cntStride + cOf(k)) : 0u;
+      }
+    }
+
+    if (drivenBlock) {
+      // background draws 1..nbg (lif.c:46-48), published for every block
+      if (a.hasBg) {
+        if (tid == 0) {
+          const float acc = __fadd_rn(sh.bgAcc, a.bgEvents);
+          const int32_t nbg = (int32_t)acc;
+          sh.bgAcc = __fsub_rn(acc, (float)nbg);
+          sh.nbg = min(nbg, a.bgCap);
+          if (nbg > a.bgCap) atomicCAS(a.err, 0, FB_EOVERFLOW);
+          a.bgCount[ring] = sh.nbg;
+        }
+        __syncthreads();
+        const uint32_t s0 = sh.rng;
+        for (int d = 1 + tid; d <= sh.nbg; d += blockDim.x)
+          a.bgList[(int64_t)ring * a.bgCap + d - 1] = xs_jump_hex(sHex, s0, (uint32_t)d) % (uint32_t)a.N;
+        __syncthreads();
+        if (tid == 0) st_release(a.bgReady, (uint32_t)(s + 1));
+        collect_bg(a, sh, S, sBg, s, true);
+      } else if (tid == 0) {
+        sh.nbg = 0;
+      }
+      // entries k = tid + r * kLB (r < m), the driven list in order round by round
+      const int m = a.m;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        const int k = tid + r * kLB;
+        if (r < m && k < a.nD) receive(a, S, k, nCur[r], a.N + k, slot);
+      }
+      lap(a, 1, tp);
+      // the draws in list order: one per non-refractory entry (lif.c:49-52). The first driven
+      // draw is state M^(nbg+1) s0; within round r, warp w's first live entry is draw
+      // (live entries of earlier rounds) + (live entries of round r before the warp) further, and
+      // its lanes step on by their rank among the warp's live entries (lane tables M^l).
+      const uint32_t lane = tid & 31u, warp = tid >> 5, ltMask = (1u << lane) - 1u;
+      uint64_t liveF = 0;  // 12-bit field r: entry r of this thread is live
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        const int k = tid + r * kLB;
+        if (r < m && k < a.nD && !(S.r[k] > 0)) liveF |= (uint64_t)1 << (12 * r);
+      }
+      uint64_t liveTot;
+      const uint64_t livePre = block_exclusive_scan(liveF, &liveTot, sh.scan64);
+      const uint32_t nbg = (uint32_t)sh.nbg;
+      const uint32_t totLive = (uint32_t)((liveTot & 0xfffu) + ((liveTot >> 12) & 0xfffu) +
+                                          ((liveTot >> 24) & 0xfffu) + ((liveTot >> 36) & 0xfffu));
+      if (lane == 0) {  // draw index of the warp's first live entry in each round
+        uint32_t rb = 0;
+        for (int r = 0; r < m; r++) {
+          sh.wfirst[r * 32 + warp] = rb + ((uint32_t)(livePre >> (12 * r)) & 0xfffu);
+          rb += (uint32_t)(liveTot >> (12 * r)) & 0xfffu;
+        }
+      }
+      __syncthreads();
+      if (warp == 0 && lane < (blockDim.x >> 5)) {  // warp 0: every warp's first state M^(nbg+1+first) s0
+        const uint32_t s0 = sh.rng;
+        for (int r = 0; r < m; r++) sh.wstate[r * 32 + lane] = xs_jump_hex(sHex, s0, nbg + 1u + sh.wfirst[r * 32 + lane]);
+      }
+      __syncthreads();
+      uint32_t nforced = 0, firedMask = 0, lastLive = 0, x = 0;
+      bool hasLast = false;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        if (r >= m) break;
+        const int k = tid + r * kLB;
+        const bool live = (liveF >> (12 * r)) & 1u;
+        const uint32_t wmask = __ballot_sync(0xffffffffu, live);
+        if (live) {  // live lanes have distinct ranks: each reads its own bank
+          const uint32_t rank = __popc(wmask & ltMask);
+          x = xs_apply_lane(sOff, rank, sh.wstate[r * 32 + warp]);
+          if (sh.wfirst[r * 32 + warp] + rank + 1 == totLive) {
+            hasLast = true;
+            lastLive = x;
+          }
+          const float u = __fmul_rn((float)(x >> 8), 1.0f / 16777216.0f);
+          if (u < __fmul_rn(S.drive[k], a.dtS)) {  // lif.c:52
+            S.v[k] = a.vReset;
+            S.r[k] = __fadd_rn(a.tRef, a.dt);
+            S.sc[k] += 1u;
+            S.tr[k] = 1.f;
+            S.ad[k] = __fadd_rn(S.ad[k], a.adaptInc);
+            firedMask |= 1u << r;
+            nforced++;
+          }
+        }
+      }
+      // the generator after the step: the state of the last draw, else after the nbg draws
+      if (totLive == 0) {
+        if (tid == 0) sh.rng = xs_jump_hex(sHex, sh.rng, nbg);
+      } else if (hasLast) {
+        sh.rng = lastLive;
+      }
+      lap(a, 2, tp);
+      uint32_t thrMask = 0;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        const int k = tid + r * kLB;
+        if (r < m && k < a.nD) {
+          const bool f = integrate(a, S, k);
+          if (f) {
+            thrMask |= 1u << r;
+          }
+          emit(a, S, k, f || ((firedMask >> r) & 1u));
+        }
+      }
+      // the step's spikes in any order, each with its rank key (the list position of a forced
+      // spike, nD + id of a threshold spike): sorted by key they are lif.c's fired order
+      uint4 *out = a.dbList + (int64_t)ring * a.nDcap * 2;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        const int k = tid + r * kLB;
+        const bool forced = (firedMask >> r) & 1u, thr = (thrMask >> r) & 1u;
+        if (forced || thr) {
+          const uint32_t e = atomicAdd(&sh.dbCount, 1u);
+          out[2 * e] = make_uint4((uint32_t)S.id[k], forced ? (uint32_t)k : (uint32_t)(a.nD + S.id[k]),
+                                  __float_as_uint(S.amp[k]), 0u);
+          out[2 * e + 1] = make_uint4(S.row0[k], S.row1[k], 0u, 0u);
+        }
+      }
+      __syncthreads();
+      lap(a, 3, tp);
+      if (tid == 0) {
+        const uint32_t n = sh.dbCount;
+        sh.dbCount = 0;
+        a.dbCnt[ring] = (int32_t)n;
+        if (a.log) atomicAdd(a.stepTot + s, (int32_t)n);
+        st_release(a.dbDone, (uint32_t)(s + 1));  // the list and count above
+        atomicAdd(a.done + ring, 1u);             // the driven block pushes nothing itself
+        if ((s & 7) == 7) {  // now and then: a later step known finished everywhere
+          const int probe = s - 2;
+          if (probe > sh.known && ld_acquire(a.done + (probe & (kLagRing - 1))) >= done_target(probe, gridDim.x))
+            sh.known = probe;
+        }
+      }
+      lap(a, 4, tp);
+      continue;
+    }
+
+    // ---------------- tile block ----------------
+    if (a.hasBg) collect_bg(a, sh, S, sBg, s, false);
+    uint64_t flags = 0;  // bit 16 r: neuron r of this thread crossed the threshold
+#pragma unroll
+    for (int r = 0; r < kMaxPer; r++) {
+      const int k = kOf(r);
+      if (r < per && k < nLocal) {
+        receive(a, S, k, nCur[r], (uint32_t)S.id[k], slot);
+        const bool f = integrate(a, S, k);
+        emit(a, S, k, f);
+        if (f) flags |= (uint64_t)1 << (16 * r);
+      }
+    }
+    // compaction in ascending local index: neurons r = 0 (k = tid) first, then r = 1, ...
+    uint32_t fired = 0;
+    if (__syncthreads_or(flags != 0)) {
+      uint64_t tot;
+      const uint64_t pos = block_exclusive_scan(flags, &tot, sh.scan64);
+      int32_t *st = a.tStage + ((int64_t)ring * a.nTB + b) * a.cap;
+      uint32_t before = 0;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        const uint32_t c = (uint32_t)(tot >> (16 * r)) & 0xffffu;
+        if ((flags >> (16 * r)) & 1u) st[before + ((uint32_t)(pos >> (16 * r)) & 0xffffu)] = kOf(r);
+        before += c;
+      }
+      fired = before;
+    }
+    lap(a, 6, tp);
+    // own spikes: one warp each, into the slot of step s + D
+    if (fired) {
+      __syncthreads();
+      const int32_t *st = a.tStage + ((int64_t)ring * a.nTB + b) * a.cap;
+      for (uint32_t w = tid >> 5; w < fired; w += blockDim.x >> 5) {
+        const int k = ldcg(st + w);
+        push_edges(a, S.row0[k], S.row1[k], (uint32_t)(a.nD + S.id[k]), S.amp[k], (s + a.D) % a.S);
+      }
+    }
+    lap(a, 7, tp);
+    // the driven block's spikes of step s - kHelp, shared out over the tile blocks
+    if (s >= kHelp) {
+      const int sp = s - kHelp, rp = sp & (kLagRing - 1);
+      if (tid == 0) {
+        bool ok = true;
+        if (dbKnown < (uint32_t)(sp + 1)) ok = wait_geq(a, a.dbDone, (uint32_t)(sp + 1), &dbKnown);
+        sh.stop = ok ? 0 : 1;
+      }
+      __syncthreads();
+      if (sh.stop) break;
+      const int nsp = ldcg(a.dbCnt + rp);
+      for (int e = b + a.nTB * (tid >> 5); e < nsp; e += a.nTB * (blockDim.x >> 5)) {
+        const uint4 x = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2);
+        const uint4 row = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2 + 1);
+        push_edges(a, row.x, row.y, x.y, __uint_as_float(x.z), (sp + a.D) % a.S);
+      }
+    }
+    if (tid == 0) {
+      a.tCnt[(int64_t)ring * a.nTB + b] = (int32_t)fired;
+      if (a.log && fired) atomicAdd(a.stepTot + s, (int32_t)fired);
+    }
+    __syncthreads();
+    lap(a, 8, tp);
+    if (tid == 0) {
+      red_release(a.done + ring, 1u);
+      if ((s & 7) == 7) {
+        const int probe = s - 2;
+        if (probe > sh.known && ld_acquire(a.done + (probe & (kLagRing - 1))) >= done_target(probe, gridDim.x))
+          sh.known = probe;
+      }
+    }
+    lap(a, 9, tp);
+  }
+
+  // ---------------- epilogue ----------------
+  __syncthreads();
+  const bool ok = lag_grid_sync(a);
+  if (!ok) return;
+  for (int k = tid; k < nLocal; k += blockDim.x) {
+    const int32_t i = S.id[k];
+    a.v[i] = S.v[k];
+    a.gE[i] = S.ge[k];
+    a.gI[i] = S.gi[k];
+    a.refr[i] = S.r[k];
+    a.trace[i] = S.tr[k];
+    a.adapt[i] = S.ad[k];
+    a.res[i] = S.rs[k];
+    a.spikeCount[i] = S.sc[k];
+  }
+  // slots delivered during the launch are empty (lif.c:44) unless refilled below
+  if (drivenBlock)
+    for (int u = tid; u < min(a.T, ns); u += blockDim.x) a.ringCount[(head0 + u) % ns] = 0;
+  if (!lag_grid_sync(a)) return;
+  if (tid == 0) sh.dbCount = 0;
+  __syncthreads();
+  // fired lists (lif.c:77-79), one block per step: the last D steps into their ring slots (the
+  // arrivals still in flight), and with logging every step of the launch into the log
+  const int first = a.log ? 0 : max(0, a.T - a.D);
+  for (int s = first + (int)blockIdx.x; s < a.T; s += gridDim.x) {
+    const int ring = s & (kLagRing - 1);
+    const int rslot = (head0 + s + ns - 1) % ns;
+    const bool toRing = s >= a.T - a.D;
+    int32_t *out = a.ring + (int64_t)rslot * a.N;
+    const int nDB = ldcg(a.dbCnt + ring);
+    const uint4 *dl = a.dbList + (int64_t)ring * a.nDcap * 2;  // entry e at dl[2 e], any order
+    // the driven block's spikes in key order into sThr (ids): forced (key < nD) in list order,
+    // then threshold spikes by ascending id
+    for (int e = tid; e < nDB; e += blockDim.x) {
+      const uint4 x = ldcg(dl + 2 * e);
+      uint32_t rank = 0;
+      for (int o = 0; o < nDB; o++) rank += ldcg(dl + 2 * o).y < x.y ? 1u : 0u;
+      sThr[rank] = (int32_t)x.x;
+      if (x.y < (uint32_t)a.nD) atomicAdd(&sh.dbCount, 1u);
+    }
+    __syncthreads();
+    const int nF = (int)sh.dbCount;
+    int32_t *tOff = (int32_t *)sBg;  // tile spike prefix over tile blocks (nTB + 1 <= kBgChunk)
+    uint32_t carry = 0;
+    for (int t0 = 0; t0 < a.nTB; t0 += blockDim.x) {
+      const int t = t0 + tid;
+      const uint32_t c = t < a.nTB ? (uint32_t)ldcg(a.tCnt + (int64_t)ring * a.nTB + t) : 0u;
+      uint32_t tot;
+      const uint32_t pre = block_exclusive_scan(c, &tot, sh.scan);
+      if (t < a.nTB) tOff[t] = (int32_t)(carry + pre);
+      carry += tot;
+    }
+    if (tid == 0) {
+      tOff[a.nTB] = (int32_t)carry;
+      int64_t rb = 0;
+      if (a.log) {  // launches with logging have at most kLagRing steps
+        rb = ldcg(&a.G->logRasterLen[steps0 & 1]);
+        for (int x = 0; x < s; x++) rb += ldcg(a.stepTot + x);
+      }
+      sh.logBase = rb;
+    }
+    __syncthreads();
+    const int64_t rbase = sh.logBase;
+    const bool logR = a.log && a.logRaster != nullptr;
+    auto put = [&](int k, int32_t id) {
+      if (toRing) out[k] = id;
+      if (logR && rbase + k < a.logRasterCap) a.logRaster[rbase + k] = id;
+    };
+    const int nDT = nDB - nF;
+    for (int k = tid; k < nF; k += blockDim.x) put(k, sThr[k]);
+    // driven threshold spikes (ascending) merged with the tile spikes (ascending)
+    for (int j = tid; j < nDT; j += blockDim.x) {
+      const int32_t y = sThr[nF + j];
+      int32_t below = 0;
+      for (int t = 0; t < a.nTB; t++) {
+        const int lo0 = a.ndLo[t], hi0 = a.ndLo[t + 1];
+        if (hi0 == lo0) continue;
+        if (a.ndIds[lo0] > y) break;
+        const int n = tOff[t + 1] - tOff[t];
+        const int32_t *st = a.tStage + ((int64_t)ring * a.nTB + t) * a.cap;
+        int lo = 0, hi = n;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (a.ndIds[lo0 + ldcg(st + mid)] < y) lo = mid + 1;
+          else hi = mid;
+        }
+        below += lo;
+      }
+      put(nF + j + below, y);
+    }
+    for (int t = 0; t < a.nTB; t++) {
+      const int n = tOff[t + 1] - tOff[t];
+      const int32_t *st = a.tStage + ((int64_t)ring * a.nTB + t) * a.cap;
+      const int lo0 = a.ndLo[t];
+      for (int p = tid; p < n; p += blockDim.x) {
+        const int32_t y = a.ndIds[lo0 + ldcg(st + p)];
+        int lo = 0, hi = nDT;  // driven threshold spikes below y
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (sThr[nF + mid] < y) lo = mid + 1;
+          else hi = mid;
+        }
+        put(nF + tOff[t] + p + lo, y);
+      }
+    }
+    if (tid == 0) {
+      const int total = nDB + (int)carry;
+      if (toRing) a.ringCount[rslot] = total;
+      if (a.log && a.logCount) {
+        const int64_t lb = steps0 + s - ldcg(&a.G->logStart);
+        if (lb >= 0 && lb < a.logCap) a.logCount[lb] = total;
+      }
+      if (s == a.T - 1) {
+        a.G->nFired = total;
+        a.G->lastSlot = rslot;
+        if (a.log && a.logRaster) a.G->logRasterLen[(steps0 + a.T) & 1] = rbase + total;
+      }
+      sh.dbCount = 0;
+    }
+    __syncthreads();
+  }
+  if (drivenBlock && tid == 0) {
+    const int64_t g = steps0 + a.T;
+    a.G->head = (head0 + a.T) % ns;
+    a.G->stepsDone = g;
+    a.G->rngP[g & 1] = sh.rng;
+    a.G->bgAccP[g & 1] = sh.bgAcc;
+  }
+}
+
+// ---- host side -------------------------------------------------------------------------------
+
+namespace {
+// 32x32 matrices over GF(2) by columns: col[b] = A e_b.
+uint32_t mat_apply(const uint32_t *col, uint32_t x) {
+  uint32_t y = 0;
+  for (int b = 0; b < 32; b++)
+    if (x >> b & 1u) y ^= col[b];
+  return y;
+}
+void mat_mul(const uint32_t *A, const uint32_t *B, uint32_t *C) {  // C = A B
+  uint32_t t[32];
+  for (int b = 0; b < 32; b++) t[b] = mat_apply(A, B[b]);
+  for (int b = 0; b < 32; b++) C[b] = t[b];
+}
+uint32_t nibble_entry(const uint32_t *col, int n, uint32_t v) {
+  uint32_t y = 0;
+  for (int b = 0; b < 4; b++)
+    if (v >> b & 1u) y ^= col[4 * n + b];
+  return y;
+}
+}  // namespace
+
+void lagged_jump_tables(std::vector<uint32_t> &tab) {
+  tab.assign(kHexWords + kOffWords, 0);
+  uint32_t M[32], I[32];
+  for (int b = 0; b < 32; b++) {
+    uint32_t x = 1u << b;  // one xorshift32 step (src/wasm/lif.c:27) is linear over GF(2)
+    x ^= x << 13;
+    x ^= x >> 17;
+    x ^= x << 5;
+    M[b] = x;
+    I[b] = 1u << b;
+  }
+  uint32_t P[32];  // M^(16^i)
+  memcpy(P, M, sizeof P);
+  for (int i = 0; i < kHexLevels; i++) {
+    uint32_t A[32];
+    memcpy(A, P, sizeof A);  // M^(v 16^i), v = 1..15
+    for (int v = 1; v <= 15; v++) {
+      for (int n = 0; n < 8; n++)
+        for (uint32_t x = 0; x < 16; x++) tab[(i * 15 + v - 1) * 128 + n * 16 + x] = nibble_entry(A, n, x);
+      mat_mul(A, P, A);
+    }
+    for (int r = 0; r < 4; r++) mat_mul(P, P, P);  // M^(16^(i+1))
+  }
+  for (int n = 0; n < 8; n++)  // M^(16^kHexLevels)
+    for (uint32_t x = 0; x < 16; x++) tab[kHexLevels * 15 * 128 + n * 16 + x] = nibble_entry(P, n, x);
+  uint32_t A[32];
+  memcpy(A, I, sizeof A);  // M^l, l = 0..31
+  for (int l = 0; l < 32; l++) {
+    for (int n = 0; n < 8; n++)
+      for (uint32_t x = 0; x < 16; x++) tab[kHexWords + ((uint32_t)n * 16 + x) * 32 + l] = nibble_entry(A, n, x);
+    mat_mul(M, A, A);
+  }
+}
+
+__global__ void edge_records_kernel(const uint32_t *indices, const uint32_t *inOff, const int32_t *posOf,
+                                    int32_t N, int64_t E, uint4 *out) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < E; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = indices[j];
+    const int32_t p = posOf[q];
+    out[j] = make_uint4(p >= 0 ? (uint32_t)(N + p) : q, inOff[q], inOff[q + 1], 0u);
+  }
+}
+
+cudaError_t launch_edge_records(const uint32_t *indices, const uint32_t *inOff, const int32_t *posOf, int32_t N,
+                                int64_t E, uint4 *out, cudaStream_t st) {
+  if (E > 0) edge_records_kernel<<<1024, 256, 0, st>>>(indices, inOff, posOf, N, E, out);
+  return cudaGetLastError();
+}
+
+size_t lagged_smem_bytes(int cap, int nDcap) {
+  const int c = cap > nDcap ? cap : nDcap;
+  return (size_t)kStateWords * 4 * c + (size_t)(kBgChunk + kHexWords + kOffWords) * 4 + (size_t)4 * nDcap;
+}
+
+int lagged_blocks_per_sm(size_t smem) {
+  if (cudaFuncSetAttribute(lagged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lagged_kernel, kLB, smem) != cudaSuccess) return 0;
+  return n;
+}
+
+cudaError_t launch_lagged(const LagArgs &a, int grid, size_t smem, cudaStream_t st) {
+  void *args[] = {(void *)&a};
+  return cudaLaunchCooperativeKernel((const void *)lagged_kernel, dim3(grid), dim3(kLB), args, smem, st);
+}
+
+}  // namespace fb

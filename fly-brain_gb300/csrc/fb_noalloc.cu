@@ -28,6 +28,7 @@ namespace fb {
 int step_kernel_blocks_per_sm(size_t smem);
 size_t step_smem_bytes(int B);
 cudaError_t launch_step(const StepArgs &a, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_rebuild_slots(Trial *Td, int nslots, int32_t *err, cudaStream_t st);
 void host_jump_tables(std::vector<uint32_t> &tab);
 int set_error(int code, const char *msg);
 }  // namespace fb
@@ -96,53 +97,6 @@ struct DeviceSetup {
 };
 std::mutex g_mu;
 DeviceSetup g_dev[64];
-
-// Rebuilds, for every ring slot, the per-arrival edge offsets and row starts, the slot's edge
-// total and its delivery work-item records from the caller's ring lists (one block per slot).
-__global__ void rebuild_slots_kernel(Trial *Tp, int32_t *err) {
-  __shared__ uint32_t scan[33];
-  const Trial &T = *Tp;
-  const int slot = blockIdx.x, tid = threadIdx.x;
-  const int N = T.N;
-  const int32_t na = T.ringCount[slot];
-  if (na < 0 || na > N) {
-    if (tid == 0) atomicCAS(err, 0, FB_EINVAL);
-    return;
-  }
-  const int32_t *list = T.ring + (int64_t)slot * N;
-  uint32_t *off = T.ringOff + (int64_t)slot * (N + 1);
-  uint32_t *row = T.ringRow + (int64_t)slot * N;
-  uint4 *chunkK = T.chunkK + (int64_t)slot * T.chunkCap;
-  uint32_t carry = 0;
-  for (int32_t k0 = 0; k0 < na; k0 += blockDim.x) {
-    const int32_t k = k0 + tid;
-    int32_t i = 0;
-    uint32_t r0 = 0, deg = 0;
-    if (k < na) {
-      i = list[k];
-      if (i < 0 || i >= N) {
-        atomicCAS(err, 0, FB_EINVAL);
-        i = 0;
-      } else {
-        r0 = T.indptr[i];
-        deg = T.indptr[i + 1] - r0;
-      }
-    }
-    uint32_t tot;
-    const uint32_t pre = block_exclusive_scan(deg, &tot, scan);
-    if (k < na) {
-      const uint32_t o = carry + pre;
-      off[k] = o;
-      row[k] = r0;
-      mark_chunks(chunkK, o, deg, (uint32_t)k, (uint32_t)i, r0);
-    }
-    carry += tot;
-  }
-  if (tid == 0) {
-    off[na] = carry;
-    T.slotEdges[slot] = carry;
-  }
-}
 
 int fail_na(int code, const char *fmt, ...) {
   char buf[512];
@@ -267,8 +221,7 @@ extern "C" int fb_lif_step_noalloc(fb_brain_view *v, int32_t nsteps, void *strea
   NA_CU(cudaMemsetAsync(B + L.liveTag, 0, (size_t)T.maxDch * 8, st));
   NA_CU(cudaMemcpyAsync(Td, &T, sizeof T, cudaMemcpyHostToDevice, st));
   NA_CU(cudaMemcpyAsync(B + L.steps, &nsteps, 4, cudaMemcpyHostToDevice, st));
-  rebuild_slots_kernel<<<v->nslots, kBlock, 0, st>>>(Td, errd);
-  NA_CU(cudaGetLastError());
+  NA_CU(launch_rebuild_slots(Td, v->nslots, errd, st));
 
   StepArgs a;
   memset(&a, 0, sizeof a);

@@ -12,6 +12,7 @@ from . import builder as _build
 FB_OK = 0
 FB_EINVAL, FB_ECUDA, FB_ENOMEM, FB_ETIMEOUT, FB_EOVERFLOW, FB_ESTATE, FB_ENODEV = -1, -2, -3, -4, -5, -6, -7
 FB_DELIVER_EXACT, FB_DELIVER_SEQUENTIAL, FB_DELIVER_FAST = 0, 1, 2
+FB_SCHEDULE_AUTO, FB_SCHEDULE_GRID, FB_SCHEDULE_LAGGED = 0, 1, 2
 FIELDS = {"v": 0, "gE": 1, "gI": 2, "refr": 3, "trace": 4, "adapt": 5, "res": 6, "bias": 7,
           "thr": 8, "drive": 9, "spikeCount": 10}
 
@@ -108,6 +109,8 @@ SIGNATURES = {
     "fb_diff_tape": (C.c_int, [P, P, P, P, I64, PI64]),
     "fb_diff_raster": (C.c_int, [P, I32, P, P]),
     "fb_diff_backward": (C.c_int, [P, P, I32, P, I32, I32, C.POINTER(FbDiffGrads)]),
+    "fb_brains_set_schedule": (C.c_int, [P, I32]),
+    "fb_last_schedule": (C.c_int, [P, C.POINTER(C.c_int32)]),
     "fb_diff_batch_create": (C.c_int, [C.POINTER(FbDiffNet), I32, I64, C.POINTER(P)]),
     "fb_diff_batch_destroy": (C.c_int, [P]),
     "fb_diff_batch_set": (C.c_int, [P, I32, I32, P]),

@@ -146,6 +146,15 @@ class BrainBatch:
     def set_mode(self, mode: int):
         nat.check(self.L.fb_brains_set_mode(self.h, int(mode)))
 
+    def set_schedule(self, schedule: int):
+        """FB_SCHEDULE_AUTO / _GRID / _LAGGED (fb_brains_set_schedule)."""
+        nat.check(self.L.fb_brains_set_schedule(self.h, int(schedule)))
+
+    def last_schedule(self) -> int:
+        x = C.c_int32()
+        nat.check(self.L.fb_last_schedule(self.h, C.byref(x)))
+        return x.value
+
     def step(self, nsteps: int = 1) -> np.ndarray:
         out = np.zeros(self.B, dtype=np.int32)
         nat.check(self.L.fb_step(self.h, int(nsteps), nat.ptr(out)))

@@ -54,7 +54,9 @@ def synth_graph(N: int, seed: int, mu: float = 3.5, sigma: float = 1.2, max_deg:
     near = (pre + rng.integers(-half, half + 1, tot)) % N
     far = rng.integers(0, N, tot)
     post = np.where(local, near, far)
-    key = np.unique(pre * N + post)  # merges duplicates; sorted by (pre, post)
+    key = pre * N + post
+    key.sort()
+    key = key[np.concatenate(([True], key[1:] != key[:-1]))]  # merges duplicates; sorted by (pre, post)
     pre = key // N
     post = key % N
     E = key.shape[0]

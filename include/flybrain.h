@@ -134,6 +134,20 @@ int fb_brains_destroy(fb_brains *br);
 /* Delivery mode for all brains of the batch (FB_DELIVER_*). */
 int fb_brains_set_mode(fb_brains *br, int32_t mode);
 
+/* Kernel schedules of fb_step (both exact). No counterpart in the reference, whose lif_step is a
+ * serial loop. GRID: the persistent two-phase kernel with two grid barriers per step (any batch,
+ * mode and logging). LAGGED: for one brain in exact mode without presynaptic inhibition, blocks
+ * synchronise only at the synaptic delay (nslots - 1 >= 3 steps; per-step logging only in
+ * launches of at most 64 steps). AUTO (default) takes LAGGED where it applies and the launch has
+ * at least 16 steps, GRID otherwise; forcing LAGGED where it does not apply fails with
+ * FB_EINVAL at fb_step. */
+#define FB_SCHEDULE_AUTO 0
+#define FB_SCHEDULE_GRID 1
+#define FB_SCHEDULE_LAGGED 2
+int fb_brains_set_schedule(fb_brains *br, int32_t schedule);
+/* The schedule the last fb_step / fb_step_uneven launch ran (FB_SCHEDULE_GRID or _LAGGED). */
+int fb_last_schedule(fb_brains *br, int32_t *schedule);
+
 /* Advances every brain by nsteps steps in one persistent launch (lif_step, src/wasm/lif.c:29-80,
  * nsteps times). out_nfired (optional, int32[B]) receives each brain's fired count of its last
  * step: the value lif_step returns. */
@@ -197,7 +211,11 @@ int fb_last_step_ms(fb_brains *br, float *ms);
  * [3] the neuron update, [4] the wait at the second barrier; within [0], for the brain block 0
  * serves: [5] the header and background draws, [6] the driven-list gathers, [7] the draws,
  * [8] the forced spikes' emission, [9] the RNG advance. fb_phase_times copies up to n
- * accumulated totals in ms. */
+ * accumulated totals in ms. With the schedule forced to FB_SCHEDULE_LAGGED the delay-scheduled
+ * kernel runs instead (AUTO takes the grid kernel while profiling) and the slots hold: the driven
+ * block's [0] lag wait, [1] background and delivery, [2] draws, [3] update and spike list,
+ * [4] completion signal; tile block 1's [5] lag wait, [6] delivery, update and compaction, [7] own
+ * spikes' pushes, [8] the driven spikes' pushes (with their wait), [9] completion signal. */
 #define FB_NPHASES 10
 int fb_profile(fb_brains *br, int32_t on);
 int fb_phase_times(fb_brains *br, double *ms, int32_t n);
