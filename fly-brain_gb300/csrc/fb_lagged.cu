@@ -61,6 +61,8 @@ struct LagShared {
   uint32_t wfirst[kMaxPer * 32];  // driven block: first live rank of each warp and round
   uint32_t wstate[kMaxPer * 32];  // ... and the generator state there
   uint32_t dbCount;               // driven block: spikes of the step
+  uint32_t rngNext;               // driven block: generator state after the step
+  uint32_t cstate[kMaxPer * kLagThreads / 32];  // driven block: state at every 32nd draw
 };
 
 __device__ __forceinline__ bool lag_timeout(const LagArgs &a, uint64_t t0, uint32_t &it) {
@@ -531,6 +533,22 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     }
     __syncthreads();
     if (sh.stop) break;
+    // step s - 1 is complete in this block (the barrier above): its completion is published now,
+    // so the release's wait for the block's writes overlaps this step's work
+    if (tid == 0 && s > 0) {
+      const int sp = s - 1;
+      if (drivenBlock) {
+        st_release(a.dbDone, (uint32_t)s);  // the spike list and count of step s - 1
+        atomicAdd(a.done + (sp & (kLagRing - 1)), 1u);  // the driven block pushes nothing itself
+      } else {
+        red_release(a.done + (sp & (kLagRing - 1)), 1u);
+      }
+      if ((sp & 7) == 7) {  // now and then: a later step known finished everywhere
+        const int probe = sp - 2;
+        if (probe > sh.known && ld_acquire(a.done + (probe & (kLagRing - 1))) >= done_target(probe, gridDim.x))
+          sh.known = probe;
+      }
+    }
     lap(a, pb + 0, tp);
     // this step's counts (prefetched when the lag allowed it), and the next step's
     uint32_t nCur[kMaxPer];
@@ -571,8 +589,22 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       } else if (tid == 0) {
         sh.nbg = 0;
       }
-      // entries k = tid + r * kLB (r < m), the driven list in order round by round
+      // generator states at every 32nd driven draw: C_q = M^(32 q) B0, B0 = M^(nbg+1) s0 (the first
+      // driven draw). The last warp computes them while the others start on the deliveries; its
+      // lane j takes q = j, 32 + j, 64 + j, 96 + j.
       const int m = a.m;
+      if ((int)tid >= (int)blockDim.x - 32) {  // the last warp (thread 0 publishes completion)
+        const uint32_t j = tid & 31u;
+        const uint32_t nbg0 = a.hasBg ? (uint32_t)sh.nbg : 0u;  // published before a barrier
+        const uint32_t b0 = xs_jump_hex(sHex, sh.rng, nbg0 + 1u);
+        const uint32_t nq = (uint32_t)(a.nD + 31) / 32;
+        uint32_t c = xs_jump_hex(sHex, b0, 32u * j);
+        for (uint32_t q = j; q < nq; q += 32) {
+          sh.cstate[q] = c;
+          c = xs_apply(sHex + (2 * 15 + 4 - 1) * 128, c);  // M^1024 = M^(4 * 16^2)
+        }
+      }
+      // entries k = tid + r * kLB (r < m), the driven list in order round by round
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         const int k = tid + r * kLB;
@@ -584,42 +616,42 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       // (live entries of earlier rounds) + (live entries of round r before the warp) further, and
       // its lanes step on by their rank among the warp's live entries (lane tables M^l).
       const uint32_t lane = tid & 31u, warp = tid >> 5, ltMask = (1u << lane) - 1u;
-      uint64_t liveF = 0;  // 12-bit field r: entry r of this thread is live
+      const uint32_t nwarps = blockDim.x >> 5;
+      // live entries per warp and round (ballots), then each warp finds its place from the
+      // per-warp counts: one barrier
+      uint32_t liveMask = 0;  // bit r: entry r of this thread is live
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         const int k = tid + r * kLB;
-        if (r < m && k < a.nD && !(S.r[k] > 0)) liveF |= (uint64_t)1 << (12 * r);
+        const bool live = r < m && k < a.nD && !(S.r[k] > 0);
+        const uint32_t wm = __ballot_sync(0xffffffffu, live);
+        if (live) liveMask |= 1u << r;
+        if (lane == 0 && r < m) sh.wfirst[r * 32 + warp] = __popc(wm);
       }
-      uint64_t liveTot;
-      const uint64_t livePre = block_exclusive_scan(liveF, &liveTot, sh.scan64);
+      __syncthreads();
       const uint32_t nbg = (uint32_t)sh.nbg;
-      const uint32_t totLive = (uint32_t)((liveTot & 0xfffu) + ((liveTot >> 12) & 0xfffu) +
-                                          ((liveTot >> 24) & 0xfffu) + ((liveTot >> 36) & 0xfffu));
-      if (lane == 0) {  // draw index of the warp's first live entry in each round
-        uint32_t rb = 0;
-        for (int r = 0; r < m; r++) {
-          sh.wfirst[r * 32 + warp] = rb + ((uint32_t)(livePre >> (12 * r)) & 0xfffu);
-          rb += (uint32_t)(liveTot >> (12 * r)) & 0xfffu;
-        }
+      uint32_t totLive = 0, wfirst[kMaxPer];
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        wfirst[r] = totLive;
+        if (r >= m) continue;
+        const uint32_t v = lane < nwarps ? sh.wfirst[r * 32 + lane] : 0u;
+        wfirst[r] = totLive + __reduce_add_sync(0xffffffffu, lane < warp ? v : 0u);
+        totLive += __reduce_add_sync(0xffffffffu, v);
       }
-      __syncthreads();
-      if (warp == 0 && lane < (blockDim.x >> 5)) {  // warp 0: every warp's first state M^(nbg+1+first) s0
-        const uint32_t s0 = sh.rng;
-        for (int r = 0; r < m; r++) sh.wstate[r * 32 + lane] = xs_jump_hex(sHex, s0, nbg + 1u + sh.wfirst[r * 32 + lane]);
-      }
-      __syncthreads();
       uint32_t nforced = 0, firedMask = 0, lastLive = 0, x = 0;
       bool hasLast = false;
+      const uint32_t s0 = sh.rng;
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         if (r >= m) break;
         const int k = tid + r * kLB;
-        const bool live = (liveF >> (12 * r)) & 1u;
+        const bool live = (liveMask >> r) & 1u;
         const uint32_t wmask = __ballot_sync(0xffffffffu, live);
-        if (live) {  // live lanes have distinct ranks: each reads its own bank
-          const uint32_t rank = __popc(wmask & ltMask);
-          x = xs_apply_lane(sOff, rank, sh.wstate[r * 32 + warp]);
-          if (sh.wfirst[r * 32 + warp] + rank + 1 == totLive) {
+        if (live) {  // draw p = its rank among all live entries: M^(p mod 32) C_(p / 32)
+          const uint32_t rank = __popc(wmask & ltMask), p = wfirst[r] + rank;
+          x = xs_apply_lane(sOff, p & 31u, sh.cstate[p >> 5]);  // lanes hold distinct p mod 32
+          if (p + 1 == totLive) {
             hasLast = true;
             lastLive = x;
           }
@@ -637,9 +669,9 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       }
       // the generator after the step: the state of the last draw, else after the nbg draws
       if (totLive == 0) {
-        if (tid == 0) sh.rng = xs_jump_hex(sHex, sh.rng, nbg);
+        if (tid == 0) sh.rngNext = xs_jump_hex(sHex, s0, nbg);
       } else if (hasLast) {
-        sh.rng = lastLive;
+        sh.rngNext = lastLive;
       }
       lap(a, 2, tp);
       uint32_t thrMask = 0;
@@ -671,17 +703,11 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       __syncthreads();
       lap(a, 3, tp);
       if (tid == 0) {
+        sh.rng = sh.rngNext;
         const uint32_t n = sh.dbCount;
         sh.dbCount = 0;
         a.dbCnt[ring] = (int32_t)n;
         if (a.log) atomicAdd(a.stepTot + s, (int32_t)n);
-        st_release(a.dbDone, (uint32_t)(s + 1));  // the list and count above
-        atomicAdd(a.done + ring, 1u);             // the driven block pushes nothing itself
-        if ((s & 7) == 7) {  // now and then: a later step known finished everywhere
-          const int probe = s - 2;
-          if (probe > sh.known && ld_acquire(a.done + (probe & (kLagRing - 1))) >= done_target(probe, gridDim.x))
-            sh.known = probe;
-        }
       }
       lap(a, 4, tp);
       continue;
@@ -749,15 +775,6 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     }
     __syncthreads();
     lap(a, 8, tp);
-    if (tid == 0) {
-      red_release(a.done + ring, 1u);
-      if ((s & 7) == 7) {
-        const int probe = s - 2;
-        if (probe > sh.known && ld_acquire(a.done + (probe & (kLagRing - 1))) >= done_target(probe, gridDim.x))
-          sh.known = probe;
-      }
-    }
-    lap(a, 9, tp);
   }
 
   // ---------------- epilogue ----------------
