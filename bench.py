@@ -34,9 +34,16 @@ import numpy as np  # noqa: E402
 METRIC = "synaptic events/s & sim-s/wall-s at 165k LIF; batched fwd+adjoint vs plain fwd"
 BRAIN_STEPS_PER_BENCH_STEP = int(os.environ.get("FB_BRAIN_STEPS", "1000"))
 L2_FLUSH_BYTES = 512 << 20
-# DRAM bytes (read + write) per brain step of the single-trial full-scale step kernel, from one
-# ncu capture of a 100-step launch (16.83 MB); traffic grows in proportion to steps.
-DRAM_BYTES_PER_STEP_SINGLE = 16.826112e6 / 100
+# DRAM bytes (read + write) per brain step of the single-trial full-scale launch, from one ncu
+# capture of a 100-step launch of each kernel (profiles/); traffic grows in proportion to steps.
+DRAM_BYTES_PER_STEP_SINGLE = {
+    "grid": 16.826112e6 / 100,    # fb::step_kernel
+    "lagged": 53.68704e6 / 100,   # fb::lagged_kernel
+}
+KERNEL_NAME = {
+    "grid": "fb::step_kernel (persistent, two grid barriers per step)",
+    "lagged": "fb::lagged_kernel (persistent, delay-scheduled)",
+}
 
 
 def peaks():
@@ -207,6 +214,8 @@ def run_ours(args, rank, world):
     e2e_events = sum_over_ranks(e2e_events, world)
 
     peak, kind = peaks()
+    from flybrain import _native as nat
+    sched = "lagged" if brain._batch.last_schedule() == nat.FB_SCHEDULE_LAGGED else "grid"
     per_launch_bytes = algorithmic_bytes(g.N, S, spikes / args.steps, events / args.steps)
     achieved = per_launch_bytes / (np.mean(launch_ms) / 1e3) / 1e9
     res = dict(
@@ -224,11 +233,12 @@ def run_ours(args, rank, world):
         events=tot_events,
         e2e=dict(value=e2e_events / e2e_s, unit="synaptic events/s", h2d_bytes_per_step=h2d // args.steps,
                  d2h_bytes_per_step=d2h // args.steps, sim_s_per_wall_s=sim_s / e2e_s),
-        gpu_launches=args.steps,
+        # the lagged schedule launches the step kernel and the ring bookkeeping kernel
+        gpu_launches=args.steps * (2 if sched == "lagged" else 1),
+        schedule=sched,
         roofline=dict(bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
-                      peak_kind=kind, traffic=DRAM_BYTES_PER_STEP_SINGLE * S,
-                      kernel="fb::step_kernel (persistent, all phases)",
-                      algorithmic_bytes_per_launch=per_launch_bytes),
+                      peak_kind=kind, traffic=DRAM_BYTES_PER_STEP_SINGLE[sched] * S,
+                      kernel=KERNEL_NAME[sched], algorithmic_bytes_per_launch=per_launch_bytes),
         clocks=clk.summary(),
     )
     if os.environ.get("FB_BENCH_ADJOINT", "1") == "1":

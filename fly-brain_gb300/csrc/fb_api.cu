@@ -898,6 +898,7 @@ static int run_lagged(fb_brains *br, int32_t steps) {
   LagRes &R = br->lag;
   Trial &T = br->host[0];
   const int N = T.N;
+  CU(cudaEventRecord(br->ev0, br->stream));  // the launch's clearing is part of its time
   CU(cudaMemsetAsync(R.sync, 0, 256 * 4, br->stream));
   CU(cudaMemsetAsync(R.cnt, 0, (size_t)R.S * (N + R.nDmax) * 4, br->stream));
   CU(cudaMemsetAsync(R.pend0, 0, (size_t)N * 4, br->stream));
@@ -938,7 +939,6 @@ static int run_lagged(fb_brains *br, int32_t steps) {
   a.edgeRec = R.edgeRec;
   a.err = br->d_err;
   a.timeoutNs = 5000000000LL;
-  CU(cudaEventRecord(br->ev0, br->stream));
   CU(launch_lagged(a, R.grid, R.smem, br->stream));
   CU(launch_rebuild_slots(br->trials, T.nslots, br->d_err, br->stream));
   CU(cudaEventRecord(br->ev1, br->stream));

@@ -284,7 +284,7 @@ __device__ __forceinline__ LagState carve(unsigned char *sm, int cap) {
 // contributions, then background hits (lif.c:48), then the neuron's own depression if its spike
 // arrives now (lif.c:37-39).
 __device__ __forceinline__ void receive(const LagArgs &a, const LagState &S, int k, uint32_t n, uint32_t ci,
-                                        int slot) {
+                                        int slot, bool haveE, uint2 e0) {
   float ge = S.ge[k], gi = S.gi[k];
   if (n) {
     const uint32_t deg = S.deg[k];
@@ -292,7 +292,12 @@ __device__ __forceinline__ void receive(const LagArgs &a, const LagState &S, int
       atomicCAS(a.err, 0, FB_EOVERFLOW);
       n = deg;
     }
-    apply_slot(a, a.buf + (int64_t)slot * a.E + S.off[k], n, ge, gi);
+    if (n == 1 && haveE) {  // the prefetched entry
+      if (e0.x & 1u) gi = __fadd_rn(gi, __uint_as_float(e0.y));
+      else ge = __fadd_rn(ge, __uint_as_float(e0.y));
+    } else {
+      apply_slot(a, a.buf + (int64_t)slot * a.E + S.off[k], n, ge, gi);
+    }
     a.cnt[(int64_t)slot * a.cntStride + ci] = 0;
   }
   const uint32_t h = S.hits[k];
@@ -511,8 +516,12 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   auto kOf = [&](int r) { return tid + r * kLB; };
   // count slot of local neuron k: driven neurons have their own slots after the N neuron ids
   auto cOf = [&](int k) { return drivenBlock ? (uint32_t)(a.N + k) : (uint32_t)S.id[k]; };
-  uint32_t nNext[kMaxPer];  // contribution counts of the next step, loaded one step ahead
-  bool haveNext = false;
+  // contribution counts are loaded two steps ahead and, where a neuron has one, its first bucket
+  // entry one step ahead (the lag guarantees those buckets are complete): nA / eA hold step s's,
+  // nB step s + 1's
+  uint32_t nA[kMaxPer], nB[kMaxPer];
+  uint2 eA[kMaxPer];
+  bool haveA = false, haveB = false;
   uint32_t dbKnown = 0;     // tile blocks: driven-block steps known finished (thread 0)
   uint64_t tp = a.prof != nullptr ? global_ns() : 0;
   const int pb = drivenBlock ? 0 : 5;  // phase slots of this block
@@ -534,8 +543,9 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     __syncthreads();
     if (sh.stop) break;
     // step s - 1 is complete in this block (the barrier above): its completion is published now,
-    // so the release's wait for the block's writes overlaps this step's work
-    if (tid == 0 && s > 0) {
+    // so the release's wait for the block's writes overlaps this step's work. The publishing
+    // thread is in the second-last warp, which has the fewest neurons (thread 0 checks the lag).
+    if ((int)tid == (int)blockDim.x - 64 && s > 0) {
       const int sp = s - 1;
       if (drivenBlock) {
         st_release(a.dbDone, (uint32_t)s);  // the spike list and count of step s - 1
@@ -550,21 +560,34 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       }
     }
     lap(a, pb + 0, tp);
-    // this step's counts (prefetched when the lag allowed it), and the next step's
+    // this step's counts and first entries (prefetched when the lag allowed it)
     uint32_t nCur[kMaxPer];
+    uint2 eCur[kMaxPer];
+    const bool haveE = haveA;
 #pragma unroll
     for (int r = 0; r < kMaxPer; r++) {
       const int k = kOf(r);
-      nCur[r] = haveNext ? nNext[r]
-                         : ((r < per && k < nLocal) ? ldcg(a.cnt + (int64_t)slot * a.cntStride + cOf(k)) : 0u);
+      nCur[r] = haveA ? nA[r] : ((r < per && k < nLocal) ? ldcg(a.cnt + (int64_t)slot * a.cntStride + cOf(k)) : 0u);
+      eCur[r] = eA[r];
     }
-    haveNext = s + 1 < a.T && sh.known >= s + 1 - a.L;
-    if (haveNext) {
+    // step s + 1: its counts (loaded last step) and their first entries
+    haveA = haveB && s + 1 < a.T;
+    if (haveA) {
       const int slot1 = (s + 1) % a.S;
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
+        nA[r] = nB[r];
+        if (nB[r]) eA[r] = ldcg(a.buf + (int64_t)slot1 * a.E + S.off[kOf(r)]);
+      }
+    }
+    // step s + 2: its counts
+    haveB = s + 2 < a.T && sh.known >= s + 2 - a.L;
+    if (haveB) {
+      const int slot2 = (s + 2) % a.S;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
         const int k = kOf(r);
-        nNext[r] = (r < per && k < nLocal) ? ldcg(a.cnt + (int64_t)slot1 * a.cntStride + cOf(k)) : 0u;
+        nB[r] = (r < per && k < nLocal) ? ldcg(a.cnt + (int64_t)slot2 * a.cntStride + cOf(k)) : 0u;
       }
     }
 
@@ -608,7 +631,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         const int k = tid + r * kLB;
-        if (r < m && k < a.nD) receive(a, S, k, nCur[r], a.N + k, slot);
+        if (r < m && k < a.nD) receive(a, S, k, nCur[r], a.N + k, slot, haveE, eCur[r]);
       }
       lap(a, 1, tp);
       // the draws in list order: one per non-refractory entry (lif.c:49-52). The first driven
@@ -720,7 +743,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     for (int r = 0; r < kMaxPer; r++) {
       const int k = kOf(r);
       if (r < per && k < nLocal) {
-        receive(a, S, k, nCur[r], (uint32_t)S.id[k], slot);
+        receive(a, S, k, nCur[r], (uint32_t)S.id[k], slot, haveE, eCur[r]);
         const bool f = integrate(a, S, k);
         emit(a, S, k, f);
         if (f) flags |= (uint64_t)1 << (16 * r);

@@ -8,7 +8,7 @@ namespace fb {
 
 constexpr int kLagRing = 64;  // ring depth of the per-step counters and lists (a power of two)
 constexpr int kLagThreads = 1024;  // threads per block
-constexpr int kLagPer = 4;        // neurons per thread at most (tile and driven blocks)
+constexpr int kLagPer = 2;        // neurons per thread at most (tile and driven blocks)
 constexpr int kHelp = 2;      // steps after which the tile blocks push the driven block's spikes
 
 struct LagArgs {
