@@ -113,24 +113,31 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def _reduce(x, world, op):
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, world):
+    import torch.distributed as dist
+    return _reduce(x, world, dist.ReduceOp.MAX if world > 1 else None)
 
 
 def sum_over_ranks(x, world):
-    if world <= 1:
-        return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, world, dist.ReduceOp.SUM if world > 1 else None)
+
+
+def replica_throughput(events, seconds, world):
+    """Whole-job throughput of independent replicas: the events of every rank over the slowest
+    rank's time (each rank times its own timed region between barriers)."""
+    return sum_over_ranks(events, world) / max_over_ranks(seconds, world)
 
 
 def algorithmic_bytes(N, steps, spikes, events):
