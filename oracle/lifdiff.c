@@ -16,9 +16,12 @@
  * hard or soft (logistic) spikes, scalar or per-neuron surrogate beta, adaptation, depression,
  * inScale from sizeAlpha/sizeLog (or given), outScale, thrOffset, thrMask/kcThreshold,
  * biasMask/laminaBias, edgeGain, the minSyn/sensory gate, logGain, the Poisson drive (xorshift32,
- * drivenSet order), adjClip, truncation, lossFrom, and a per-step dLoss/dspike (dLdSpike per step
- * generalises dLdSpikePerEpoch). Not covered: driveSoft, driveIdx (drive gradients), spikeTrain
- * replay, exact32.
+ * drivenSet order), adjClip, truncation, lossFrom, a per-step dLoss/dspike (dLdSpike per step
+ * generalises dLdSpikePerEpoch), driveSoft (:338, :453, :588-604), driveIdx/driveEpoch with the
+ * drive held per epoch and its gradient (:134-144, :242-251, :407-412, :523-528, :572, :604),
+ * spikeTrain replay (:298-306, :430-436) and exact32 (:172-190, :231-240, :256-275, :317-326).
+ * The drive schedule is given as the values the reference's onEpoch callback would set: at every
+ * epoch boundary, driveAt[epoch][k] is set for driveIdx[k] in k order (setDriveOne semantics).
  *
  * Beyond the reference's outputs (which it also computes here), the sweep accumulates:
  *   gEdge[j]  = dLoss/dW_j for the effective weight W_j = count*edgeGain*inScale[q](*inhGain) of
@@ -40,7 +43,8 @@ typedef struct {
   double kcThreshold, laminaBias, surrogateBeta, adjClip;
   int32_t coba, soft, checkpoint, truncate, lossFrom, steps;
   uint32_t seed;
-  int32_t nDriven, pad;
+  int32_t nDriven;
+  int32_t driveSoft, exact32, driveEpoch, nDriveIdx;
 } ld_params;
 
 typedef struct {
@@ -54,6 +58,10 @@ typedef struct {
   const uint8_t *thrMask, *biasMask, *sensory;         /* may be null */
   const float *drive;                  /* per neuron, Hz */
   const int32_t *driven;               /* driven set in insertion order, nDriven entries */
+  const int32_t *driveIdx;             /* neurons whose drive is an input (nDriveIdx) or null */
+  const float *driveAt;                /* [epochs][nDriveIdx] drive schedule, or null */
+  const int64_t *trainOff;             /* spikeTrain: per step offsets (steps + 1) or null */
+  const int32_t *trainIdx;
 } ld_graph;
 
 typedef struct {
@@ -63,6 +71,8 @@ typedef struct {
   double *gEdge;    /* E (optional) */
   double *gBias;    /* N (optional) */
   double *gOut;     /* N (optional) */
+  float *gDrive;    /* [epochs][nDriveIdx] (optional) */
+  int32_t clamped_drive, pad;
 } ld_grads;
 
 /* ---- the tape -------------------------------------------------------------------------------- */
@@ -83,7 +93,40 @@ typedef struct {
   float *v, *gE, *gI, *adapt, *res, *refr, *spikeCount, *inScale;
   uint8_t *gate;
   uint32_t rng;
+  /* the live drive (setDriveOne changes it) and the driven set in insertion order */
+  float *drive;
+  int32_t *driven, nDriven;
+  uint8_t *inSet;
+  /* exact32: writeGraph's two baked arrays (src/lifdiff.js:177-189) */
+  float *W32, *signW32;
 } ld_state;
+
+static const double DRIVE_MAX = 0.999; /* src/lifdiff.js:72 */
+static inline float F(double x) { return (float)x; }
+
+/* setDriveOne (src/lifdiff.js:207): a Set keeps insertion order; delete then re-add appends. */
+static void ld_set_drive(ld_state *S, int32_t i, float rate) {
+  S->drive[i] = rate;
+  if (rate > 0) {
+    if (!S->inSet[i]) { S->driven[S->nDriven++] = i; S->inSet[i] = 1; }
+  } else if (S->inSet[i]) {
+    int32_t n = 0;
+    for (int32_t k = 0; k < S->nDriven; k++)
+      if (S->driven[k] != i) S->driven[n++] = S->driven[k];
+    S->nDriven = n;
+    S->inSet[i] = 0;
+  }
+}
+
+static void ld_drive_init(const ld_params *p, const ld_graph *g, ld_state *S) {
+  memcpy(S->drive, g->drive, (size_t)S->N * 4);
+  memset(S->inSet, 0, (size_t)S->N);
+  S->nDriven = 0;
+  for (int32_t k = 0; k < p->nDriven; k++) {
+    S->driven[S->nDriven++] = g->driven[k];
+    S->inSet[g->driven[k]] = 1;
+  }
+}
 
 static uint32_t ld_rand_u32(uint32_t *s) {
   uint32_t x = *s;
@@ -108,6 +151,17 @@ static void ld_prepare(const ld_params *p, const ld_graph *g, ld_state *S) {
   }
   for (int64_t j = 0; j < g->E; j++)
     S->gate[j] = ((double)g->counts[j] >= p->minSyn && !(g->sensory && g->sensory[g->indices[j]])) ? 1 : 0;
+  if (p->exact32 && S->W32) {
+    for (int32_t j = 0; j < g->N; j++) {
+      const double sg = g->sign[j];
+      S->signW32[j] = F(sg * p->wSyn);
+      const double og = g->outScale ? (double)g->outScale[j] : 1.0, ig = (sg < 0 ? p->inhGain : 1.0) * og;
+      for (uint32_t k = g->indptr[j]; k < g->indptr[j + 1]; k++)
+        S->W32[k] = S->gate[k] ? F((double)g->counts[k] * (g->edgeGain ? (double)g->edgeGain[k] : 1.0) *
+                                   (double)S->inScale[g->indices[k]] * ig)
+                               : 0.f;
+    }
+  }
 }
 
 static void ld_reset(const ld_params *p, ld_state *S) {
@@ -138,9 +192,23 @@ static inline double ld_u(const ld_params *p, double vv, double gEv, double gIv,
 
 /* Delivery of one step's arrivals (src/lifdiff.js:276-283). resAt (optional) records res[pre]. */
 static void ld_deliver(const ld_params *p, const ld_graph *g, ld_state *S, const int32_t *idx,
-                       const float *amp, int64_t na, float *resAt) {
+                       const float *amp, int64_t na, float *resAt, int ex) {
+  const float dU = F(p->depU);
   for (int64_t k = 0; k < na; k++) {
     const int32_t pre = idx[k];
+    if (ex) {  /* lif.c's factorization (src/lifdiff.js:256-272) */
+      float sv = F((double)S->signW32[pre] * (double)S->res[pre]);
+      if (amp[k] != 1.f) sv = F((double)sv * (double)amp[k]);
+      if (sv == 0) continue;
+      S->res[pre] = F((double)S->res[pre] - (double)dU * (double)S->res[pre]);
+      const uint32_t a = g->indptr[pre], b = g->indptr[pre + 1];
+      float *gg = sv > 0 ? S->gE : S->gI;
+      for (uint32_t j = a; j < b; j++) {
+        const float dlt = F((double)S->W32[j] * (double)sv);
+        if (dlt != 0) gg[g->indices[j]] = F((double)gg[g->indices[j]] + (double)dlt);
+      }
+      continue;
+    }
     const double sg = g->sign[pre];
     if (sg == 0) continue;
     if (resAt) resAt[k] = S->res[pre];
@@ -174,16 +242,23 @@ typedef struct {
 } ld_arena;
 
 /* One forward step; fills the tape's list for step t (and the arena row when A is given).
- * forced (optional): the step's forced spikes taken from the tape instead of drawn. */
-static void ld_step(const ld_params *p, const ld_graph *g, ld_state *S, ld_tape *T, int32_t t,
-                    const int32_t *arrIdx, const float *arrAmp, int64_t na, ld_arena *A, int32_t r,
-                    const int32_t *forced, int32_t nForced, int32_t *outIdx, float *outAmp,
-                    int64_t *outN, int32_t *outForced, uint8_t *isForced) {
+ * forced (optional): the step's forced spikes taken from the tape instead of drawn (the replay).
+ * ex: exact32 arithmetic (forward only; the replay is not exact32 in the reference either). */
+static void ld_step(const ld_params *p, const ld_graph *g, ld_state *S, int32_t t, const int32_t *arrIdx,
+                    const float *arrAmp, int64_t na, ld_arena *A, int32_t r, const int32_t *forced,
+                    int32_t nForced, int32_t *outIdx, float *outAmp, int64_t *outN, int32_t *outForced,
+                    uint8_t *isForced, int ex) {
   const int32_t N = S->N;
-  const double dt = p->dt, dtS = S->dtS;
-  ld_deliver(p, g, S, arrIdx, arrAmp, na, A ? A->resAt + A->resOff[r] : NULL);
+  const double dtS = S->dtS;
+  /* lif.c reads its scalars from the f32 header: exact32 uses the rounded values (:232-240) */
+  const double vR = ex ? F(p->vRest) : p->vRest, eE = ex ? F(p->eExc) : p->eExc, eI = ex ? F(p->eInh) : p->eInh,
+               vTh = ex ? F(p->vThresh) : p->vThresh, vRs = ex ? F(p->vReset) : p->vReset,
+               tRf = ex ? F(p->tRef) : p->tRef, aI = ex ? F(p->adaptInc) : p->adaptInc, dT = ex ? F(p->dt) : p->dt,
+               lB = ex ? F(p->laminaBias) : p->laminaBias, dEp = ex ? F(S->dE) : S->dE, dAp = ex ? F(S->dA) : S->dA,
+               kRp = ex ? F(S->kRec) : S->kRec, kMp = ex ? F(S->kM) : S->kM, dtSp = ex ? F(dtS) : dtS,
+               cEp = ex ? F(S->cE) : S->cE, cIp = ex ? F(S->cI) : S->cI;
+  ld_deliver(p, g, S, arrIdx, arrAmp, na, A ? A->resAt + A->resOff[r] : NULL, ex);
   int64_t n = 0;
-  /* exogenous drive, in drivenSet order (:290-297) */
   if (forced) {
     for (int32_t k = 0; k < nForced; k++) {
       const int32_t i = forced[k];
@@ -196,19 +271,35 @@ static void ld_step(const ld_params *p, const ld_graph *g, ld_state *S, ld_tape 
       isForced[i] = 1;
     }
   } else {
-    for (int32_t k = 0; k < p->nDriven; k++) {
-      const int32_t i = g->driven[k];
-      if (S->refr[i] > 0) continue;
-      if (ld_rand(&S->rng) < (double)g->drive[i] * dtS) {
-        S->refr[i] = (float)(p->tRef + p->dt);
+    /* exogenous drive, in drivenSet order (:290-297); none under driveSoft */
+    if (!p->driveSoft)
+      for (int32_t k = 0; k < S->nDriven; k++) {
+        const int32_t i = S->driven[k];
+        if (S->refr[i] > 0) continue;
+        const double thrP = ex ? (double)F((double)S->drive[i] * dtSp) : (double)S->drive[i] * dtS;
+        if (ld_rand(&S->rng) < thrP) {
+          S->refr[i] = ex ? F(tRf + dT) : (float)(p->tRef + p->dt);
+          outIdx[n] = i;
+          outAmp[n] = 1.f;
+          n++;
+          S->spikeCount[i] = (float)((double)S->spikeCount[i] + 1);
+          S->adapt[i] = (float)((double)S->adapt[i] + aI);
+          if (isForced) isForced[i] = 1;
+        }
+      }
+    /* spikeTrain: recorded spikes forced at their steps, no draw (:298-306) */
+    if (g->trainOff)
+      for (int64_t q = g->trainOff[t]; q < g->trainOff[t + 1]; q++) {
+        const int32_t i = g->trainIdx[q];
+        if (S->refr[i] > 0) continue;
+        S->refr[i] = ex ? F(tRf + dT) : (float)(p->tRef + p->dt);
         outIdx[n] = i;
         outAmp[n] = 1.f;
         n++;
         S->spikeCount[i] = (float)((double)S->spikeCount[i] + 1);
-        S->adapt[i] = (float)((double)S->adapt[i] + p->adaptInc);
+        S->adapt[i] = (float)((double)S->adapt[i] + aI);
         if (isForced) isForced[i] = 1;
       }
-    }
   }
   *outForced = (int32_t)n;
   /* integrate and spike (:313-344); replay's bookkeeping (:439-458) */
@@ -223,24 +314,44 @@ static void ld_step(const ld_params *p, const ld_graph *g, ld_state *S, ld_tape 
     }
     const int wasRefr = S->refr[i] > 0;
     if (wasRefr) {
-      S->refr[i] = (float)((double)S->refr[i] - dt);
-      vi = p->vReset;
+      S->refr[i] = (float)((double)S->refr[i] - dT);
+      vi = vRs;
       if (isForced && isForced[i]) { md = 2; s = 1; } else md = 1;
+    } else if (ex) {
+      /* lif.c's expression, one f32 rounding per C operation (:317-326); current-based: lif.c:67 */
+      const double bias = biasOf(p, g, i) != 0 ? lB : 0.0;
+      float acc = F(vR - vi);
+      if (p->coba) {
+        acc = F((double)acc + (double)F((double)F((double)S->gE[i] * (double)F(eE - vi)) * cEp));
+        acc = F((double)acc + (double)F((double)F((double)S->gI[i] * (double)F(vi - eI)) * cIp));
+      } else {
+        acc = F((double)acc + (double)S->gE[i]);
+        acc = F((double)acc + (double)S->gI[i]);
+      }
+      vi = F(vi + (double)F((double)F((double)acc + bias) * kMp));
     } else {
       vi = ld_u(p, vi, S->gE[i], S->gI[i], biasOf(p, g, i), S->kM, S->cE, S->cI);
     }
-    S->gE[i] = (float)((double)S->gE[i] * S->dE);
-    S->gI[i] = (float)((double)S->gI[i] * S->dE);
-    S->adapt[i] = (float)((double)S->adapt[i] * S->dA);
-    S->res[i] = (float)((double)S->res[i] + (1 - (double)S->res[i]) * S->kRec);
+    S->gE[i] = (float)((double)S->gE[i] * dEp);
+    S->gI[i] = (float)((double)S->gI[i] * dEp);
+    S->adapt[i] = (float)((double)S->adapt[i] * dAp);
+    S->res[i] = ex ? F((double)S->res[i] + (double)F((double)F(1 - (double)S->res[i]) * kRp))
+                   : (float)((double)S->res[i] + (1 - (double)S->res[i]) * kRp);
     if (A) A->adapt[off + i] = S->adapt[i];
     if (!wasRefr) {
-      const double thr = p->vThresh + (double)S->adapt[i] + kcOf(p, g, i) + (double)g->thrOffset[i];
+      const double thr = ex ? (double)F((double)F(vTh + (double)S->adapt[i]) + (double)g->thrOffset[i])
+                            : p->vThresh + (double)S->adapt[i] + kcOf(p, g, i) + (double)g->thrOffset[i];
       s = p->soft ? 1 / (1 + exp(-(vi - thr) / betaOf(p, g, i))) : (vi >= thr ? 1 : 0);
+      /* driveSoft: the drive's expected spike (:338, :453) */
+      if (p->driveSoft && S->drive[i] > 0) {
+        const double sd = fmin(DRIVE_MAX, (double)S->drive[i] * dtS);
+        s = sd + (1 - sd) * s;
+        md = 3;
+      }
       if (s > 0) {
-        vi = s * p->vReset + (1 - s) * vi;
-        if (!p->soft) S->refr[i] = (float)p->tRef;
-        S->adapt[i] = (float)((double)S->adapt[i] + s * p->adaptInc);
+        vi = s * vRs + (1 - s) * vi;
+        if (!p->soft) S->refr[i] = (float)tRf;
+        S->adapt[i] = (float)((double)S->adapt[i] + s * aI);
       }
       S->spikeCount[i] = (float)((double)S->spikeCount[i] + s);
       if (s > (p->soft ? 1e-4 : 0.5)) {
@@ -258,8 +369,16 @@ static void ld_step(const ld_params *p, const ld_graph *g, ld_state *S, ld_tape 
   if (isForced)
     for (int64_t k = 0; k < *outForced; k++) isForced[outIdx[k]] = 0;
   *outN = n;
-  (void)t;
-  (void)T;
+}
+
+/* The drive the forward pass used at step t (:242-251, :407-412): at each epoch boundary (and at
+ * the first step of a replayed segment) the schedule's values for driveIdx, in k order. */
+static void ld_drive_epoch(const ld_params *p, const ld_graph *g, ld_state *S, int32_t t, int32_t segStart) {
+  if (!g->driveAt || !g->driveIdx) return;
+  const int32_t ep = p->driveEpoch > 1 ? p->driveEpoch : 1;
+  if (!(t % ep == 0 || t == segStart)) return;
+  const float *row = g->driveAt + (int64_t)(t / ep) * p->nDriveIdx;
+  for (int32_t k = 0; k < p->nDriveIdx; k++) ld_set_drive(S, g->driveIdx[k], row[k]);
 }
 
 static void ld_consts(const ld_params *p, ld_state *S) {
@@ -292,11 +411,19 @@ int64_t ld_forward(const ld_params *p, const ld_graph *g, float *spikeCount, int
   S.refr = buf + 5 * N; S.inScale = buf + 6 * N;
   S.spikeCount = spikeCount;
   S.gate = (uint8_t *)malloc((size_t)(g->E > 0 ? g->E : 1));
+  S.drive = (float *)malloc((size_t)N * 4);
+  S.driven = (int32_t *)malloc((size_t)N * 4);
+  S.inSet = (uint8_t *)malloc((size_t)N);
+  if (p->exact32) {
+    S.W32 = (float *)malloc((size_t)(g->E > 0 ? g->E : 1) * 4);
+    S.signW32 = (float *)malloc((size_t)N * 4);
+  }
   uint8_t *isForced = (uint8_t *)calloc((size_t)N, 1);
   int32_t *oIdx = (int32_t *)malloc((size_t)N * 2 * sizeof(int32_t));
   float *oAmp = (float *)malloc((size_t)N * 2 * sizeof(float));
   ld_prepare(p, g, &S);
   ld_reset(p, &S);
+  ld_drive_init(p, g, &S);
   S.rng = (uint32_t)fmod(floor((double)p->seed * 2654435761.0), 4294967296.0);
   if (!S.rng) S.rng = 1;
   int64_t len = 0;
@@ -317,7 +444,8 @@ int64_t ld_forward(const ld_params *p, const ld_graph *g, float *spikeCount, int
     if (e >= 0) { aI = tIdx + tOff[e]; aA = tAmp + tOff[e]; na = tOff[e + 1] - tOff[e]; }
     int64_t n = 0;
     int32_t nf = 0;
-    ld_step(p, g, &S, NULL, t, aI, aA, na, NULL, 0, NULL, 0, oIdx, oAmp, &n, &nf, isForced);
+    ld_drive_epoch(p, g, &S, t, -1);
+    ld_step(p, g, &S, t, aI, aA, na, NULL, 0, NULL, 0, oIdx, oAmp, &n, &nf, isForced, p->exact32);
     if (len + n > tapeCap) { len = -1; break; }
     memcpy(tIdx + len, oIdx, n * 4);
     memcpy(tAmp + len, oAmp, n * 4);
@@ -326,6 +454,7 @@ int64_t ld_forward(const ld_params *p, const ld_graph *g, float *spikeCount, int
     tForced[t] = nf;
   }
   free(buf); free(S.gate); free(isForced); free(oIdx); free(oAmp);
+  free(S.drive); free(S.driven); free(S.inSet); free(S.W32); free(S.signW32);
   return len;
 }
 
@@ -351,7 +480,22 @@ int32_t ld_backward(const ld_params *p, const ld_graph *g, const int32_t *tIdx, 
   S.v = buf; S.gE = buf + N; S.gI = buf + 2 * N; S.adapt = buf + 3 * N; S.res = buf + 4 * N;
   S.refr = buf + 5 * N; S.inScale = buf + 6 * N; S.spikeCount = buf + 7 * N;
   S.gate = (uint8_t *)malloc((size_t)(g->E > 0 ? g->E : 1));
+  S.drive = (float *)malloc((size_t)N * 4);
+  S.driven = (int32_t *)malloc((size_t)N * 4);
+  S.inSet = (uint8_t *)malloc((size_t)N);
   ld_prepare(p, g, &S);
+  ld_drive_init(p, g, &S);
+  /* the drive adjoint, per epoch and driveIdx entry (:523-528) */
+  const int32_t ep = p->driveEpoch > 1 ? p->driveEpoch : 1, nD = g->driveAt ? p->nDriveIdx : 0;
+  int32_t *dSlot = NULL;
+  if (nD) {
+    dSlot = (int32_t *)malloc((size_t)N * 4);
+    for (int32_t i = 0; i < N; i++) dSlot[i] = -1;
+    for (int32_t k = 0; k < nD; k++) dSlot[g->driveIdx[k]] = k;
+  }
+  float *gDrive = out->gDrive;
+  const int32_t nEpochs = (steps + ep - 1) / ep;
+  if (gDrive) memset(gDrive, 0, (size_t)nEpochs * (nD ? nD : 0) * 4);
   /* adjoint state (Float32Array in the reference) */
   float *lv = (float *)calloc(N, 4), *lgE = (float *)calloc(N, 4), *lgI = (float *)calloc(N, 4);
   float *lad = (float *)calloc(N, 4), *lres = (float *)calloc(N, 4);
@@ -394,7 +538,8 @@ int32_t ld_backward(const ld_params *p, const ld_graph *g, const int32_t *tIdx, 
       A.resOff[r + 1] = A.resOff[r] + na;
       int64_t n = 0;
       int32_t nf = 0;
-      ld_step(p, g, &S, NULL, t, aI, aA, na, &A, r, tIdx + tOff[t], tForced[t], oIdx, oAmp, &n, &nf, isForced);
+      ld_drive_epoch(p, g, &S, t, from);
+      ld_step(p, g, &S, t, aI, aA, na, &A, r, tIdx + tOff[t], tForced[t], oIdx, oAmp, &n, &nf, isForced, 0);
     }
     /* reverse steps of the segment */
     for (int32_t t = to - 1; t >= from; t--) {
@@ -407,6 +552,7 @@ int32_t ld_backward(const ld_params *p, const ld_graph *g, const int32_t *tIdx, 
       }
       float *ls = lsRing + (int64_t)(t % ns) * N;
       const float *dLt = dLPerStep ? dL + (int64_t)t * N : dL;
+      const int64_t dOff = (int64_t)(t / ep) * nD;
       for (int32_t i = 0; i < N; i++) {
         const int md = A.mode[off + i];
         const double lpA = lad[i];
@@ -414,7 +560,11 @@ int32_t ld_backward(const ld_params *p, const ld_graph *g, const int32_t *tIdx, 
         lgE[i] = (float)lE; lgI[i] = (float)lI; lad[i] = (float)lA; lres[i] = (float)lR;
         if (md == 1) { lv[i] = 0; continue; }
         if (md == 2) {
+          /* the drive fired: its gradient takes ds/d(sd) = 1 (:565-573) */
+          const double lspike2 = (double)ls[i] + (scored ? (double)dLt[i] : 0);
           sAdaptInc += lA;
+          if (gDrive && dSlot[i] >= 0)
+            gDrive[dOff + dSlot[i]] = (float)((double)gDrive[dOff + dSlot[i]] + (lA * p->adaptInc + lspike2) * S.dtS);
           lv[i] = 0;
           ls[i] = 0;
           continue;
@@ -425,7 +575,13 @@ int32_t ld_backward(const ld_params *p, const ld_graph *g, const int32_t *tIdx, 
         const double thr = p->vThresh + (double)A.adapt[off + i] + kcOf(p, g, i) + (double)g->thrOffset[i];
         const double d = u - thr;
         const double s = A.sp[off + i];
-        const double sd = 0, st = s;
+        /* a soft drive's composite amplitude split back into sd and the threshold's st (:587-591) */
+        double sd = 0, st = s;
+        if (md == 3) {
+          const double rate = (dSlot && dSlot[i] >= 0) ? (double)g->driveAt[dOff + dSlot[i]] : (double)g->drive[i];
+          sd = fmin(DRIVE_MAX, rate * S.dtS);
+          st = (s - sd) / (1 - sd);
+        }
         const double beta = betaOf(p, g, i);
         double sgr;
         if (p->soft) sgr = st * (1 - st) / beta;
@@ -436,6 +592,8 @@ int32_t ld_backward(const ld_params *p, const ld_graph *g, const int32_t *tIdx, 
         const double lt = lsTot * (1 - sd) * sgr;
         const double lu = lvNew * (1 - s) + lt;
         const double lthr = -lt;
+        if (gDrive && dSlot[i] >= 0)  /* through sd: ds/d(sd) = 1 - st, d(sd)/d(rate) = dt/1000 (:604) */
+          gDrive[dOff + dSlot[i]] = (float)((double)gDrive[dOff + dSlot[i]] + lsTot * (1 - st) * S.dtS);
         sAdaptInc += lpA * s;
         sVThresh += lthr;
         if (g->thrMask && g->thrMask[i]) sKc += lthr;
@@ -530,6 +688,11 @@ int32_t ld_backward(const ld_params *p, const ld_graph *g, const int32_t *tIdx, 
     out->logGain[i] = x;
     if (out->gOut) out->gOut[i] = (double)x / outs(g, i);
   }
+  out->clamped_drive = 0;
+  if (gDrive)
+    for (int64_t k = 0; k < (int64_t)nEpochs * nD; k++)
+      if (!isfinite(gDrive[k])) { gDrive[k] = 0; out->clamped_drive++; }
+  free(S.drive); free(S.driven); free(S.inSet); free(dSlot);
   free(buf); free(S.gate); free(lv); free(lgE); free(lgI); free(lad); free(lres); free(gInScale);
   free(gLogGain); free(lsRing); free(A.vPre); free(A.gE); free(A.gI); free(A.adapt); free(A.sp);
   free(A.mode); free(A.resOff); free(A.resAt); free(isForced); free(oIdx); free(oAmp);
