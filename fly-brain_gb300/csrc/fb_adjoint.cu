@@ -12,7 +12,17 @@
 // The backward accumulates without float atomics: within one step every edge and every
 // presynaptic neuron is touched by one arrival at most, so per-edge and per-neuron accumulators
 // have a single writer per step and are summed in time order; scalars are reduced in a fixed order.
+//
+// Inputs beyond the network: a drive schedule (driveIdx/driveEpoch, src/lifdiff.js:134-144) whose
+// values are set at every epoch boundary with setDriveOne semantics -- the drivenSet keeps
+// insertion order, so the host derives each boundary's edits (members removed, members appended)
+// and a one-block kernel applies them to the live list the draws walk; driveSoft (:338), the
+// drive's expected spike instead of a draw; a recorded spike train (:298-306) forced like driven
+// spikes; and exact32 (:172-190, :256-275, :317-326), a forward in lif.c's f32 arithmetic with the
+// two weight arrays writeGraph bakes.
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include <algorithm>
 #include <cmath>
@@ -35,6 +45,8 @@ constexpr int kDBucket = 8;   // bucket slots per target and step
 constexpr int kDSortMax = 64; // contributions per target sorted in local memory
 constexpr int kRB = 128;      // blocks per instance of the final reduction
 constexpr int kNSums = 9;     // scalar sums per instance
+constexpr int32_t kClaimFree = 0x7f7f7f7f;  // spike-train claim slots between steps
+constexpr double kDriveMax = 0.999;         // a soft drive's largest expected spike (src/lifdiff.js:72)
 
 struct DOvf {
   uint32_t k, j, next, pad;
@@ -46,14 +58,31 @@ struct DiffDev {
   int32_t N, nslots, K, coba, soft, nDriven, nro, nTiles;
   int32_t steps;   // length of the current forward; the instance sits out steps t >= steps
   uint32_t seed0;  // xorshift state after seeding
+  int32_t driveSoft, exact32;
+  int32_t nDS, driveEpoch;  // schedule columns (0: no schedule) and steps per epoch
   int64_t E;
   // graph and per-neuron structure
   const uint32_t *indptr, *indices;
   const uint32_t *cscPtr, *cscEdge, *cscSrc;  // in-edges of each target, ascending edge id
   const float *counts, *edgeGain, *sign, *logGain, *outScale, *thrOffset, *betaArr, *biasArr, *sizeLog;
   const uint8_t *thrMask, *biasMask;
-  const float *drive;
-  const int32_t *driven;
+  const float *drive;     // the drive as set (Hz)
+  const int32_t *driven;  // the drivenSet at reset, in insertion order
+  // the drive schedule: neuron -> schedule column (-1: none), the values [epochs][nDS], the live
+  // drivenSet, and per epoch the edits that keep it in insertion order ([removed | appended])
+  const int32_t *dSlot;
+  const float *driveAt;
+  int32_t *drivenLive, *nLive;
+  const int32_t *epOff, *epList;
+  uint8_t *rmFlag;
+  // a recorded spike train: step t forces trainIdx[trainOff[t] .. trainOff[t+1]); claim[i] picks
+  // the first listing of a neuron within a step
+  const int64_t *trainOff;
+  const int32_t *trainIdx;
+  int32_t *claim;
+  // exact32: W32[j] = f32(count * edgeGain * inScale * inhibitory gain * outScale) (0 if gated
+  // off) and signW32[i] = f32(sign * wSyn), lif.c's two weight arrays (src/lifdiff.js:177-189)
+  float *W32, *signW32;
   // derived per forward: inScale, gate, P[j] = (count * edgeGain) * inScale[q] (double, float)
   const float *inScale;
   const uint8_t *gate;
@@ -94,9 +123,10 @@ struct DiffDev {
   double *accA, *accV, *accKc, *accLa, *accEI, *accW, *accD, *gLog, *gBias, *gEdge;
   float *gLogF;  // log-gain gradient as returned (non-finite -> 0)
   double *gOut;  // outScale gradient
+  float *gDrive; // [epochs][nDS] dLoss/d(scheduled drive), float as the reference accumulates it
   const float *dL;       // flat [N], or per step over the readout set [steps][nro]
   const int32_t *roMap;  // neuron -> readout column, -1 elsewhere (per-step dL)
-  int32_t *nonfinite;    // count of non-finite log-gain gradients
+  int32_t *nonfinite;    // counts of non-finite log-gain [0] and drive [1] gradients
   uint32_t ovfCap, pad0;
   int32_t *err;
   const uint32_t *jump;
@@ -119,7 +149,20 @@ template <typename R>
 struct DP {
   R dt, vRest, vThresh, vReset, tRef, wSyn, adaptInc, depU, eExc, eInh, inhGain;
   R kcThreshold, laminaBias, beta, adjClip, dE, dA, kRec, kM, dtS, cE, cI;
+  // exact32: the same scalars rounded to f32, as lif.c reads them from its header
+  float xdt, xvRest, xvThresh, xvReset, xtRef, xadaptInc, xdepU, xeExc, xeInh, xlaminaBias;
+  float xdE, xdA, xkRec, xkM, xdtS, xcE, xcI;
 };
+
+// The drive neuron i runs at in step t: the schedule's value for its column (the last driveIdx
+// entry naming it), else the drive as set (src/lifdiff.js:242-251).
+__device__ __forceinline__ float d_drive(const DiffDev &D, int i, int t) {
+  if (D.driveAt) {
+    const int k = D.dSlot[i];
+    if (k >= 0) return D.driveAt[(int64_t)(t / D.driveEpoch) * D.nDS + k];
+  }
+  return D.drive[i];
+}
 
 template <typename R>
 __device__ __forceinline__ R d_bias(const DiffDev &D, const DP<R> &P, int i, R *lam) {
@@ -186,12 +229,72 @@ __global__ void k_reset(const DiffDev *Ds, float vRest) {
     D.isForced[i] = 0;
     D.cnt[i] = 0;
     D.ovfHead[i] = kNil;
+    if (i < D.nDriven) D.drivenLive[i] = D.driven[i];
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *D.rng = D.seed0;
     D.tOff[0] = 0;
     *D.ovfTop = 0;
+    *D.nLive = D.nDriven;
   }
+}
+
+// exact32's baked weights (src/lifdiff.js:177-189), warp per presynaptic row: every product in
+// double, in the reference's operand order, stored once as f32.
+__global__ void k_prepare_w32(const DiffDev *Ds, double wSyn, double inhGain) {
+  __shared__ DiffDev D;
+  load_dev(Ds, D);
+  if (!D.W32) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = w0; j < D.N; j += nw) {
+    const double sg = D.sign[j];
+    if (lane == 0) D.signW32[j] = (float)(sg * wSyn);
+    const double ig = (sg < 0 ? inhGain : 1.0) * (D.outScale ? (double)D.outScale[j] : 1.0);
+    for (uint32_t k = D.indptr[j] + lane; k < D.indptr[j + 1]; k += 32)
+      D.W32[k] = D.gate[k] ? (float)((double)D.counts[k] * (D.edgeGain ? (double)D.edgeGain[k] : 1.0) *
+                                     (double)D.inScale[D.indices[k]] * ig)
+                           : 0.f;
+  }
+}
+
+// An epoch boundary of the drive schedule (forward): the drivenSet loses the epoch's removed
+// members (order kept) and gains its appended ones at the end, in the order setDriveOne calls in
+// driveIdx order would leave them (src/lifdiff.js:207). One block per instance.
+__global__ void __launch_bounds__(1024) k_epoch(const DiffDev *Ds, int32_t t) {
+  __shared__ DiffDev D;
+  __shared__ uint32_t scan[33];
+  load_dev(Ds, D);
+  if (t >= D.steps || !D.epOff || t % D.driveEpoch) return;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  const int64_t e = t / D.driveEpoch;
+  const int32_t r0 = D.epOff[2 * e], r1 = D.epOff[2 * e + 1], a1 = D.epOff[2 * e + 2];
+  for (int32_t k = r0 + tid; k < r1; k += bd) D.rmFlag[D.epList[k]] = 1;
+  __syncthreads();
+  const int32_t n = *D.nLive;
+  uint32_t kept = (uint32_t)n;
+  if (r1 > r0) {
+    // stable in-place compaction: every entry moves to a lower or equal index, and a chunk's reads
+    // all precede (through the scan's barriers) its writes
+    kept = 0;
+    for (int32_t c0 = 0; c0 < n; c0 += bd) {
+      const int32_t k = c0 + tid;
+      int32_t i = 0;
+      uint32_t keep = 0;
+      if (k < n) {
+        i = D.drivenLive[k];
+        keep = D.rmFlag[i] ? 0u : 1u;
+      }
+      uint32_t tot;
+      const uint32_t pos = block_exclusive_scan(keep, &tot, scan);
+      if (keep) D.drivenLive[kept + pos] = i;
+      kept += tot;
+    }
+    __syncthreads();
+    for (int32_t k = r0 + tid; k < r1; k += bd) D.rmFlag[D.epList[k]] = 0;
+  }
+  for (int32_t k = r1 + tid; k < a1; k += bd) D.drivenLive[kept + (k - r1)] = D.epList[k];
+  if (tid == 0) *D.nLive = (int32_t)kept + (a1 - r1);
 }
 
 // Saves (save=1, at t % K == 0) or restores (save=0) the checkpoint of step t.
@@ -215,6 +318,8 @@ __global__ void __launch_bounds__(kDB, 4) k_ckpt(const DiffDev *Ds, int32_t t, i
 // Delivery of the arrivals at step t (the spikes of step t - (nslots-1)), warp per arrival
 // (src/lifdiff.js:276-283): lane 0 forms eff and depresses res; lanes push (rank, edge) per
 // gated edge into the target's bucket. In a replay (row >= 0) the arrival's res is recorded.
+// exact32 (forward): lane 0 forms lif.c's s = f32(signW32 * res) (times the amplitude when it is
+// not 1) and skips a zero s before depressing res (src/lifdiff.js:256-272).
 template <typename R>
 __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
   __shared__ DiffDev D;
@@ -222,24 +327,38 @@ __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, 
   const int e = t - (D.nslots - 1);
   if (t >= D.steps || e < 0) return;
   float *resRow = row >= 0 ? D.resAt + (int64_t)row * D.maxArr : nullptr;
+  const bool ex = row < 0 && D.exact32;
   const int64_t a0 = D.tOff[e], na = D.tOff[e + 1] - a0;
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t k = w0; k < na; k += nw) {
     const int32_t pre = D.tIdx[a0 + k];
-    const float sg = D.sign[pre];
+    int go = 0;
     if (lane == 0) {
-      R eff = 0;
-      if (sg != 0) {
-        const R r = D.res[pre];
-        if (resRow) resRow[k] = (float)r;
-        eff = (R)sg * P.wSyn * d_out<R>(D, pre) * exp((R)D.logGain[pre]) * r * (R)D.tAmp[a0 + k];
-        D.res[pre] = (float)(r - P.depU * r);
+      if (ex) {
+        const float r = D.res[pre], amp = D.tAmp[a0 + k];
+        float sv = D.signW32[pre] * r;
+        if (amp != 1.f) sv = sv * amp;
+        if (sv != 0.f) {
+          D.res[pre] = (float)((double)r - (double)P.xdepU * (double)r);
+          go = 1;
+        }
+        D.effK[k] = (double)sv;
+      } else {
+        const float sg = D.sign[pre];
+        R eff = 0;
+        if (sg != 0) {
+          const R r = D.res[pre];
+          if (resRow) resRow[k] = (float)r;
+          eff = (R)sg * P.wSyn * d_out<R>(D, pre) * exp((R)D.logGain[pre]) * r * (R)D.tAmp[a0 + k];
+          D.res[pre] = (float)(r - P.depU * r);
+          go = 1;
+        }
+        D.effK[k] = (double)eff;
       }
-      D.effK[k] = (double)eff;
     }
-    if (sg == 0) continue;
+    if (!__shfl_sync(0xffffffffu, go, 0)) continue;
     const uint32_t lo = D.indptr[pre], hi = D.indptr[pre + 1];
     for (uint32_t j = lo + lane; j < hi; j += 32) {
       if (!D.gate[j]) continue;
@@ -264,10 +383,12 @@ __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, 
   }
 }
 
-// Forced spikes of step t (src/lifdiff.js:290-297), one block per instance. Forward: one draw per
-// non-refractory driven neuron in drivenSet order, compared (in R) against drive * dt/1000; each
-// spike goes to the head of step t's tape list. Replay: the tape's forced list. Runs after the
-// step's delivery, so it also rewinds the overflow pool for the next step.
+// Forced spikes of step t, one block per instance. Forward (src/lifdiff.js:290-306): unless
+// driveSoft, one draw per non-refractory member of the live drivenSet in insertion order, compared
+// (in R; exact32: in f32 as lif.c) against drive * dt/1000; then the spike train's neurons of step
+// t that are not refractory, first listing only. Each spike goes to the head of step t's tape list.
+// Replay: the tape's forced list. Runs after the step's delivery, so it also rewinds the overflow
+// pool for the next step.
 template <typename R>
 __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) {
   __shared__ DiffDev D;
@@ -289,49 +410,81 @@ __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) 
     if (tid == 0) *D.ovfTop = 0;
     return;
   }
-  for (int k = tid; k < 32 * 128; k += blockDim.x) sJump[k] = D.jump[k];
-  if (tid == 0) sh_s0 = *D.rng;
-  __syncthreads();
-  const uint32_t s0 = sh_s0;
-  uint32_t draws = 0, nf = 0;
-  for (int32_t r0 = 0; r0 < D.nDriven; r0 += blockDim.x) {
-    const int32_t k = r0 + tid;
-    int32_t i = 0;
-    uint32_t live = 0;
-    float dr = 0.f;
-    if (k < D.nDriven) {
-      i = D.driven[k];
-      live = D.refr[i] > 0 ? 0u : 1u;
-      dr = D.drive[i];
+  const bool ex = D.exact32 != 0;
+  const float refrF = ex ? P.xtRef + P.xdt : (float)(P.tRef + P.dt);
+  const R aInc = ex ? (R)P.xadaptInc : P.adaptInc;
+  uint32_t nf = 0;
+  auto fire_one = [&](int32_t i, int64_t o) {
+    if (o < D.tapeCap) {
+      D.tIdx[o] = i;
+      D.tAmp[o] = 1.f;
+    } else {
+      atomicCAS(D.err, 0, FB_EOVERFLOW);
     }
-    uint32_t nlive;
-    const uint32_t dpos = block_exclusive_scan(live, &nlive, scan);
-    uint32_t fire = 0;
-    if (live) {
-      const uint32_t x = xs_jump(sJump, s0, draws + dpos + 1);
-      const R u = (R)(x >> 8) * (R)(1.0 / 16777216.0);
-      fire = u < (R)dr * P.dtS ? 1u : 0u;
-    }
-    uint32_t nfire;
-    const uint32_t fpos = block_exclusive_scan(fire, &nfire, scan);
-    if (fire) {
-      const int64_t o = base + nf + fpos;
-      if (o < D.tapeCap) {
-        D.tIdx[o] = i;
-        D.tAmp[o] = 1.f;
-      } else {
-        atomicCAS(D.err, 0, FB_EOVERFLOW);
+    D.refr[i] = refrF;
+    D.spikeCount[i] = (float)((R)D.spikeCount[i] + R(1));
+    D.adapt[i] = (float)((R)D.adapt[i] + aInc);
+    D.isForced[i] = 1;
+  };
+  if (!D.driveSoft) {
+    for (int k = tid; k < 32 * 128; k += blockDim.x) sJump[k] = D.jump[k];
+    if (tid == 0) sh_s0 = *D.rng;
+    __syncthreads();
+    const uint32_t s0 = sh_s0;
+    const int32_t nLive = *D.nLive;
+    uint32_t draws = 0;
+    for (int32_t r0 = 0; r0 < nLive; r0 += blockDim.x) {
+      const int32_t k = r0 + tid;
+      int32_t i = 0;
+      uint32_t live = 0;
+      float dr = 0.f;
+      if (k < nLive) {
+        i = D.drivenLive[k];
+        live = D.refr[i] > 0 ? 0u : 1u;
+        dr = d_drive(D, i, t);
       }
-      D.refr[i] = (float)(P.tRef + P.dt);
-      D.spikeCount[i] = (float)((R)D.spikeCount[i] + R(1));
-      D.adapt[i] = (float)((R)D.adapt[i] + P.adaptInc);
-      D.isForced[i] = 1;
+      uint32_t nlive;
+      const uint32_t dpos = block_exclusive_scan(live, &nlive, scan);
+      uint32_t fire = 0;
+      if (live) {
+        const uint32_t x = xs_jump(sJump, s0, draws + dpos + 1);
+        const R u = (R)(x >> 8) * (R)(1.0 / 16777216.0);  // exact in f32 and f64
+        fire = (ex ? u < (R)(dr * P.xdtS) : u < (R)dr * P.dtS) ? 1u : 0u;
+      }
+      uint32_t nfire;
+      const uint32_t fpos = block_exclusive_scan(fire, &nfire, scan);
+      if (fire) fire_one(i, base + nf + fpos);
+      draws += nlive;
+      nf += nfire;
     }
-    draws += nlive;
-    nf += nfire;
+    if (tid == 0) *D.rng = xs_jump(sJump, s0, draws);
+  }
+  if (D.trainOff) {
+    const int64_t q0 = D.trainOff[t], q1 = D.trainOff[t + 1];
+    if (q1 > q0) {
+      __syncthreads();  // the draws' refractory marks are visible
+      for (int64_t q = q0 + tid; q < q1; q += blockDim.x) {
+        const int32_t i = D.trainIdx[q];
+        if (!(D.refr[i] > 0)) atomicMin(D.claim + i, (int32_t)(q - q0));
+      }
+      __syncthreads();
+      for (int64_t c0 = q0; c0 < q1; c0 += blockDim.x) {
+        const int64_t q = c0 + tid;
+        int32_t i = 0;
+        uint32_t fire = 0;
+        if (q < q1) {
+          i = D.trainIdx[q];
+          fire = D.claim[i] == (int32_t)(q - q0) ? 1u : 0u;
+        }
+        uint32_t nfire;
+        const uint32_t fpos = block_exclusive_scan(fire, &nfire, scan);
+        if (fire) fire_one(i, base + nf + fpos);
+        nf += nfire;
+      }
+      for (int64_t q = q0 + tid; q < q1; q += blockDim.x) D.claim[D.trainIdx[q]] = kClaimFree;
+    }
   }
   if (tid == 0) {
-    *D.rng = xs_jump(sJump, s0, draws);
     D.tForced[t] = (int32_t)nf;
     *D.ovfTop = 0;
   }
@@ -340,9 +493,18 @@ __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) 
 // Adds target i's bucket in arrival-rank order: gE (or gI) = f32(g + P[j] (*inhGain) * eff) in R.
 // Up to kDSortMax contributions are sorted in local memory; beyond that they are applied in
 // successive windows of the kDSortMax smallest ranks above the last one applied (ranks are unique
-// per target: one contribution per arrival).
+// per target: one contribution per arrival). exact32: lif.c's per-edge f32(W32 * s), skipped when
+// zero, added in f32 (src/lifdiff.js:270).
 template <typename R>
-__device__ __forceinline__ void d_add(const DiffDev &D, const DP<R> &Pp, uint2 c, float &geF, float &giF) {
+__device__ __forceinline__ void d_add(const DiffDev &D, const DP<R> &Pp, uint2 c, float &geF, float &giF, bool ex) {
+  if (ex) {
+    const float sv = (float)D.effK[c.x], dlt = D.W32[c.y] * sv;
+    if (dlt != 0.f) {
+      if (sv > 0.f) geF = geF + dlt;
+      else giF = giF + dlt;
+    }
+    return;
+  }
   const R eff = (R)D.effK[c.x];
   const R p = sizeof(R) == 8 ? (R)D.P[c.y] : (R)D.Pf[c.y];
   if (eff > 0) geF = (float)((R)geF + p * eff);
@@ -350,7 +512,7 @@ __device__ __forceinline__ void d_add(const DiffDev &D, const DP<R> &Pp, uint2 c
 }
 
 template <typename R>
-__device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, float &geF, float &giF) {
+__device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, float &geF, float &giF, bool ex) {
   uint2 e[kDSortMax];
   const uint2 *bk = D.bucket + (int64_t)i * kDBucket;
   const uint32_t nb = n < (uint32_t)kDBucket ? n : (uint32_t)kDBucket;
@@ -379,7 +541,7 @@ __device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, fl
       atomicCAS(D.err, 0, FB_EOVERFLOW);
       break;
     }
-    for (uint32_t u = 0; u < m; u++) d_add<R>(D, Pp, e[u], geF, giF);
+    for (uint32_t u = 0; u < m; u++) d_add<R>(D, Pp, e[u], geF, giF, ex);
     last = e[m - 1].x;
     any = true;
     done += m;
@@ -389,7 +551,9 @@ __device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, fl
 
 // Integrate and spike (src/lifdiff.js:313-344), one thread per neuron, tiles of kDB neurons; with
 // `row` >= 0 it also records the replay arena (:439-456). In a forward pass the spikes above the
-// tape threshold are staged per tile.
+// tape threshold are staged per tile. exact32 (forward): lif.c's expression with one f32 rounding
+// per C operation and the header's f32 scalars (:317-326). driveSoft: a driven neuron's spike is
+// sd + (1 - sd) s with sd = min(0.999, drive dt/1000) (:338).
 template <typename R>
 __global__ void __launch_bounds__(kDB, 4) k_update(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
   __shared__ DiffDev D;
@@ -397,6 +561,8 @@ __global__ void __launch_bounds__(kDB, 4) k_update(const DiffDev *Ds, DP<R> P, i
   load_dev(Ds, D);
   if (t >= D.steps) return;
   const int tid = threadIdx.x;
+  const bool ex = row < 0 && D.exact32;
+  const R vReset = ex ? (R)P.xvReset : P.vReset, aInc = ex ? (R)P.xadaptInc : P.adaptInc;
   for (int tl = blockIdx.x; tl < D.nTiles; tl += gridDim.x) {
     const int i = tl * kDB + tid;
     bool emit = false;
@@ -405,7 +571,7 @@ __global__ void __launch_bounds__(kDB, 4) k_update(const DiffDev *Ds, DP<R> P, i
       float geF = D.gE[i], giF = D.gI[i];
       const uint32_t n = D.cnt[i];
       if (n) {
-        d_apply<R>(D, P, i, n, geF, giF);
+        d_apply<R>(D, P, i, n, geF, giF, ex);
         D.cnt[i] = 0;
       }
       const R ge = geF, gi = giF;
@@ -422,30 +588,52 @@ __global__ void __launch_bounds__(kDB, 4) k_update(const DiffDev *Ds, DP<R> P, i
       if (forced) D.isForced[i] = 0;
       const bool wasRefr = refr > 0;
       if (wasRefr) {
-        refr = (float)((R)refr - P.dt);
-        vi = P.vReset;
+        refr = ex ? refr - P.xdt : (float)((R)refr - P.dt);
+        vi = vReset;
         if (forced) {
           md = 2;
           s = 1;
         } else {
           md = 1;
         }
+      } else if (ex) {
+        const float vf = D.v[i];
+        float acc = P.xvRest - vf;
+        if (D.coba) {
+          acc = acc + (geF * (P.xeExc - vf)) * P.xcE;
+          acc = acc + (giF * (vf - P.xeInh)) * P.xcI;
+        } else {
+          acc = acc + geF;
+          acc = acc + giF;
+        }
+        const float lam = (D.biasMask && D.biasMask[i]) ? P.xlaminaBias : 0.f;
+        acc = D.biasArr ? (float)((double)acc + ((double)lam + (double)D.biasArr[i])) : acc + lam;
+        vi = vf + acc * P.xkM;
       } else {
         vi = d_u<R>(D, P, vi, ge, gi, d_bias<R>(D, P, i, nullptr));
       }
-      geF = (float)(ge * P.dE);
-      giF = (float)(gi * P.dE);
-      float ad = (float)((R)D.adapt[i] * P.dA);
-      const R rs = D.res[i];
-      D.res[i] = (float)(rs + (R(1) - rs) * P.kRec);
+      geF = ex ? geF * P.xdE : (float)(ge * P.dE);
+      giF = ex ? giF * P.xdE : (float)(gi * P.dE);
+      float ad = ex ? D.adapt[i] * P.xdA : (float)((R)D.adapt[i] * P.dA);
+      const float rsF = D.res[i];
+      D.res[i] = ex ? rsF + (1.f - rsF) * P.xkRec : (float)((R)rsF + (R(1) - (R)rsF) * P.kRec);
       if (row >= 0) D.aAd[off] = ad;
       if (!wasRefr) {
-        const R thr = P.vThresh + (R)ad + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
+        const R thr = ex ? (R)((P.xvThresh + ad) + D.thrOffset[i])
+                         : P.vThresh + (R)ad + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
         s = D.soft ? R(1) / (R(1) + exp(-(vi - thr) / d_beta<R>(D, P, i))) : (vi >= thr ? R(1) : R(0));
+        if (D.driveSoft) {
+          const float dr = d_drive(D, i, t);
+          if (dr > 0.f) {
+            const R x = (R)dr * P.dtS, sd = x < (R)kDriveMax ? x : (R)kDriveMax;
+            s = sd + (R(1) - sd) * s;
+            md = 3;
+          }
+        }
         if (s > 0) {
-          vi = s * P.vReset + (R(1) - s) * vi;
-          if (!D.soft) refr = (float)P.tRef;
-          ad = (float)((R)ad + s * P.adaptInc);
+          vi = s * vReset + (R(1) - s) * vi;
+          if (!D.soft) refr = ex ? P.xtRef : (float)P.tRef;
+          ad = (float)((R)ad + s * aInc);
         }
         D.spikeCount[i] = (float)((R)D.spikeCount[i] + s);
         if (s > (D.soft ? R(1e-4) : R(0.5))) {
@@ -516,6 +704,10 @@ __global__ void k_zero_adjoint(const DiffDev *Ds) {
   }
   for (int64_t i = s0; i < (int64_t)D.nslots * N; i += ns) D.lsRing[i] = 0.f;
   for (int64_t j = s0; j < D.E; j += ns) D.gEdge[j] = 0.0;
+  if (D.gDrive) {
+    const int64_t nd = (int64_t)((D.steps + D.driveEpoch - 1) / D.driveEpoch) * D.nDS;
+    for (int64_t k = s0; k < nd; k += ns) D.gDrive[k] = 0.f;
+  }
 }
 
 // Truncated BPTT (src/lifdiff.js:541-548): the adjoint state restarts at every multiple of
@@ -530,13 +722,17 @@ __global__ void __launch_bounds__(kDB, 4) k_truncate(const DiffDev *Ds, int32_t 
 }
 
 // Reverse of integrate-and-spike at step t (src/lifdiff.js:555-617), with the adjoint clip
-// (:623-629) fused: one thread per neuron. Scalar terms accumulate per neuron in double.
+// (:623-629) fused: one thread per neuron. Scalar terms accumulate per neuron in double. The
+// gradient of a scheduled drive (:565-573, :587-604) accumulates per neuron into its column of the
+// step's epoch: a forced spike through ds/d(sd) = 1, a soft drive through ds/d(sd) = 1 - st, with
+// d(sd)/d(rate) = dt/1000 (the min's clamp is not differentiated, as in the reference).
 template <typename R>
 __global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row, int32_t scored) {
   __shared__ DiffDev D;
   load_dev(Ds, D);
   if (t >= D.steps) return;
   float *ls = D.lsRing + (int64_t)(t % D.nslots) * D.N;
+  float *gDrv = D.gDrive ? D.gDrive + (int64_t)(t / D.driveEpoch) * D.nDS : nullptr;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
     const int64_t off = (int64_t)row * D.N + i;
     const int md = D.aMode[off];
@@ -546,25 +742,7 @@ __global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, 
     float lvF = D.lv[i], lgEF = (float)lE, lgIF = (float)lI, ladF = (float)lA, lresF = (float)lR;
     if (md == 1) {
       lvF = 0.f;
-    } else if (md == 2) {
-      D.accA[i] += (double)lA;
-      lvF = 0.f;
-      ls[i] = 0.f;
     } else {
-      const R vv = D.aV[off], gEv = D.aGE[off], gIv = D.aGI[off];
-      R lam;
-      const R bias = d_bias<R>(D, P, i, &lam);
-      const R u = d_u<R>(D, P, vv, gEv, gIv, bias);
-      const R thr = P.vThresh + (R)D.aAd[off] + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
-      const R d = u - thr;
-      const R s = D.aSp[off];
-      const R beta = d_beta<R>(D, P, i);
-      R sg;
-      if (D.soft) sg = s * (R(1) - s) / beta;
-      else {
-        const R tt = R(1) + fabs(d) / beta;
-        sg = R(1) / (beta * tt * tt);
-      }
       R dl = 0;
       if (scored && D.dL) {
         if (D.roMap) {
@@ -574,29 +752,59 @@ __global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, 
           dl = D.dL[i];
         }
       }
-      const R lspike = (R)ls[i] + dl;
-      const R lvNew = lvF;
-      const R lsTot = (P.vReset - u) * lvNew + lpA * P.adaptInc + lspike;
-      const R lt = lsTot * R(1) * sg;
-      const R lu = lvNew * (R(1) - s) + lt;
-      const R lthr = -lt;
-      D.accA[i] += (double)(lpA * s);
-      D.accV[i] += (double)lthr;
-      if (D.thrMask && D.thrMask[i]) D.accKc[i] += (double)lthr;
-      ladF = (float)(lA + lthr * P.dA);
-      if (D.coba) {
-        lvF = (float)(lu * (R(1) + P.kM * (R(-1) - gEv * P.cE + gIv * P.cI)));
-        lgEF = (float)(lE + lu * P.kM * (P.eExc - vv) * P.cE);
-        lgIF = (float)(lI + lu * P.kM * (vv - P.eInh) * P.cI);
-        D.accEI[i] += (double)(lu * P.kM * gIv * P.cI * (R(-1) + (vv - P.eInh) * P.cI));
+      const int slot = gDrv ? D.dSlot[i] : -1;
+      if (md == 2) {
+        D.accA[i] += (double)lA;
+        if (slot >= 0) gDrv[slot] = (float)((R)gDrv[slot] + (lA * P.adaptInc + ((R)ls[i] + dl)) * P.dtS);
+        lvF = 0.f;
+        ls[i] = 0.f;
       } else {
-        lvF = (float)(lu * (R(1) - P.kM));
-        lgEF = (float)(lE + lu * P.kM);
-        lgIF = (float)(lI + lu * P.kM);
+        const R vv = D.aV[off], gEv = D.aGE[off], gIv = D.aGI[off];
+        R lam;
+        const R bias = d_bias<R>(D, P, i, &lam);
+        const R u = d_u<R>(D, P, vv, gEv, gIv, bias);
+        const R thr = P.vThresh + (R)D.aAd[off] + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
+        const R d = u - thr;
+        const R s = D.aSp[off];
+        // a soft drive's composite spike split back into sd and the threshold's st
+        R sd = 0, st = s;
+        if (md == 3) {
+          const R x = (R)d_drive(D, i, t) * P.dtS;
+          sd = x < (R)kDriveMax ? x : (R)kDriveMax;
+          st = (s - sd) / (R(1) - sd);
+        }
+        const R beta = d_beta<R>(D, P, i);
+        R sg;
+        if (D.soft) sg = st * (R(1) - st) / beta;
+        else {
+          const R tt = R(1) + fabs(d) / beta;
+          sg = R(1) / (beta * tt * tt);
+        }
+        const R lspike = (R)ls[i] + dl;
+        const R lvNew = lvF;
+        const R lsTot = (P.vReset - u) * lvNew + lpA * P.adaptInc + lspike;
+        const R lt = lsTot * (R(1) - sd) * sg;
+        const R lu = lvNew * (R(1) - s) + lt;
+        const R lthr = -lt;
+        if (slot >= 0) gDrv[slot] = (float)((R)gDrv[slot] + lsTot * (R(1) - st) * P.dtS);
+        D.accA[i] += (double)(lpA * s);
+        D.accV[i] += (double)lthr;
+        if (D.thrMask && D.thrMask[i]) D.accKc[i] += (double)lthr;
+        ladF = (float)(lA + lthr * P.dA);
+        if (D.coba) {
+          lvF = (float)(lu * (R(1) + P.kM * (R(-1) - gEv * P.cE + gIv * P.cI)));
+          lgEF = (float)(lE + lu * P.kM * (P.eExc - vv) * P.cE);
+          lgIF = (float)(lI + lu * P.kM * (vv - P.eInh) * P.cI);
+          D.accEI[i] += (double)(lu * P.kM * gIv * P.cI * (R(-1) + (vv - P.eInh) * P.cI));
+        } else {
+          lvF = (float)(lu * (R(1) - P.kM));
+          lgEF = (float)(lE + lu * P.kM);
+          lgIF = (float)(lI + lu * P.kM);
+        }
+        if (lam != 0) D.accLa[i] += (double)(lu * P.kM);
+        D.gBias[i] += (double)(lu * P.kM);
+        ls[i] = 0.f;
       }
-      if (lam != 0) D.accLa[i] += (double)(lu * P.kM);
-      D.gBias[i] += (double)(lu * P.kM);
-      ls[i] = 0.f;
     }
     const R c = P.adjClip;
     if (c > 0) {
@@ -723,6 +931,14 @@ __global__ void k_finalize(const DiffDev *Ds) {
     D.gLogF[i] = x;
     D.gOut[i] = (double)x / (D.outScale ? (double)D.outScale[i] : 1.0);
   }
+  if (D.gDrive) {
+    const int64_t nd = (int64_t)((D.steps + D.driveEpoch - 1) / D.driveEpoch) * D.nDS;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nd; k += (int64_t)gridDim.x * blockDim.x)
+      if (!isfinite(D.gDrive[k])) {
+        D.gDrive[k] = 0.f;
+        atomicAdd(D.nonfinite + 1, 1);
+      }
+  }
 }
 
 // The readout raster of one instance's recorded forward: out[t * nro + c] = amplitude at t.
@@ -796,6 +1012,14 @@ struct Inst {
   int32_t recordedSteps = 0;
   float *dLbuf = nullptr;
   int32_t *roMap = nullptr;
+  // host copies for the drive schedule's set edits and the exact32 check
+  std::vector<int32_t> driven0, driveIdx;
+  bool thrMaskAny = false;
+  // per-forward input buffers (grown on demand)
+  float *sched = nullptr, *gDrive = nullptr;
+  int32_t *epOff = nullptr, *epList = nullptr, *trainIdx = nullptr;
+  int64_t *trainOff = nullptr;
+  int64_t schedCap = 0, epOffCap = 0, epListCap = 0, trainOffCap = 0, trainIdxCap = 0, gDriveCap = 0;
 };
 
 }  // namespace
@@ -997,6 +1221,29 @@ int create_instance(fb_diff_batch *b, Inst &I, const fb_diff_net *net, int64_t t
     DCU(cudaMemcpy(dvD, dv.data(), dv.size() * 4, cudaMemcpyHostToDevice));
     D.drive = f;
     D.driven = dvD;
+    I.driven0.assign(dv.begin(), dv.begin() + net->nDriven);
+  }
+  // the schedule's columns (src/lifdiff.js:139-143): neuron -> the last driveIdx entry naming it
+  if (net->nDriveIdx < 0 || (net->nDriveIdx > 0 && !net->drive_idx))
+    return dfail(FB_EINVAL, "fb_diff: nDriveIdx=%d without drive_idx", net->nDriveIdx);
+  if (net->nDriveIdx > 0) {
+    I.driveIdx.resize(net->nDriveIdx);
+    DCU(cudaMemcpy(I.driveIdx.data(), net->drive_idx, 4 * (size_t)net->nDriveIdx, cudaMemcpyDefault));
+    std::vector<int32_t> slot(N, -1);
+    for (int32_t k = 0; k < net->nDriveIdx; k++) {
+      const int32_t i = I.driveIdx[k];
+      if (i < 0 || i >= N) return dfail(FB_EINVAL, "fb_diff: drive_idx[%d]=%d", k, i);
+      slot[i] = k;
+    }
+    int32_t *sl;
+    if ((rc = talloc(b, &sl, N))) return rc;
+    DCU(cudaMemcpy(sl, slot.data(), N * 4, cudaMemcpyHostToDevice));
+    D.dSlot = sl;
+  }
+  if (net->thr_mask) {
+    std::vector<uint8_t> m(N);
+    DCU(cudaMemcpy(m.data(), net->thr_mask, N, cudaMemcpyDefault));
+    for (int64_t i = 0; i < N && !I.thrMaskAny; i++) I.thrMaskAny = m[i] != 0;
   }
   // per-instance state, scratch, adjoint state and accumulators in one allocation
   D.ovfCap = (uint32_t)std::min<int64_t>(std::min<int64_t>(E + 1, (1 << 20) + E / 8), 0x7fffffff);
@@ -1010,9 +1257,12 @@ int create_instance(fb_diff_batch *b, Inst &I, const fb_diff_net *net, int64_t t
   c.add(&D.lv, N); c.add(&D.lgE, N); c.add(&D.lgI, N); c.add(&D.lad, N); c.add(&D.lres, N);
   c.add(&D.accA, N); c.add(&D.accV, N); c.add(&D.accKc, N); c.add(&D.accLa, N); c.add(&D.accEI, N);
   c.add(&D.accW, N); c.add(&D.accD, N); c.add(&D.gLog, N); c.add(&D.gBias, N); c.add(&D.gEdge, E);
-  c.add(&D.gLogF, N); c.add(&D.gOut, N); c.add(&D.nonfinite, 1);
+  c.add(&D.gLogF, N); c.add(&D.gOut, N); c.add(&D.nonfinite, 2);
   c.add(&D.tIdx, D.tapeCap); c.add(&D.tAmp, D.tapeCap);
+  c.add(&D.drivenLive, N); c.add(&D.nLive, 1); c.add(&D.rmFlag, N); c.add(&D.claim, N);
   if ((rc = c.commit(b))) return rc;
+  DCU(cudaMemset(D.rmFlag, 0, N));
+  DCU(cudaMemset(D.claim, 0x7f, N * 4));  // kClaimFree in every word
   DCU(cudaMemset(D.ovfTop, 0, 4));
   DCU(cudaMemset(D.cnt, 0, N * 4));
   DCU(cudaMemset(D.ovfHead, 0xff, N * 4));
@@ -1064,6 +1314,16 @@ DP<R> typed_params(const fb_diff_params *p) {
   q.dtS = (R)(p->dt / 1000);
   q.cE = (R)(1 / (p->eExc - p->vRest));
   q.cI = (R)(1 / (p->vRest - p->eInh));
+  q.xdt = (float)p->dt; q.xvRest = (float)p->vRest; q.xvThresh = (float)p->vThresh; q.xvReset = (float)p->vReset;
+  q.xtRef = (float)p->tRef; q.xadaptInc = (float)p->adaptInc; q.xdepU = (float)p->depU; q.xeExc = (float)p->eExc;
+  q.xeInh = (float)p->eInh; q.xlaminaBias = (float)p->laminaBias;
+  q.xdE = (float)std::exp(-p->dt / p->tauSyn);
+  q.xdA = (float)std::exp(-p->dt / p->adaptTau);
+  q.xkRec = (float)(p->dt / p->depTau);
+  q.xkM = (float)(p->dt / p->tauM);
+  q.xdtS = (float)(p->dt / 1000);
+  q.xcE = (float)(1 / (p->eExc - p->vRest));
+  q.xcI = (float)(1 / (p->vRest - p->eInh));
   return q;
 }
 
@@ -1079,6 +1339,11 @@ int fill_params(fb_diff_batch *b, const fb_diff_params *p) {
     I.D.K = p->checkpoint;
     I.D.coba = p->coba ? 1 : 0;
     I.D.soft = p->soft ? 1 : 0;
+    I.D.driveSoft = p->drive_soft ? 1 : 0;
+    I.D.exact32 = p->exact32 ? 1 : 0;
+    I.D.driveEpoch = std::max(1, p->drive_epoch);
+    if (p->exact32 && I.thrMaskAny)
+      return dfail(FB_EINVAL, "fb_diff: exact32 requires the full threshold field in thr_offset; thr_mask must be empty");
   }
   b->f32 = p->precision == FB_DIFF_F32;
   b->P64 = typed_params<double>(p);
@@ -1168,6 +1433,137 @@ int set_readout(fb_diff_batch *b, Inst &I, int32_t nro, const int32_t *ro) {
   return FB_OK;
 }
 
+// The drivenSet edits of every epoch boundary (src/lifdiff.js:207): setDriveOne(idx[k], at[e][k])
+// in k order leaves the set it found minus the members it removed (the rest keep their order),
+// plus the neurons it inserted, at the end in the order of their last insertion.
+// list[off[2e] .. off[2e+1]) are epoch e's removals, list[off[2e+1] .. off[2e+2]) its appends.
+int set_edits(int32_t N, const std::vector<int32_t> &driven0, const std::vector<int32_t> &idx, const float *at,
+              int64_t nEp, std::vector<int32_t> &off, std::vector<int32_t> &list) {
+  const int32_t nD = (int32_t)idx.size();
+  std::vector<uint8_t> in(N, 0), startIn(N, 0), removed(N, 0);
+  std::vector<int64_t> stamp(N, -1);
+  std::vector<int32_t> key(N, -1), touched;
+  std::vector<std::pair<int32_t, int32_t>> app;
+  for (int32_t i : driven0) in[i] = 1;
+  off.assign(2 * nEp + 1, 0);
+  list.clear();
+  for (int64_t e = 0; e < nEp; e++) {
+    touched.clear();
+    const float *row = at + e * nD;
+    for (int32_t k = 0; k < nD; k++) {
+      const int32_t i = idx[k];
+      if (stamp[i] != e) {
+        stamp[i] = e;
+        startIn[i] = in[i];
+        removed[i] = 0;
+        key[i] = -1;
+        touched.push_back(i);
+      }
+      if (row[k] > 0) {
+        if (!in[i]) {
+          in[i] = 1;
+          key[i] = k;
+        }
+      } else if (in[i]) {
+        in[i] = 0;
+        key[i] = -1;
+        if (startIn[i]) removed[i] = 1;
+      }
+    }
+    for (int32_t i : touched)
+      if (removed[i]) list.push_back(i);
+    off[2 * e + 1] = (int32_t)list.size();
+    app.clear();
+    for (int32_t i : touched)
+      if (in[i] && key[i] >= 0) app.emplace_back(key[i], i);
+    std::sort(app.begin(), app.end());
+    for (auto &a : app) list.push_back(a.second);
+    if (list.size() > (size_t)INT32_MAX / 2)
+      return dfail(FB_EINVAL, "fb_diff_forward: drive schedule edits exceed 2^30 entries");
+    off[2 * e + 2] = (int32_t)list.size();
+  }
+  return FB_OK;
+}
+
+// Grows a per-instance device buffer to at least n elements.
+template <typename T>
+int grow(fb_diff_batch *b, T **p, int64_t *cap, int64_t n) {
+  if (*p && *cap >= n) return FB_OK;
+  int rc = talloc(b, p, (size_t)std::max<int64_t>(n, 1));
+  if (rc) return rc;
+  *cap = std::max<int64_t>(n, 1);
+  return FB_OK;
+}
+
+// The schedule and spike train of one instance's forward (in may be null).
+int set_inputs(fb_diff_batch *b, Inst &I, int32_t steps, const fb_diff_inputs *in) {
+  DiffDev &D = I.D;
+  const int64_t N = D.N;
+  int rc;
+  D.driveAt = nullptr;
+  D.nDS = 0;
+  D.epOff = D.epList = nullptr;
+  D.trainOff = nullptr;
+  D.trainIdx = nullptr;
+  const int32_t nD = (int32_t)I.driveIdx.size();
+  if (nD > 0) {
+    // a drive schedule: the given one, else the drive as set held for every epoch (the values the
+    // reference tapes when no onEpoch changes them), which only indexes the drive gradient
+    const int32_t ep = D.driveEpoch;
+    const int64_t nEp = std::max<int64_t>(1, ((int64_t)steps + ep - 1) / ep);
+    std::vector<float> at((size_t)(nEp * nD));
+    const bool given = in && in->drive_at;
+    if (given) {
+      DCU(cudaMemcpy(at.data(), in->drive_at, at.size() * 4, cudaMemcpyDefault));
+    } else {
+      std::vector<float> dr(N);
+      DCU(cudaMemcpy(dr.data(), D.drive, N * 4, cudaMemcpyDeviceToHost));
+      for (int64_t e = 0; e < nEp; e++)
+        for (int32_t k = 0; k < nD; k++) at[e * nD + k] = dr[I.driveIdx[k]];
+    }
+    if ((rc = grow(b, &I.sched, &I.schedCap, nEp * nD))) return rc;
+    DCU(cudaMemcpy(I.sched, at.data(), at.size() * 4, cudaMemcpyHostToDevice));
+    D.driveAt = I.sched;
+    D.nDS = nD;
+    if (given) {
+      std::vector<int32_t> off, list;
+      if ((rc = set_edits(D.N, I.driven0, I.driveIdx, at.data(), nEp, off, list))) return rc;
+      if ((rc = grow(b, &I.epOff, &I.epOffCap, (int64_t)off.size())) ||
+          (rc = grow(b, &I.epList, &I.epListCap, (int64_t)list.size())))
+        return rc;
+      DCU(cudaMemcpy(I.epOff, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+      if (!list.empty()) DCU(cudaMemcpy(I.epList, list.data(), list.size() * 4, cudaMemcpyHostToDevice));
+      D.epOff = I.epOff;
+      D.epList = I.epList;
+    }
+  } else if (in && in->drive_at) {
+    return dfail(FB_EINVAL, "fb_diff_forward: a drive schedule needs drive_idx on the network");
+  }
+  if (in && in->train_off) {
+    std::vector<int64_t> off(steps + 1);
+    DCU(cudaMemcpy(off.data(), in->train_off, off.size() * 8, cudaMemcpyDefault));
+    if (off[0] < 0) return dfail(FB_EINVAL, "fb_diff_forward: train_off[0]=%lld", (long long)off[0]);
+    for (int32_t t = 0; t < steps; t++)
+      if (off[t + 1] < off[t]) return dfail(FB_EINVAL, "fb_diff_forward: train_off decreases at step %d", t);
+    const int64_t tot = off[steps];
+    if (tot > 0 && !in->train_idx) return dfail(FB_EINVAL, "fb_diff_forward: train_off without train_idx");
+    std::vector<int32_t> idx((size_t)std::max<int64_t>(tot, 1));
+    if (tot > 0) DCU(cudaMemcpy(idx.data(), in->train_idx, tot * 4, cudaMemcpyDefault));
+    for (int64_t q = off[0]; q < tot; q++)
+      if (idx[q] < 0 || idx[q] >= N) return dfail(FB_EINVAL, "fb_diff_forward: train_idx[%lld]=%d", (long long)q, idx[q]);
+    if ((rc = grow(b, &I.trainOff, &I.trainOffCap, steps + 1)) || (rc = grow(b, &I.trainIdx, &I.trainIdxCap, tot)))
+      return rc;
+    DCU(cudaMemcpy(I.trainOff, off.data(), off.size() * 8, cudaMemcpyHostToDevice));
+    if (tot > 0) DCU(cudaMemcpy(I.trainIdx, idx.data(), tot * 4, cudaMemcpyHostToDevice));
+    D.trainOff = I.trainOff;
+    D.trainIdx = I.trainIdx;
+  }
+  if (D.exact32 && !D.W32) {
+    if ((rc = talloc(b, &D.W32, std::max<int64_t>(D.E, 1))) || (rc = talloc(b, &D.signW32, N))) return rc;
+  }
+  return FB_OK;
+}
+
 uint32_t seed_state(uint32_t seed) {
   // (seed * 2654435761) >>> 0 || 1, the product in double (src/lifdiff.js:221)
   uint32_t s0 = (uint32_t)std::fmod(std::floor((double)seed * 2654435761.0), 4294967296.0);
@@ -1250,6 +1646,12 @@ extern "C" int fb_diff_batch_set(fb_diff_batch *b, int32_t inst, int32_t field, 
 
 extern "C" int fb_diff_batch_forward(fb_diff_batch *b, const fb_diff_params *p, const int32_t *steps,
                                      const uint32_t *seeds, int32_t record, float *spike_counts) {
+  return fb_diff_batch_forward_ex(b, p, steps, seeds, record, spike_counts, nullptr);
+}
+
+extern "C" int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *p, const int32_t *steps,
+                                        const uint32_t *seeds, int32_t record, float *spike_counts,
+                                        const fb_diff_inputs *in) {
   if (!b || !p || !steps || !seeds) return dfail(FB_EINVAL, "fb_diff_forward: bad arguments");
   int rc = fill_params(b, p);
   if (rc) return rc;
@@ -1276,11 +1678,20 @@ extern "C" int fb_diff_batch_forward(fb_diff_batch *b, const fb_diff_params *p, 
       if ((rc = talloc(b, &D.tOff, cap)) || (rc = talloc(b, &D.tForced, cap))) return rc;
       I.tStepsCap = cap;
     }
+    if ((rc = set_inputs(b, I, steps[k], in ? in + k : nullptr))) return rc;
   }
+  bool edits = false;
+  for (int k = 0; k < b->B; k++) edits = edits || b->in[k].D.epOff;
   if ((rc = push_devs(b)) || (rc = prepare(b, p))) return rc;
+  if (p->exact32) {
+    k_prepare_w32<<<dim3(256, b->B), kDB, 0, b->st>>>(b->dDevs, p->wSyn, p->inhGain);
+    DCU(cudaGetLastError());
+  }
   k_reset<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, (float)p->vRest);
+  const int32_t ep = std::max(1, p->drive_epoch);
   for (int32_t t = 0; t < maxSteps; t++) {
     if (record && t % p->checkpoint == 0) k_ckpt<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, t, 1);
+    if (edits && t % ep == 0) k_epoch<<<dim3(1, b->B), 1024, 0, b->st>>>(b->dDevs, t);
     run_step(b, t, 0, -1);
   }
   DCU(cudaGetLastError());
@@ -1395,6 +1806,12 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
       I.resAtCap = maxArr * K;
     }
     D.maxArr = maxArr;
+    D.gDrive = nullptr;
+    if (D.driveAt) {
+      const int64_t nd = ((steps + D.driveEpoch - 1) / D.driveEpoch) * D.nDS;
+      if ((rc = grow(b, &I.gDrive, &I.gDriveCap, nd))) return rc;
+      D.gDrive = I.gDrive;
+    }
     if (!D.lsRing) {
       if ((rc = talloc(b, &D.lsRing, (size_t)D.nslots * N))) return rc;
     }
@@ -1403,7 +1820,7 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
   if ((rc = push_devs(b))) return rc;
   const dim3 ng = neuron_grid(b);
   k_zero_adjoint<<<ng, kDB, 0, b->st>>>(b->dDevs);
-  for (int k = 0; k < b->B; k++) DCU(cudaMemsetAsync(b->in[k].D.nonfinite, 0, 4, b->st));
+  for (int k = 0; k < b->B; k++) DCU(cudaMemsetAsync(b->in[k].D.nonfinite, 0, 8, b->st));
   if ((rc = prepare(b, &b->lastP))) return rc;
   const int32_t steps = b->maxSteps;
   const int nseg = (steps + K - 1) / K;
@@ -1427,10 +1844,10 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
   k_finalize<<<ng, kDB, 0, b->st>>>(b->dDevs);
   DCU(cudaGetLastError());
   std::vector<double> part((size_t)b->B * kRB * kNSums);
-  std::vector<int32_t> nonfin(b->B);
+  std::vector<int32_t> nonfin(2 * b->B);
   DCU(cudaMemcpyAsync(part.data(), b->partial, part.size() * 8, cudaMemcpyDeviceToHost, b->st));
   for (int k = 0; k < b->B; k++)
-    DCU(cudaMemcpyAsync(&nonfin[k], b->in[k].D.nonfinite, 4, cudaMemcpyDeviceToHost, b->st));
+    DCU(cudaMemcpyAsync(&nonfin[2 * k], b->in[k].D.nonfinite, 8, cudaMemcpyDeviceToHost, b->st));
   DCU(cudaStreamSynchronize(b->st));
   for (int k = 0; k < b->B; k++) {
     const DiffDev &D = b->in[k].D;
@@ -1445,7 +1862,12 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
       if (!std::isfinite(vals[q])) { vals[q] = 0; G.clamped_params++; }
       G.params[q] = vals[q];
     }
-    G.clamped_log_gain = nonfin[k];
+    G.clamped_log_gain = nonfin[2 * k];
+    G.clamped_drive = nonfin[2 * k + 1];
+    if (G.drive && D.gDrive) {
+      const int64_t nd = ((int64_t)(D.steps + D.driveEpoch - 1) / D.driveEpoch) * D.nDS;
+      if (nd > 0) DCU(cudaMemcpyAsync(G.drive, D.gDrive, (size_t)nd * 4, cudaMemcpyDefault, b->st));
+    }
     if (G.log_gain) DCU(cudaMemcpyAsync(G.log_gain, D.gLogF, (size_t)D.N * 4, cudaMemcpyDefault, b->st));
     if (G.out_scale) DCU(cudaMemcpyAsync(G.out_scale, D.gOut, (size_t)D.N * 8, cudaMemcpyDefault, b->st));
     if (G.bias) DCU(cudaMemcpyAsync(G.bias, D.gBias, (size_t)D.N * 8, cudaMemcpyDefault, b->st));
@@ -1514,7 +1936,13 @@ extern "C" int fb_diff_set(fb_diff *d, int32_t field, const float *values) {
 extern "C" int fb_diff_forward(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed, int32_t record,
                                float *spike_count) {
   if (!d || !p || steps < 0) return dfail(FB_EINVAL, "fb_diff_forward: bad arguments");
-  return fb_diff_batch_forward(d->b, p, &steps, &seed, record, spike_count);
+  return fb_diff_batch_forward_ex(d->b, p, &steps, &seed, record, spike_count, nullptr);
+}
+
+extern "C" int fb_diff_forward_ex(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed, int32_t record,
+                                  float *spike_count, const fb_diff_inputs *in) {
+  if (!d || !p || steps < 0) return dfail(FB_EINVAL, "fb_diff_forward: bad arguments");
+  return fb_diff_batch_forward_ex(d->b, p, &steps, &seed, record, spike_count, in);
 }
 
 extern "C" int fb_diff_tape(fb_diff *d, int64_t *offsets, int32_t *idx, float *amp, int64_t cap, int64_t *len) {

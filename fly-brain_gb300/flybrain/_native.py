@@ -51,20 +51,27 @@ class FbDiffParams(C.Structure):
         "dt", "vRest", "vThresh", "vReset", "tauM", "tauSyn", "tRef", "delay", "wSyn", "adaptInc",
         "adaptTau", "depU", "depTau", "minSyn", "eExc", "eInh", "inhGain", "sizeAlpha",
         "maxSizeScale", "boostCap", "kcThreshold", "laminaBias", "surrogateBeta", "adjClip")] + [
-        (k, C.c_int32) for k in ("coba", "soft", "checkpoint", "precision")]
+        (k, C.c_int32) for k in ("coba", "soft", "checkpoint", "precision", "drive_soft", "exact32",
+                                 "drive_epoch", "pad")]
 
 
 class FbDiffNet(C.Structure):
     _fields_ = [("N", C.c_int32), ("nDriven", C.c_int32), ("E", C.c_int64)] + [
         (k, C.c_void_p) for k in ("indptr", "indices", "counts", "edge_gain", "sign", "size_log",
                                   "in_scale", "log_gain", "out_scale", "thr_offset", "beta", "bias",
-                                  "thr_mask", "bias_mask", "sensory", "drive", "driven")]
+                                  "thr_mask", "bias_mask", "sensory", "drive", "driven")] + [
+        ("nDriveIdx", C.c_int32), ("pad", C.c_int32), ("drive_idx", C.c_void_p)]
 
 
 class FbDiffGrads(C.Structure):
     _fields_ = [("params", C.c_double * 9), ("clamped_params", C.c_int32),
                 ("clamped_log_gain", C.c_int32), ("log_gain", C.c_void_p), ("edge", C.c_void_p),
-                ("bias", C.c_void_p), ("out_scale", C.c_void_p)]
+                ("bias", C.c_void_p), ("out_scale", C.c_void_p), ("drive", C.c_void_p),
+                ("clamped_drive", C.c_int32), ("pad", C.c_int32)]
+
+
+class FbDiffInputs(C.Structure):
+    _fields_ = [("drive_at", C.c_void_p), ("train_off", C.c_void_p), ("train_idx", C.c_void_p)]
 
 
 SIGNATURES = {
@@ -106,6 +113,7 @@ SIGNATURES = {
     "fb_diff_destroy": (C.c_int, [P]),
     "fb_diff_set": (C.c_int, [P, I32, P]),
     "fb_diff_forward": (C.c_int, [P, C.POINTER(FbDiffParams), I32, U32, I32, P]),
+    "fb_diff_forward_ex": (C.c_int, [P, C.POINTER(FbDiffParams), I32, U32, I32, P, C.POINTER(FbDiffInputs)]),
     "fb_diff_tape": (C.c_int, [P, P, P, P, I64, PI64]),
     "fb_diff_raster": (C.c_int, [P, I32, P, P]),
     "fb_diff_backward": (C.c_int, [P, P, I32, P, I32, I32, C.POINTER(FbDiffGrads)]),
@@ -115,6 +123,7 @@ SIGNATURES = {
     "fb_diff_batch_destroy": (C.c_int, [P]),
     "fb_diff_batch_set": (C.c_int, [P, I32, I32, P]),
     "fb_diff_batch_forward": (C.c_int, [P, C.POINTER(FbDiffParams), P, P, I32, P]),
+    "fb_diff_batch_forward_ex": (C.c_int, [P, C.POINTER(FbDiffParams), P, P, I32, P, P]),
     "fb_diff_batch_tape": (C.c_int, [P, I32, P, P, P, I64, PI64]),
     "fb_diff_batch_raster": (C.c_int, [P, I32, I32, P, P]),
     "fb_diff_batch_backward": (C.c_int, [P, P, P, P, I32, I32, C.POINTER(FbDiffGrads)]),

@@ -1,8 +1,11 @@
 """The differentiable brain on the GB300 kernels: a drop-in for the reference's LIFDiff
 (src/lifdiff.js:77-687) -- new LIFDiff(data, opts), setDrive/setDriveOne, forward(steps,
-{seed, record}) and backward(tape, dLdSpike, {truncate, lossFrom}) returning
-{params, logGain, clamped} -- plus per-edge, per-neuron-bias and outScale gradients, and a
+{seed, record, onEpoch, spikeTrain}) and backward(tape, dLdSpike, {truncate, lossFrom}) returning
+{params, logGain, drive, clamped} -- plus per-edge, per-neuron-bias and outScale gradients, and a
 torch.autograd.Function over per-edge gains, per-neuron biases and per-cell-type gains.
+
+The reference's onEpoch callback is given as its result: driveAt[epoch][k], the drive of
+driveIdx[k] from that epoch's first step, applied with setDriveOne in k order.
 """
 from __future__ import annotations
 
@@ -22,8 +25,9 @@ DIFF_DEFAULTS = dict(
     wSyn=0.3, adaptInc=0.0, adaptTau=100.0, depU=0.0, depTau=200.0, minSyn=1.0, coba=True,
     eExc=0.0, eInh=-70.0, inhGain=1.0, sizeAlpha=0.0, maxSizeScale=20.0, boostCap=1.0,
     kcThreshold=0.0, laminaBias=0.0, surrogateBeta=2.0, adjClip=0.0, soft=False, checkpoint=16,
-    precision="f64",
+    precision="f64", driveSoft=False, exact32=False, driveEpoch=1,
 )
+_INT_PARAMS = ("coba", "soft", "checkpoint", "precision", "drive_soft", "exact32", "drive_epoch", "pad")
 PRECISIONS = dict(f64=0, f32=1)
 
 _ARRAYS_N = ("size_log", "in_scale", "log_gain", "out_scale", "thr_offset", "beta", "bias")
@@ -34,10 +38,12 @@ _FIELDS = dict(log_gain=0, out_scale=1, thr_offset=2, bias=3, edge_gain=4, drive
 def make_params(p: dict) -> nat.FbDiffParams:
     q = nat.FbDiffParams()
     for k, _ in nat.FbDiffParams._fields_:
-        if k in ("coba", "soft", "checkpoint", "precision"):
+        if k in _INT_PARAMS:
             continue
         setattr(q, k, float(p[k]))
     q.coba, q.soft, q.checkpoint = int(bool(p["coba"])), int(bool(p["soft"])), int(p["checkpoint"])
+    q.drive_soft, q.exact32 = int(bool(p["driveSoft"])), int(bool(p["exact32"]))
+    q.drive_epoch = max(1, int(p["driveEpoch"] or 1))
     if p["precision"] not in PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {p['precision']!r}")
     q.precision = PRECISIONS[p["precision"]]
@@ -76,29 +82,71 @@ class _Desc:
         out.nDriven = int(driven.shape[0])
         out.drive = self.arr(n.drive.copy(), np.float32)
         out.driven = self.arr(driven if driven.shape[0] else np.zeros(1, np.int32), np.int32)
+        if n.driveIdx is not None:
+            out.nDriveIdx = int(n.driveIdx.shape[0])
+            out.drive_idx = self.arr(n.driveIdx, np.int32)
 
 
-def _grads(N, E, edge=True, device=None):
-    """An FbDiffGrads with its output arrays (numpy, or torch tensors on `device`)."""
+def _epochs(steps, p):
+    ep = max(1, int(p["driveEpoch"] or 1))
+    return (int(steps) + ep - 1) // ep
+
+
+class _Inputs:
+    """An fb_diff_inputs record: a drive schedule f32[epochs][nDriveIdx] and a spike train (one
+    index list, or None, per step) as CSR offsets and indices."""
+
+    def __init__(self, n, steps, p, driveAt=None, spikeTrain=None):
+        self.rec = nat.FbDiffInputs()
+        self.keep = []
+        if driveAt is not None:
+            if n.driveIdx is None:
+                raise ValueError("driveAt needs the network's driveIdx")
+            a = np.ascontiguousarray(driveAt, np.float32)
+            want = (_epochs(steps, p), n.driveIdx.shape[0])
+            if a.size != want[0] * want[1]:
+                raise ValueError(f"driveAt must hold {want[0]} x {want[1]} values, not {a.shape}")
+            self.keep.append(a)
+            self.rec.drive_at = a.ctypes.data
+        if spikeTrain is not None:
+            if len(spikeTrain) < steps:
+                raise ValueError(f"spikeTrain has {len(spikeTrain)} steps, the forward {steps}")
+            lens = [0 if spikeTrain[t] is None else len(spikeTrain[t]) for t in range(steps)]
+            off = np.zeros(steps + 1, np.int64)
+            np.cumsum(lens, out=off[1:])
+            idx = np.zeros(max(1, int(off[-1])), np.int32)
+            for t in range(steps):
+                if lens[t]:
+                    idx[off[t]:off[t + 1]] = np.asarray(spikeTrain[t], np.int32)
+            self.keep += [off, idx]
+            self.rec.train_off, self.rec.train_idx = off.ctypes.data, idx.ctypes.data
+
+
+def _grads(N, E, edge=True, device=None, drive_shape=None):
+    """An FbDiffGrads with its output arrays (numpy, or torch tensors on `device`); drive_shape
+    (epochs, nDriveIdx) adds the drive gradient."""
     g = nat.FbDiffGrads()
     if device is None:
         lg, gb, go = np.zeros(N, np.float32), np.zeros(N, np.float64), np.zeros(N, np.float64)
         ge = np.zeros(E, np.float64) if edge else None
+        gd = None if drive_shape is None else np.zeros(drive_shape, np.float32)
         ptr = lambda a: a.ctypes.data  # noqa: E731
     else:
         import torch
         lg = torch.zeros(N, dtype=torch.float32, device=device)
         gb, go = (torch.zeros(N, dtype=torch.float64, device=device) for _ in range(2))
         ge = torch.zeros(E, dtype=torch.float64, device=device) if edge else None
+        gd = None if drive_shape is None else torch.zeros(drive_shape, dtype=torch.float32, device=device)
         ptr = lambda a: a.data_ptr()  # noqa: E731
     g.log_gain, g.bias, g.out_scale = ptr(lg), ptr(gb), ptr(go)
     g.edge = None if ge is None else ptr(ge)
-    return g, dict(logGain=lg, edge=ge, bias=gb, outScale=go)
+    g.drive = None if gd is None else ptr(gd)
+    return g, dict(logGain=lg, edge=ge, bias=gb, outScale=go, drive=gd)
 
 
 def _grad_dict(g, arrays, truncate):
     return dict(params=dict(zip(DIFF_PARAMS, list(g.params))),
-                clamped=dict(params=g.clamped_params, logGain=g.clamped_log_gain),
+                clamped=dict(params=g.clamped_params, logGain=g.clamped_log_gain, drive=g.clamped_drive),
                 truncate=truncate, **arrays)
 
 
@@ -115,7 +163,7 @@ class DiffNet:
     """LIFDiff on the device. data: {N, indptr, indices, weights (raw counts), nt} as the
     reference takes it (or sign= for preSign); opts: model parameters and per-neuron structure
     (sizeLog, thrMask, biasMask, logGain, outScale, thrOffset, sensoryMask, edgeGain, inScale,
-    surrogateBeta as an array, bias)."""
+    surrogateBeta as an array, bias, driveIdx)."""
 
     def __init__(self, data: dict, opts: dict | None = None, tape_cap: int = 0, _defer: bool = False):
         self.L = nat.load()
@@ -144,6 +192,8 @@ class DiffNet:
             edge_gain=opts.get("edgeGain"))
         self.drive = np.zeros(self.N, np.float32)
         self.drivenSet: dict[int, None] = {}
+        di = opts.get("driveIdx")
+        self.driveIdx = None if di is None else np.ascontiguousarray(di, np.int32)
         self.h = None
         self._tape_cap = tape_cap
         if not _defer:
@@ -195,14 +245,17 @@ class DiffNet:
     def params(self, **over) -> nat.FbDiffParams:
         return make_params(dict(self.p, **over))
 
-    def forward(self, steps: int, seed: int = 1, record: bool = True, **over):
-        """Runs from reset; returns spikeCount f32[N] (src/lifdiff.js:219)."""
+    def forward(self, steps: int, seed: int = 1, record: bool = True, driveAt=None, spikeTrain=None, **over):
+        """Runs from reset; returns spikeCount f32[N] (src/lifdiff.js:219). driveAt: the drive
+        schedule f32[epochs][len(driveIdx)]; spikeTrain: per step a list of neurons to force."""
         if self._drive_dirty:
             self._create(self._tape_cap)
         sc = np.zeros(self.N, np.float32)
-        self._last = dict(steps=steps, seed=seed, over=over)
-        nat.check(self.L.fb_diff_forward(self.h, C.byref(self.params(**over)), int(steps), int(seed),
-                                         1 if record else 0, sc.ctypes.data))
+        p = dict(self.p, **over)
+        self._last = dict(steps=steps, seed=seed, over=over, p=p)
+        ins = _Inputs(self, steps, p, driveAt, spikeTrain)
+        nat.check(self.L.fb_diff_forward_ex(self.h, C.byref(make_params(p)), int(steps), int(seed),
+                                            1 if record else 0, sc.ctypes.data, C.byref(ins.rec)))
         self.spikeCount = sc
         return sc
 
@@ -231,9 +284,10 @@ class DiffNet:
     def backward(self, dLdSpike, truncate: int = 0, lossFrom: int = 0, readout=None, edge: bool = True,
                  device=None):
         """src/lifdiff.js:494: dLdSpike f32[N] (every scored step), or f32[steps][len(readout)]
-        with readout indices. Returns {params, logGain, clamped, edge, bias, outScale} (numpy, or
-        torch tensors on `device`)."""
-        g, arrays = _grads(self.N, self.E, edge, device)
+        with readout indices. Returns {params, logGain, drive, clamped, edge, bias, outScale}
+        (numpy, or torch tensors on `device`); drive is f32[epochs][len(driveIdx)] or None."""
+        ds = None if self.driveIdx is None else (_epochs(self._last["steps"], self._last["p"]), self.driveIdx.shape[0])
+        g, arrays = _grads(self.N, self.E, edge, device, ds)
         dptr, _keep = _dl_ptr(dLdSpike)
         ro = None if readout is None else np.ascontiguousarray(readout, np.int32)
         nat.check(self.L.fb_diff_backward(self.h, dptr, 0 if ro is None else ro.shape[0],
@@ -263,6 +317,7 @@ class DiffBatch:
         nat.check(self.L.fb_diff_batch_create(nets, self.B, int(tape_cap), C.byref(h)))
         self.h = h
         self._steps = [0] * self.B
+        self._p = self.p
 
     def __del__(self):
         h = getattr(self, "h", None)
@@ -280,16 +335,23 @@ class DiffBatch:
             ptr = v.ctypes.data
         nat.check(self.L.fb_diff_batch_set(self.h, int(inst), _FIELDS[key], ptr))
 
-    def forward(self, steps, seeds=1, record: bool = True, counts: bool = True, **over):
+    def forward(self, steps, seeds=1, record: bool = True, counts: bool = True, driveAt=None,
+                spikeTrain=None, **over):
         """Every member from reset for steps[b] steps with seeds[b]; returns the members' spike
-        counts (or None with counts=False)."""
+        counts (or None with counts=False). driveAt / spikeTrain: per member (lists, entries may
+        be None) as DiffNet.forward takes them."""
         st = np.broadcast_to(np.asarray(steps, np.int32), (self.B,)).copy()
         sd = np.broadcast_to(np.asarray(seeds, np.uint32), (self.B,)).copy()
         sc = np.zeros(sum(self.N), np.float32) if counts else None
-        nat.check(self.L.fb_diff_batch_forward(self.h, C.byref(make_params(dict(self.p, **over))),
-                                               st.ctypes.data, sd.ctypes.data, 1 if record else 0,
-                                               None if sc is None else sc.ctypes.data))
+        p = dict(self.p, **over)
+        ins = [_Inputs(m, int(st[b]), p, None if driveAt is None else driveAt[b],
+                       None if spikeTrain is None else spikeTrain[b]) for b, m in enumerate(self.members)]
+        recs = (nat.FbDiffInputs * self.B)(*[x.rec for x in ins])
+        nat.check(self.L.fb_diff_batch_forward_ex(self.h, C.byref(make_params(p)), st.ctypes.data,
+                                                  sd.ctypes.data, 1 if record else 0,
+                                                  None if sc is None else sc.ctypes.data, recs))
         self._steps = st.tolist()
+        self._p = p
         if sc is None:
             return None
         return np.split(sc, np.cumsum(self.N)[:-1])
@@ -334,7 +396,9 @@ class DiffBatch:
         gs = (nat.FbDiffGrads * B)()
         arrays = []
         for b in range(B):
-            g, a = _grads(self.N[b], self.E[b], edge, device)
+            m = self.members[b]
+            ds = None if m.driveIdx is None else (_epochs(self._steps[b], self._p), m.driveIdx.shape[0])
+            g, a = _grads(self.N[b], self.E[b], edge, device, ds)
             gs[b] = g
             arrays.append(a)
         nat.check(self.L.fb_diff_batch_backward(self.h, ptrs, nro.ctypes.data, ros, int(truncate), int(lossFrom), gs))

@@ -232,7 +232,11 @@ typedef struct fb_diff_params {
   double eExc, eInh, inhGain, sizeAlpha, maxSizeScale, boostCap;
   double kcThreshold, laminaBias, surrogateBeta, adjClip;
   int32_t coba, soft, checkpoint;
-  int32_t precision; /* FB_DIFF_F64 (the reference's double intermediates) or FB_DIFF_F32 */
+  int32_t precision;  /* FB_DIFF_F64 (the reference's double intermediates) or FB_DIFF_F32 */
+  int32_t drive_soft; /* driveSoft (src/lifdiff.js:102-104, :338): the drive's expected spike */
+  int32_t exact32;    /* exact32 (:105-109): the forward in lif.c's f32 arithmetic */
+  int32_t drive_epoch;/* driveEpoch (:134-144): steps a scheduled drive value is held */
+  int32_t pad;
 } fb_diff_params;
 
 /* Arithmetic of the differentiable step's intermediates. FB_DIFF_F64 is LIFDiff's (JS numbers:
@@ -261,6 +265,8 @@ typedef struct fb_diff_net {
   const uint8_t *thr_mask, *bias_mask, *sensory;
   const float *drive;
   const int32_t *driven;
+  int32_t nDriveIdx, pad;
+  const int32_t *drive_idx; /* driveIdx (src/lifdiff.js:134-144): neurons whose drive is an input */
 } fb_diff_net;
 
 /* Gradients returned by fb_diff_backward (host arrays; each pointer may be null):
@@ -274,7 +280,19 @@ typedef struct fb_diff_grads {
   int32_t clamped_params, clamped_log_gain;
   float *log_gain;
   double *edge, *bias, *out_scale;
+  float *drive;          /* [epochs][nDriveIdx]: dLoss/d(scheduled drive) (src/lifdiff.js:685) */
+  int32_t clamped_drive, pad;
 } fb_diff_grads;
+
+/* Per-forward inputs beyond the network: the drive schedule drive_at[epochs][nDriveIdx] (the
+ * values the reference's onEpoch callback sets, applied at every epoch boundary in driveIdx order
+ * with setDriveOne semantics), and a recorded spike train (spikeTrain, src/lifdiff.js:298-306):
+ * step t forces neurons train_idx[train_off[t] .. train_off[t+1]). Any pointer may be null. */
+typedef struct fb_diff_inputs {
+  const float *drive_at;
+  const int64_t *train_off;
+  const int32_t *train_idx;
+} fb_diff_inputs;
 
 typedef struct fb_diff fb_diff; /* opaque */
 
@@ -298,6 +316,9 @@ int fb_diff_set(fb_diff *d, int32_t field, const float *values);
  * record keeps the tape and a state checkpoint every p->checkpoint steps for fb_diff_backward. */
 int fb_diff_forward(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed, int32_t record,
                     float *spike_count);
+/* fb_diff_forward with a drive schedule and/or a spike train (in may be null). */
+int fb_diff_forward_ex(fb_diff *d, const fb_diff_params *p, int32_t steps, uint32_t seed, int32_t record,
+                       float *spike_count, const fb_diff_inputs *in);
 
 /* The recorded forward's spike tape: offsets i64[steps+1] (step t's spikes are entries
  * offsets[t] .. offsets[t+1]-1, forced spikes first), neuron indices and amplitudes (up to cap
@@ -330,6 +351,10 @@ int fb_diff_batch_set(fb_diff_batch *b, int32_t inst, int32_t field, const float
  * receives the instances' f32[N_b] spike totals back to back. */
 int fb_diff_batch_forward(fb_diff_batch *b, const fb_diff_params *p, const int32_t *steps,
                           const uint32_t *seeds, int32_t record, float *spike_counts);
+/* ... with per-member inputs in[B] (may be null, as may any member's pointers). */
+int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *p, const int32_t *steps,
+                             const uint32_t *seeds, int32_t record, float *spike_counts,
+                             const fb_diff_inputs *in);
 int fb_diff_batch_tape(fb_diff_batch *b, int32_t inst, int64_t *offsets, int32_t *idx, float *amp,
                        int64_t cap, int64_t *len);
 int fb_diff_batch_raster(fb_diff_batch *b, int32_t inst, int32_t nro, const int32_t *readout, float *out);

@@ -137,9 +137,10 @@ class DiffProblem:
             extra.append(da)
             G.driveAt = da.ctypes.data
         if spikeTrain is not None:  # list of index arrays, one per step
+            lists = [[] if x is None else x for x in spikeTrain[:steps]]
             off = np.zeros(steps + 1, np.int64)
-            off[1:] = np.cumsum([len(x) for x in spikeTrain[:steps]] + [0] * max(0, steps - len(spikeTrain)))
-            idx = np.concatenate([np.asarray(x, np.int32) for x in spikeTrain[:steps]] + [np.zeros(1, np.int32)])
+            off[1:] = np.cumsum([len(x) for x in lists] + [0] * max(0, steps - len(lists)))
+            idx = np.concatenate([np.asarray(x, np.int32).reshape(-1) for x in lists] + [np.zeros(1, np.int32)])
             extra += [off, idx]
             G.trainOff, G.trainIdx = off.ctypes.data, idx.ctypes.data
         return P, G, extra
