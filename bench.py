@@ -303,8 +303,10 @@ def run_batched(g, args, n_trials=256, seed=7):
         nd = int(rng.integers(500, 4001))
         idx = np.sort(rng.choice(g.N, nd, replace=False)).astype(np.int32)
         batch.set_drive(b, idx, rng.uniform(50.0, 250.0, nd))
-    batch.step(args.warmup * 10)  # warm-up, then back to rest
-    batch.reset(-1)
+    batch.step(args.warmup * 10)  # warm-up
+    from flybrain.autotune import tune_brains
+    tune = tune_brains(batch, steps=100, key=f"bench-ensemble|B={n_trials}|N={g.N}|E={g.E}")
+    batch.reset(-1)  # back to rest
     outdeg = g.outdeg().astype(np.int64)
     torch.cuda.synchronize()
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
@@ -330,6 +332,8 @@ def run_batched(g, args, n_trials=256, seed=7):
                               peak_kind=kind, traffic=None,
                               algorithmic_bytes=byts),
                 clocks=clk.summary(), gpu_launches=1,
+                tuning=dict(blocks_per_sm=tune["blocks_per_sm"], item_chunks=tune["item_chunks"],
+                            cached=tune["cached"], candidates=len(tune.get("table", []))),
                 config="256 trials x N=165,122, own seeds, durations U(200,2000) ms, drives "
                        "U{500..4000} neurons at U(50,250) Hz, 64 cell-type gains lognormal(0,0.2); "
                        "one persistent launch, uneven steps; state in HBM (no L2 flush needed: "
@@ -427,6 +431,16 @@ def _adj_loss_grads(batch, readouts, targets, dt):
     return dls, loss / batch.B
 
 
+def _tune_adjoint(batch, seeds, readouts, rng, key, steps=400):
+    """The autotuner's pick of K and the per-step launch shape for `batch`, from a recorded forward
+    and backward of `steps` steps per member with a random readout-loss gradient."""
+    from flybrain.autotune import tune_diff
+    dls = [rng.standard_normal((steps, r.shape[0])).astype(np.float32) * 1e-3 for r in readouts]
+    r = tune_diff(batch, [steps] * batch.B, seeds, dls, readouts, Ks=(50, 100, 200), key=key)
+    return dict(checkpoint=r["checkpoint"], neuron_blocks=r["neuron_blocks"], arrival_blocks=r["arrival_blocks"],
+                cached=r["cached"], candidates=len(r.get("table", [])), tuning_s=sum(x["s"] for x in r.get("table", [])))
+
+
 def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
     """Batched forward+adjoint: n_trials trials of the differentiable workload (surrogate slope
     25/mV, adjClip 100, 500 ms at dt 0.1 ms, K=100, float32 intermediates) sharing the full graph
@@ -463,6 +477,7 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
         return out, time.perf_counter() - t0
 
     batch.forward(200, seeds, counts=False)  # warm-up
+    tune = _tune_adjoint(batch, seeds, readouts, rng, f"bench-adjoint|B={n_trials}|N={g.N}|E={g.E}")
     _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
     _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
     (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
@@ -472,7 +487,8 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
     trial_s = n_trials * steps * 0.1 / 1000
     total = fwd_s + loss_s + bwd_s + sum_s
     spikes = sum(int(batch.tape(b)[0][-1]) for b in range(min(n_trials, 4)))
-    return dict(trials=n_trials, neurons=g.N, edges=g.E, steps=steps, checkpoint=100, precision=prec,
+    return dict(trials=n_trials, neurons=g.N, edges=g.E, steps=steps, checkpoint=batch.p["checkpoint"],
+                precision=prec, tuning=tune,
                 create_s=create_s, plain_batch_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s,
                 backward_s=bwd_s, edge_sum_s=sum_s, trial_s=trial_s,
                 fwd_bwd_per_trial_s=total / trial_s, plain_batch_forward_per_trial_s=plain_s / trial_s,
@@ -480,7 +496,8 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
                 grads=dict(edge_nonzero=int((ge != 0).sum()), edge_finite=bool(torch.isfinite(ge).all()),
                            bias_nonzero=int(sum(int((x["bias"] != 0).sum()) for x in gs))),
                 config=f"{n_trials} trials sharing the N=165,122 graph and its edge gains, own seeds and "
-                       "target traces; surrogate slope 25/mV, adjClip 100, 500 ms at dt 0.1 ms, K=100")
+                       "target traces; surrogate slope 25/mV, adjClip 100, 500 ms at dt 0.1 ms, K and "
+                       "launch shape autotuned")
 
 
 def run_adjoint_uneven(n_inst=128, seed=11):
@@ -525,6 +542,7 @@ def run_adjoint_uneven(n_inst=128, seed=11):
         return out, time.perf_counter() - t0
 
     batch.forward([200] * n_inst, seeds, counts=False)  # warm-up
+    tune = _tune_adjoint(batch, seeds, readouts, rng, f"bench-uneven|B={n_inst}|N={sum(batch.N)}")
     _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
     _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
     (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
@@ -533,12 +551,14 @@ def run_adjoint_uneven(n_inst=128, seed=11):
     total = fwd_s + loss_s + bwd_s
     return dict(instances=n_inst, neurons_total=int(sum(batch.N)), edges_total=int(sum(batch.E)),
                 steps_min=min(steps), steps_max=max(steps), precision=prec, graph_gen_s=gen_s,
+                checkpoint=batch.p["checkpoint"], tuning=tune,
                 plain_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s, backward_s=bwd_s,
                 trial_s=trial_s, trial_s_of_gradient_per_wall_s=trial_s / total,
                 trial_s_of_plain_forward_per_wall_s=trial_s / plain_s, cost_vs_plain_forward=total / plain_s,
                 loss=loss,
                 config=f"{n_inst} instances over synthetic subgraphs of 5,000-60,000 neurons, 100-400 ms at "
-                       "dt 0.1 ms, own drive/seed/target; surrogate slope 25/mV, adjClip 100, K=100")
+                       "dt 0.1 ms, own drive/seed/target; surrogate slope 25/mV, adjClip 100, K and launch "
+                       "shape autotuned")
 
 
 def run_reference(args, rank, world):

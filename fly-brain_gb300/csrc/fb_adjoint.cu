@@ -1036,6 +1036,7 @@ struct fb_diff_batch {
   std::vector<void *> allocs;
   fb_diff_params lastP;
   int32_t f32 = 0, recordedK = 0, recorded = 0, maxSteps = 0, maxTiles = 1, maxN = 1;
+  int32_t tuneNeuron = 0, tuneArrival = 0;  // launch shape overrides (0: default)
   DP<double> P64;
   DP<float> P32;
   int32_t *err = nullptr, *nonfinite = nullptr;
@@ -1387,10 +1388,14 @@ int check_err(fb_diff_batch *b, const char *fn) {
 // 256-thread blocks over the whole batch otherwise; warp-per-arrival kernels 304 blocks over the
 // batch (at least two per instance).
 dim3 neuron_grid(const fb_diff_batch *b) {
+  if (b->tuneNeuron > 0) return dim3(std::min(b->maxTiles, b->tuneNeuron), b->B);
   const int gx = b->B == 1 ? b->maxTiles : std::max(1, std::min(b->maxTiles, 1216 / b->B));
   return dim3(gx, b->B);
 }
-dim3 arrival_grid(const fb_diff_batch *b) { return dim3(std::max(2, 304 / b->B), b->B); }
+dim3 arrival_grid(const fb_diff_batch *b) {
+  if (b->tuneArrival > 0) return dim3(b->tuneArrival, b->B);
+  return dim3(std::max(2, 304 / b->B), b->B);
+}
 
 template <typename R>
 void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int32_t row) {
@@ -1621,6 +1626,14 @@ extern "C" int fb_diff_batch_create(const fb_diff_net *nets, int32_t B, int64_t 
   if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(dfail(FB_ECUDA, "fb_diff_batch_create: stream creation failed"));
   *out = b;
+  return FB_OK;
+}
+
+extern "C" int fb_diff_batch_set_tuning(fb_diff_batch *b, const fb_diff_tuning *t) {
+  if (!b || !t || t->neuron_blocks < 0 || t->arrival_blocks < 0 || t->arrival_blocks > 65535)
+    return dfail(FB_EINVAL, "fb_diff_batch_set_tuning: bad arguments");
+  b->tuneNeuron = t->neuron_blocks;
+  b->tuneArrival = t->arrival_blocks;
   return FB_OK;
 }
 

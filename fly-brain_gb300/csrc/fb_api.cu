@@ -428,6 +428,8 @@ struct fb_brains {
   std::vector<double> dts;   // each brain's dt as given (double), for setBackground
   int grid = 0;
   size_t smem = 0;
+  int blocksPerSm = 0, maxBlocksPerSm = 0, sms = 0;  // the persistent grid: sms x blocksPerSm
+  int32_t itemChunks = 1;
   int logging = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float lastMs = 0.f;
@@ -601,6 +603,8 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
   const int per = step_kernel_blocks_per_sm(br->smem);
   if (per <= 0) return brains_fail_cleanup(br, fail(FB_ECUDA, "step kernel does not fit on an SM (smem %zu)", br->smem));
   br->grid = sms * per;
+  br->sms = sms;
+  br->blocksPerSm = br->maxBlocksPerSm = per;
   cudaEventCreate(&br->ev0);
   cudaEventCreate(&br->ev1);
   if (cudaStreamSynchronize(br->stream) != cudaSuccess)
@@ -634,6 +638,28 @@ extern "C" int fb_brains_set_schedule(fb_brains *br, int32_t schedule) {
   if (!br || schedule < FB_SCHEDULE_AUTO || schedule > FB_SCHEDULE_LAGGED)
     return fail(FB_EINVAL, "fb_brains_set_schedule: bad schedule %d", schedule);
   br->schedule = schedule;
+  return FB_OK;
+}
+
+extern "C" int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t) {
+  if (!br || !t) return fail(FB_EINVAL, "fb_brains_set_tuning: null argument");
+  if (t->blocks_per_sm < 0 || t->blocks_per_sm > br->maxBlocksPerSm || t->item_chunks < 0 || t->item_chunks > 64)
+    return fail(FB_EINVAL, "fb_brains_set_tuning: blocks_per_sm %d (1..%d), item_chunks %d (1..64)", t->blocks_per_sm,
+                br->maxBlocksPerSm, t->item_chunks);
+  if (t->blocks_per_sm) {
+    br->blocksPerSm = t->blocks_per_sm;
+    br->grid = br->sms * br->blocksPerSm;
+  }
+  if (t->item_chunks) br->itemChunks = t->item_chunks;
+  return FB_OK;
+}
+
+extern "C" int fb_brains_tuning(fb_brains *br, fb_tuning *t) {
+  if (!br || !t) return fail(FB_EINVAL, "fb_brains_tuning: null argument");
+  t->blocks_per_sm = br->blocksPerSm;
+  t->item_chunks = br->itemChunks;
+  t->max_blocks_per_sm = br->maxBlocksPerSm;
+  t->sms = br->sms;
   return FB_OK;
 }
 
@@ -994,6 +1020,7 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     a.ovfTop = br->d_ovfTop;
     a.ovfCap = br->ovfCap;
     a.log = br->logging;
+    a.itemChunks = br->itemChunks;
     a.timeoutNs = 5000000000LL;
     a.dbg = br->d_dbg;
     CU(cudaEventRecord(br->ev0, br->stream));

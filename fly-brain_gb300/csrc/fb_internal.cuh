@@ -98,6 +98,8 @@ struct StepArgs {
   uint32_t *ovfTop;          // [2]
   uint32_t ovfCap;
   int32_t log;               // 1: record per-step fired counts / lists
+  int32_t itemChunks;        // kChunk-edge delivery chunks per warp work item (>= 1)
+  int32_t pad1;
   int64_t timeoutNs;
   uint32_t *dbg;             // checked builds: [site, value, value, count] of the first bad index
 };

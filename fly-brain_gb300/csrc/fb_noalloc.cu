@@ -225,6 +225,7 @@ extern "C" int fb_lif_step_noalloc(fb_brain_view *v, int32_t nsteps, void *strea
 
   StepArgs a;
   memset(&a, 0, sizeof a);
+  a.itemChunks = 1;
   a.trials = Td;
   a.B = 1;
   a.maxSteps = nsteps;

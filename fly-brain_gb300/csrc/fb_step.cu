@@ -618,7 +618,8 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
           const Trial &T = hdr(b);
           if (T.mode != FB_DELIVER_SEQUENTIAL) {
             const int head = (sHead0[b] + s) % sNs[b];
-            n = (ldcg(T.slotEdges + head) + kChunk - 1) / kChunk;
+            const uint32_t per = (uint32_t)kChunk * (uint32_t)a.itemChunks;
+            n = (ldcg(T.slotEdges + head) + per - 1) / per;
           }
         }
         uint32_t tot;
@@ -640,7 +641,9 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
       }
       const Trial &T = hdr(lo);
       const int head = (sHead0[lo] + s) % sNs[lo];
-      deliver_chunk(a, T, a.trials + lo, head, ldcg(T.slotEdges + head), w - sPre[lo], (uint32_t)(s & 1));
+      const uint32_t F = ldcg(T.slotEdges + head), c0 = (w - sPre[lo]) * (uint32_t)a.itemChunks;
+      for (int u = 0; u < a.itemChunks && (c0 + u) * (uint32_t)kChunk < F; u++)
+        deliver_chunk(a, T, a.trials + lo, head, F, c0 + u, (uint32_t)(s & 1));
     }
     lap(1);
     if (!grid_sync(a)) return;

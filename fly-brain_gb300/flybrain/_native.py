@@ -70,6 +70,14 @@ class FbDiffGrads(C.Structure):
                 ("clamped_drive", C.c_int32), ("pad", C.c_int32)]
 
 
+class FbTuning(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in ("blocks_per_sm", "item_chunks", "max_blocks_per_sm", "sms")]
+
+
+class FbDiffTuning(C.Structure):
+    _fields_ = [("neuron_blocks", C.c_int32), ("arrival_blocks", C.c_int32)]
+
+
 class FbDiffInputs(C.Structure):
     _fields_ = [("drive_at", C.c_void_p), ("train_off", C.c_void_p), ("train_idx", C.c_void_p)]
 
@@ -119,6 +127,9 @@ SIGNATURES = {
     "fb_diff_backward": (C.c_int, [P, P, I32, P, I32, I32, C.POINTER(FbDiffGrads)]),
     "fb_brains_set_schedule": (C.c_int, [P, I32]),
     "fb_last_schedule": (C.c_int, [P, C.POINTER(C.c_int32)]),
+    "fb_brains_set_tuning": (C.c_int, [P, C.POINTER(FbTuning)]),
+    "fb_brains_tuning": (C.c_int, [P, C.POINTER(FbTuning)]),
+    "fb_diff_batch_set_tuning": (C.c_int, [P, C.POINTER(FbDiffTuning)]),
     "fb_diff_batch_create": (C.c_int, [C.POINTER(FbDiffNet), I32, I64, C.POINTER(P)]),
     "fb_diff_batch_destroy": (C.c_int, [P]),
     "fb_diff_batch_set": (C.c_int, [P, I32, I32, P]),

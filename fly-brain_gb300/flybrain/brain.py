@@ -155,6 +155,16 @@ class BrainBatch:
         nat.check(self.L.fb_last_schedule(self.h, C.byref(x)))
         return x.value
 
+    def set_tuning(self, blocks_per_sm: int = 0, item_chunks: int = 0):
+        """Launch shape of the grid schedule (fb_brains_set_tuning); 0 keeps a knob."""
+        t = nat.FbTuning(int(blocks_per_sm), int(item_chunks), 0, 0)
+        nat.check(self.L.fb_brains_set_tuning(self.h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = nat.FbTuning()
+        nat.check(self.L.fb_brains_tuning(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in nat.FbTuning._fields_}
+
     def step(self, nsteps: int = 1) -> np.ndarray:
         out = np.zeros(self.B, dtype=np.int32)
         nat.check(self.L.fb_step(self.h, int(nsteps), nat.ptr(out)))

@@ -325,6 +325,12 @@ class DiffBatch:
             self.L.fb_diff_batch_destroy(h)
             self.h = None
 
+    def set_tuning(self, neuron_blocks: int = 0, arrival_blocks: int = 0):
+        """Launch shape of the per-step kernels (fb_diff_batch_set_tuning); 0 = default."""
+        t = nat.FbDiffTuning(int(neuron_blocks), int(arrival_blocks))
+        nat.check(self.L.fb_diff_batch_set_tuning(self.h, C.byref(t)))
+        self.tuning = dict(neuron_blocks=int(neuron_blocks), arrival_blocks=int(arrival_blocks))
+
     def set_array(self, inst: int, name: str, values):
         key = {"logGain": "log_gain", "outScale": "out_scale", "thrOffset": "thr_offset",
                "bias": "bias", "edgeGain": "edge_gain", "drive": "drive"}.get(name, name)

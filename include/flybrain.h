@@ -148,6 +148,18 @@ int fb_brains_set_schedule(fb_brains *br, int32_t schedule);
 /* The schedule the last fb_step / fb_step_uneven launch ran (FB_SCHEDULE_GRID or _LAGGED). */
 int fb_last_schedule(fb_brains *br, int32_t *schedule);
 
+/* Launch shape of the grid schedule's persistent kernel, the knobs the autotuner
+ * (flybrain.autotune) searches: resident CTAs per SM (1 .. max_blocks_per_sm; the grid is
+ * sms x blocks_per_sm, 512 threads each) and kChunk = 32-edge delivery chunks per warp work item
+ * (edges per warp item = 32 x item_chunks, 1 .. 64). fb_brains_set_tuning ignores max_blocks_per_sm
+ * and sms; 0 in a field keeps its current value. Results do not depend on the shape. */
+typedef struct fb_tuning {
+  int32_t blocks_per_sm, item_chunks;
+  int32_t max_blocks_per_sm, sms; /* read only */
+} fb_tuning;
+int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t);
+int fb_brains_tuning(fb_brains *br, fb_tuning *t);
+
 /* Advances every brain by nsteps steps in one persistent launch (lif_step, src/wasm/lif.c:29-80,
  * nsteps times). out_nfired (optional, int32[B]) receives each brain's fired count of its last
  * step: the value lif_step returns. */
@@ -349,6 +361,15 @@ int fb_diff_batch_set(fb_diff_batch *b, int32_t inst, int32_t field, const float
 
 /* Forward of every instance from reset: steps[B] and seeds[B]; spike_counts (may be null)
  * receives the instances' f32[N_b] spike totals back to back. */
+/* Launch shape of the per-step kernels (the autotuner's knobs): blocks per member of the
+ * thread-per-neuron kernels (256 threads; at most the member's tile count is used) and of the
+ * warp-per-arrival kernels. 0 restores the default (one tile per block for one member, about
+ * four waves over the batch otherwise; 304 blocks over the batch). Results do not depend on it. */
+typedef struct fb_diff_tuning {
+  int32_t neuron_blocks, arrival_blocks;
+} fb_diff_tuning;
+int fb_diff_batch_set_tuning(fb_diff_batch *b, const fb_diff_tuning *t);
+
 int fb_diff_batch_forward(fb_diff_batch *b, const fb_diff_params *p, const int32_t *steps,
                           const uint32_t *seeds, int32_t record, float *spike_counts);
 /* ... with per-member inputs in[B] (may be null, as may any member's pointers). */
