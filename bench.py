@@ -390,6 +390,11 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3):
         raster = LIFDiffFunction.apply(eg, bias, tg, dctx)
         return ((lowpass_rates(raster, 0.1) - target) ** 2).mean()
 
+    # warm-up of the whole autograd path: the first float64 cumsum of a process loads (on some
+    # builds JIT-compiles) torch's scan kernel, seconds that belong to no step
+    fwd().backward()
+    for p_ in (eg, bias, tg):
+        p_.grad = None
     loss, fwd_s = clock(fwd)
     _, bwd_s = clock(loss.backward)
     sim_s = steps * 0.1 / 1000
@@ -398,7 +403,7 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3):
                 plain_forward_s=plain, library_forward_recorded_s=lib_fwd, library_backward_s=lib_bwd,
                 autograd_forward_s=fwd_s, autograd_backward_s=bwd_s,
                 fwd_bwd_per_trial_s=(fwd_s + bwd_s) / sim_s, plain_per_trial_s=plain / sim_s,
-                cost_vs_plain_forward=(fwd_s + bwd_s) / plain, loss=float(loss),
+                cost_vs_plain_forward=(fwd_s + bwd_s) / plain, loss=float(loss.detach()),
                 spikes=int(net.tape()[0][-1]),
                 grads=dict(edge_nonzero=int((ge != 0).sum()), edge_finite=bool(torch.isfinite(ge).all()),
                            bias_nonzero=int((gb != 0).sum()), type_gain=[float(x) for x in gt[:4]]),

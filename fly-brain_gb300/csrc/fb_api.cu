@@ -821,7 +821,9 @@ static bool lag_applies(fb_brains *br, int32_t steps, const char **why) {
   else if (T.mode != FB_DELIVER_EXACT || (T.flags & kHasPreInh)) *why = "a delivery mode other than exact without presynaptic inhibition";
   else if (br->profiling && br->schedule != FB_SCHEDULE_LAGGED) *why = "phase profiling";
   else if (br->logging && steps > kLagRing) *why = "per-step logging of a launch longer than 64 steps";
-  else if (T.nslots - 1 < kHelp + 1 || T.nslots - 1 > 32) *why = "a ring depth outside 4..33 slots";
+  // a block's wait at step s (for step s - L, L = D - kHelp) must not need its own completion of
+  // that step, which it publishes at step s - L + 1: L >= 2
+  else if (T.nslots - 1 < kHelp + 2 || T.nslots - 1 > 32) *why = "a ring depth outside 5..33 slots";
   else if (T.bgEvents > (float)(1 << 20)) *why = "more than 2^20 background events per step";
   return *why == nullptr;
 }
