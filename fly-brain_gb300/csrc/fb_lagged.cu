@@ -49,6 +49,8 @@ struct LagShared {
   int32_t nLocal;  // neurons owned by this block
   int32_t idLo, idHi;
   int32_t stop;
+  int32_t stopP[2];  // the lag check's verdict, by step parity (the driven block's steps have one
+                     // barrier, so thread 0 may write step s + 1's before a slow warp reads step s's)
   uint32_t rng;
   float bgAcc;
   int32_t nbg;
@@ -58,12 +60,19 @@ struct LagShared {
   int64_t logBase;
   uint32_t scan[33];
   uint64_t scan64[33];
-  uint32_t wfirst[kMaxPer * 32];  // driven block: first live rank of each warp and round
-  uint32_t wstate[kMaxPer * 32];  // ... and the generator state there
-  uint32_t dbCount;               // driven block: spikes of the step
-  uint32_t rngNext;               // driven block: generator state after the step
-  uint32_t cstate[kMaxPer * kLagThreads / 32];  // driven block: state at every 32nd draw
+  uint32_t dbCount;               // epilogue scratch
+  // driven block, by step parity: each step prepares the next one's inputs while it runs, so a
+  // step needs one block barrier. Live entries per warp and round (ballots after the previous
+  // update), the generator at the step's start, its states at every 32nd driven draw, the
+  // background draws, the accumulator after them, and the step's spike count.
+  uint32_t wcnt[2][kMaxPer * 32];
+  uint32_t cst[2][kMaxPer * kLagThreads / 32];
+  uint32_t rngP[2];
+  int32_t nbgP[2];
+  float bgAccP[2];
+  uint32_t dbCnt2[2];
 };
+
 
 __device__ __forceinline__ bool lag_timeout(const LagArgs &a, uint64_t t0, uint32_t &it) {
   if ((++it & 63u) == 0) {
@@ -389,6 +398,50 @@ __device__ void collect_bg(const LagArgs &a, LagShared &sh, const LagState &S, u
   }
 }
 
+// The driven block's generator work for step t, done by one warp while the others update the
+// step before: the state at the start of step t (`s0`), its background draw count (the
+// accumulator advanced by lane 0, lif.c:46-47) and the states M^(32 q) M^(nbg+1) s0 at every 32nd
+// driven draw (lane j: q = j, 32 + j, ...).
+__device__ __forceinline__ void driven_prepare(const LagArgs &a, LagShared &sh, const uint32_t *sHex, int par,
+                                               uint32_t s0, float accIn) {
+  const uint32_t j = threadIdx.x & 31u;
+  uint32_t nbg = 0;
+  if (a.hasBg) {
+    if (j == 0) {
+      const float acc = __fadd_rn(accIn, a.bgEvents);
+      const int32_t n = (int32_t)acc;
+      sh.bgAccP[par] = __fsub_rn(acc, (float)n);
+      if (n > a.bgCap) atomicCAS(a.err, 0, FB_EOVERFLOW);
+      nbg = (uint32_t)min(n, a.bgCap);
+    }
+    nbg = __shfl_sync(0xffffffffu, nbg, 0);
+  }
+  if (j == 0) {
+    sh.nbgP[par] = (int32_t)nbg;
+    sh.rngP[par] = s0;
+  }
+  const uint32_t b0 = xs_jump_hex(sHex, s0, nbg + 1u);
+  const uint32_t nq = (uint32_t)(a.nD + 31) / 32;
+  uint32_t c = xs_jump_hex(sHex, b0, 32u * j);
+  for (uint32_t q = j; q < nq; q += 32) {
+    sh.cst[par][q] = c;
+    c = xs_apply(sHex + (2 * 15 + 4 - 1) * 128, c);  // M^1024 = M^(4 * 16^2)
+  }
+}
+
+// The driven block's live entries per warp and round for the coming step (ballots over the
+// refractory state, lif.c:50).
+__device__ __forceinline__ void driven_ballots(const LagArgs &a, LagShared &sh, const LagState &S, int par) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < kMaxPer; r++) {
+    const int k = threadIdx.x + r * kLB;
+    const bool live = r < a.m && k < a.nD && !(S.r[k] > 0);
+    const uint32_t wm = __ballot_sync(0xffffffffu, live);
+    if (lane == 0 && r < a.m) sh.wcnt[par][r * 32 + warp] = __popc(wm);
+  }
+}
+
 __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ LagShared sh;
@@ -406,6 +459,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   // ---------------- prologue: own state into shared memory ----------------
   if (tid == 0) {
     sh.stop = 0;
+    sh.stopP[0] = sh.stopP[1] = 0;
     sh.known = -1;
     sh.dbCount = 0;
     sh.head0 = ldcg(&a.G->head);
@@ -508,6 +562,11 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     }
   }
   if (!lag_grid_sync(a)) return;
+  if (drivenBlock) {  // step 0's inputs
+    driven_ballots(a, sh, S, 0);
+    if ((int)tid >= (int)blockDim.x - 32) driven_prepare(a, sh, sHex, 0, sh.rng, sh.bgAcc);
+    if (tid == 0) sh.dbCnt2[0] = sh.dbCnt2[1] = 0;
+  }
 
   // ---------------- the steps ----------------
   // this thread's neurons: k = tid + r * kLB (r < per); for the driven block the list in order,
@@ -525,6 +584,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   uint32_t dbKnown = 0;     // tile blocks: driven-block steps known finished (thread 0)
   uint64_t tp = a.prof != nullptr ? global_ns() : 0;
   const int pb = drivenBlock ? 0 : 5;  // phase slots of this block
+  int sEnd = a.T;                      // the steps run (fewer after a failed wait)
   for (int s = 0; s < a.T; s++) {
     const int slot = s % a.S;
     const int ring = s & (kLagRing - 1);
@@ -538,23 +598,31 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         if (ok) sh.known = need;
       }
       if (ok && !drivenBlock && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s + 1));
-      sh.stop = ok ? 0 : 1;
+      sh.stopP[s & 1] = ok ? 0 : 1;
     }
     __syncthreads();
-    if (sh.stop) break;
+    if (sh.stopP[s & 1]) {
+      sEnd = s;
+      break;
+    }
     // step s - 1 is complete in this block (the barrier above): its completion is published now,
     // so the release's wait for the block's writes overlaps this step's work. The publishing
     // thread is in the second-last warp, which has the fewest neurons (thread 0 checks the lag).
     if ((int)tid == (int)blockDim.x - 64 && s > 0) {
       const int sp = s - 1;
       if (drivenBlock) {
+        const uint32_t n = sh.dbCnt2[sp & 1];
+        sh.dbCnt2[sp & 1] = 0;
+        a.dbCnt[sp & (kLagRing - 1)] = (int32_t)n;
+        if (a.log) atomicAdd(a.stepTot + sp, (int32_t)n);
         st_release(a.dbDone, (uint32_t)s);  // the spike list and count of step s - 1
         atomicAdd(a.done + (sp & (kLagRing - 1)), 1u);  // the driven block pushes nothing itself
       } else {
         red_release(a.done + (sp & (kLagRing - 1)), 1u);
       }
-      if ((sp & 7) == 7) {  // now and then: a later step known finished everywhere
-        const int probe = sp - 2;
+      if ((sp & 3) == 3) {  // now and then: a later step known finished everywhere, which keeps
+        // the count prefetch two steps ahead going (it needs step s + 2 - L finished)
+        const int probe = sp - 5;
         if (probe > sh.known && ld_acquire(a.done + (probe & (kLagRing - 1))) >= done_target(probe, gridDim.x))
           sh.known = probe;
       }
@@ -592,41 +660,35 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     }
 
     if (drivenBlock) {
+      const int par = s & 1, parN = par ^ 1;
+      const int m = a.m;
+      const uint32_t nbg = (uint32_t)sh.nbgP[par], s0 = sh.rngP[par];
       // background draws 1..nbg (lif.c:46-48), published for every block
       if (a.hasBg) {
-        if (tid == 0) {
-          const float acc = __fadd_rn(sh.bgAcc, a.bgEvents);
-          const int32_t nbg = (int32_t)acc;
-          sh.bgAcc = __fsub_rn(acc, (float)nbg);
-          sh.nbg = min(nbg, a.bgCap);
-          if (nbg > a.bgCap) atomicCAS(a.err, 0, FB_EOVERFLOW);
-          a.bgCount[ring] = sh.nbg;
-        }
-        __syncthreads();
-        const uint32_t s0 = sh.rng;
-        for (int d = 1 + tid; d <= sh.nbg; d += blockDim.x)
+        if (tid == 0) a.bgCount[ring] = (int32_t)nbg;
+        for (int d = 1 + tid; d <= (int)nbg; d += blockDim.x)
           a.bgList[(int64_t)ring * a.bgCap + d - 1] = xs_jump_hex(sHex, s0, (uint32_t)d) % (uint32_t)a.N;
         __syncthreads();
         if (tid == 0) st_release(a.bgReady, (uint32_t)(s + 1));
         collect_bg(a, sh, S, sBg, s, true);
-      } else if (tid == 0) {
-        sh.nbg = 0;
       }
-      // generator states at every 32nd driven draw: C_q = M^(32 q) B0, B0 = M^(nbg+1) s0 (the first
-      // driven draw). The last warp computes them while the others start on the deliveries; its
-      // lane j takes q = j, 32 + j, 64 + j, 96 + j.
-      const int m = a.m;
-      if ((int)tid >= (int)blockDim.x - 32) {  // the last warp (thread 0 publishes completion)
-        const uint32_t j = tid & 31u;
-        const uint32_t nbg0 = a.hasBg ? (uint32_t)sh.nbg : 0u;  // published before a barrier
-        const uint32_t b0 = xs_jump_hex(sHex, sh.rng, nbg0 + 1u);
-        const uint32_t nq = (uint32_t)(a.nD + 31) / 32;
-        uint32_t c = xs_jump_hex(sHex, b0, 32u * j);
-        for (uint32_t q = j; q < nq; q += 32) {
-          sh.cstate[q] = c;
-          c = xs_apply(sHex + (2 * 15 + 4 - 1) * 128, c);  // M^1024 = M^(4 * 16^2)
-        }
+      // each warp's first draw among the step's live entries, from the ballots taken at the end
+      // of the last step: (live entries of earlier rounds) + (live entries of earlier warps)
+      const uint32_t lane = tid & 31u, warp = tid >> 5, ltMask = (1u << lane) - 1u;
+      const uint32_t nwarps = blockDim.x >> 5;
+      uint32_t totLive = 0, wfirst[kMaxPer];
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        wfirst[r] = totLive;
+        if (r >= m) continue;
+        const uint32_t v = lane < nwarps ? sh.wcnt[par][r * 32 + lane] : 0u;
+        wfirst[r] = totLive + __reduce_add_sync(0xffffffffu, lane < warp ? v : 0u);
+        totLive += __reduce_add_sync(0xffffffffu, v);
       }
+      // the last warp prepares the next step's generator states: after this step's nbg
+      // background and totLive driven draws
+      if ((int)tid >= (int)blockDim.x - 32)
+        driven_prepare(a, sh, sHex, parN, xs_jump_hex(sHex, s0, nbg + totLive), a.hasBg ? sh.bgAccP[par] : 0.f);
       // entries k = tid + r * kLB (r < m), the driven list in order round by round
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
@@ -634,50 +696,18 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         if (r < m && k < a.nD) receive(a, S, k, nCur[r], a.N + k, slot, haveE, eCur[r]);
       }
       lap(a, 1, tp);
-      // the draws in list order: one per non-refractory entry (lif.c:49-52). The first driven
-      // draw is state M^(nbg+1) s0; within round r, warp w's first live entry is draw
-      // (live entries of earlier rounds) + (live entries of round r before the warp) further, and
-      // its lanes step on by their rank among the warp's live entries (lane tables M^l).
-      const uint32_t lane = tid & 31u, warp = tid >> 5, ltMask = (1u << lane) - 1u;
-      const uint32_t nwarps = blockDim.x >> 5;
-      // live entries per warp and round (ballots), then each warp finds its place from the
-      // per-warp counts: one barrier
-      uint32_t liveMask = 0;  // bit r: entry r of this thread is live
-#pragma unroll
-      for (int r = 0; r < kMaxPer; r++) {
-        const int k = tid + r * kLB;
-        const bool live = r < m && k < a.nD && !(S.r[k] > 0);
-        const uint32_t wm = __ballot_sync(0xffffffffu, live);
-        if (live) liveMask |= 1u << r;
-        if (lane == 0 && r < m) sh.wfirst[r * 32 + warp] = __popc(wm);
-      }
-      __syncthreads();
-      const uint32_t nbg = (uint32_t)sh.nbg;
-      uint32_t totLive = 0, wfirst[kMaxPer];
-#pragma unroll
-      for (int r = 0; r < kMaxPer; r++) {
-        wfirst[r] = totLive;
-        if (r >= m) continue;
-        const uint32_t v = lane < nwarps ? sh.wfirst[r * 32 + lane] : 0u;
-        wfirst[r] = totLive + __reduce_add_sync(0xffffffffu, lane < warp ? v : 0u);
-        totLive += __reduce_add_sync(0xffffffffu, v);
-      }
-      uint32_t nforced = 0, firedMask = 0, lastLive = 0, x = 0;
-      bool hasLast = false;
-      const uint32_t s0 = sh.rng;
+      // the draws in list order: one per non-refractory entry (lif.c:49-52). Entry k's draw is
+      // its rank p among the live entries: M^(p mod 32) C_(p / 32) (lane tables M^l)
+      uint32_t firedMask = 0;
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         if (r >= m) break;
         const int k = tid + r * kLB;
-        const bool live = (liveMask >> r) & 1u;
+        const bool live = k < a.nD && !(S.r[k] > 0);
         const uint32_t wmask = __ballot_sync(0xffffffffu, live);
-        if (live) {  // draw p = its rank among all live entries: M^(p mod 32) C_(p / 32)
-          const uint32_t rank = __popc(wmask & ltMask), p = wfirst[r] + rank;
-          x = xs_apply_lane(sOff, p & 31u, sh.cstate[p >> 5]);  // lanes hold distinct p mod 32
-          if (p + 1 == totLive) {
-            hasLast = true;
-            lastLive = x;
-          }
+        if (live) {
+          const uint32_t p = wfirst[r] + __popc(wmask & ltMask);
+          const uint32_t x = xs_apply_lane(sOff, p & 31u, sh.cst[par][p >> 5]);  // lanes hold distinct p mod 32
           const float u = __fmul_rn((float)(x >> 8), 1.0f / 16777216.0f);
           if (u < __fmul_rn(S.drive[k], a.dtS)) {  // lif.c:52
             S.v[k] = a.vReset;
@@ -686,15 +716,8 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
             S.tr[k] = 1.f;
             S.ad[k] = __fadd_rn(S.ad[k], a.adaptInc);
             firedMask |= 1u << r;
-            nforced++;
           }
         }
-      }
-      // the generator after the step: the state of the last draw, else after the nbg draws
-      if (totLive == 0) {
-        if (tid == 0) sh.rngNext = xs_jump_hex(sHex, s0, nbg);
-      } else if (hasLast) {
-        sh.rngNext = lastLive;
       }
       lap(a, 2, tp);
       uint32_t thrMask = 0;
@@ -703,9 +726,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         const int k = tid + r * kLB;
         if (r < m && k < a.nD) {
           const bool f = integrate(a, S, k);
-          if (f) {
-            thrMask |= 1u << r;
-          }
+          if (f) thrMask |= 1u << r;
           emit(a, S, k, f || ((firedMask >> r) & 1u));
         }
       }
@@ -717,21 +738,15 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         const int k = tid + r * kLB;
         const bool forced = (firedMask >> r) & 1u, thr = (thrMask >> r) & 1u;
         if (forced || thr) {
-          const uint32_t e = atomicAdd(&sh.dbCount, 1u);
+          const uint32_t e = atomicAdd(&sh.dbCnt2[par], 1u);
           out[2 * e] = make_uint4((uint32_t)S.id[k], forced ? (uint32_t)k : (uint32_t)(a.nD + S.id[k]),
                                   __float_as_uint(S.amp[k]), 0u);
           out[2 * e + 1] = make_uint4(S.row0[k], S.row1[k], 0u, 0u);
         }
       }
-      __syncthreads();
       lap(a, 3, tp);
-      if (tid == 0) {
-        sh.rng = sh.rngNext;
-        const uint32_t n = sh.dbCount;
-        sh.dbCount = 0;
-        a.dbCnt[ring] = (int32_t)n;
-        if (a.log) atomicAdd(a.stepTot + s, (int32_t)n);
-      }
+      // the next step's live entries (the count is published at the next step's start)
+      driven_ballots(a, sh, S, parN);
       lap(a, 4, tp);
       continue;
     }
@@ -784,7 +799,10 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         sh.stop = ok ? 0 : 1;
       }
       __syncthreads();
-      if (sh.stop) break;
+      if (sh.stop) {
+        sEnd = s;
+        break;
+      }
       const int nsp = ldcg(a.dbCnt + rp);
       for (int e = b + a.nTB * (tid >> 5); e < nsp; e += a.nTB * (blockDim.x >> 5)) {
         const uint4 x = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2);
@@ -802,6 +820,11 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
 
   // ---------------- epilogue ----------------
   __syncthreads();
+  if (drivenBlock && (int)tid == (int)blockDim.x - 64 && a.T > 0 && sEnd == a.T) {  // the last step's count
+    const int sp = a.T - 1;
+    a.dbCnt[sp & (kLagRing - 1)] = (int32_t)sh.dbCnt2[sp & 1];
+    if (a.log) atomicAdd(a.stepTot + sp, (int32_t)sh.dbCnt2[sp & 1]);
+  }
   const bool ok = lag_grid_sync(a);
   if (!ok) return;
   for (int k = tid; k < nLocal; k += blockDim.x) {
@@ -925,8 +948,8 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     const int64_t g = steps0 + a.T;
     a.G->head = (head0 + a.T) % ns;
     a.G->stepsDone = g;
-    a.G->rngP[g & 1] = sh.rng;
-    a.G->bgAccP[g & 1] = sh.bgAcc;
+    a.G->rngP[g & 1] = sh.rngP[a.T & 1];  // the state at the start of step T
+    a.G->bgAccP[g & 1] = (a.hasBg && a.T > 0) ? sh.bgAccP[(a.T - 1) & 1] : sh.bgAcc;
   }
 }
 
