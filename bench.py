@@ -268,6 +268,9 @@ def run_ours(args, rank, world):
         bt = run_batched(g, args, n_trials=int(os.environ.get("FB_BATCH_TRIALS", "256")))
         bt["cost_vs_plain_per_trial_s"] = (1.0 / bt["trial_s_per_wall_s"]) / (dev_s / sim_s)
         res["batched"] = bt
+    if os.environ.get("FB_BENCH_FLYVIS", "1") == "1":
+        torch.cuda.empty_cache()
+        res["flyvis"] = run_flyvis(n_eyes=int(os.environ.get("FB_FLYVIS_EYES", "64")))
     if rank == 0:
         sample = int(os.environ.get("FB_CPU_SAMPLE_STEPS", "4000"))
         v, secs, ev = cpu_baseline(g, idx, hz, SYNTH_PARAMS, sample)
@@ -275,6 +278,53 @@ def run_ours(args, rank, world):
                                    sample=f"{sample} brain steps of the same workload from rest "
                                           f"({secs:.1f} s, oracle port of lif_step, 1 thread)")
         print(json.dumps(res), flush=True)
+
+
+def run_flyvis(n_eyes=64, steps=200, seed=1):
+    """The flyvis optic lobe (lif.c's fv_step) for n_eyes eyes (two per fly) sharing one
+    flyvis-shaped model (N=45,669 nodes, ~1.5 M synapses, dt 20 ms), each with its own
+    luminance input: eye-steps per second and synaptic operations (edges x eyes) per second,
+    against the oracle port of fv_step on the host cores. Inputs are set once; each timed step is
+    the whole batch's fv_step."""
+    import torch
+    from oracle import oracle as O
+    from flybrain.flyvis import FlyVis, synth_flyvis
+    m = synth_flyvis(seed=seed)
+    rng = np.random.default_rng(seed)
+    fv = FlyVis(m, B=n_eyes)
+    for b in range(n_eyes):
+        fv.setInput(rng.uniform(0, 1, 721).astype(np.float32), b)
+    fv.step(10)  # warm-up
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        fv.step(steps)
+        ms = fv.last_ms()
+    secs = ms / 1e3
+    N, E = m["N"], m["E"]
+    # compulsory bytes per step: the transposed graph (source id + weight per edge) and
+    # bias/kdt/pointers once, each eye's v read and written and x read
+    byts = E * 8 + N * 12 + n_eyes * N * 12
+    peak, kind = peaks()
+    ach = byts * steps / secs / 1e9
+    # the host baseline: the oracle port of fv_step, eyes spread over the host threads
+    cpu_eyes, cpu_steps = min(16, n_eyes), 5
+    v = np.tile(m["bias"], (cpu_eyes, 1)).astype(np.float32)
+    x = np.zeros_like(v)
+    t0 = time.perf_counter()
+    O.fv_run(m, v, x, cpu_steps)
+    cpu_s = time.perf_counter() - t0
+    threads = int(O.lib("port").ob_threads())
+    return dict(eyes=n_eyes, nodes=N, synapses=E, steps=steps, ms_per_step=ms / steps,
+                eye_steps_per_s=n_eyes * steps / secs, synaptic_ops_per_s=E * n_eyes * steps / secs,
+                sim_s_per_wall_s=steps * m["dt"] / secs,
+                roofline=dict(bound="hbm", achieved=ach, peak=peak, unit="GB/s", frac=ach / peak, peak_kind=kind,
+                              traffic=None, note="the per-edge state gathers are served from L2 (the eyes' v is "
+                                                 f"{n_eyes * N * 4 / 1e6:.1f} MB); HBM carries the compulsory bytes"),
+                clocks=clk.summary(), gpu_launches=steps,
+                cpu_baseline=dict(value=cpu_eyes * cpu_steps / cpu_s, unit="eye-steps/s", cores=threads, kind="port",
+                                  sample=f"{cpu_eyes} eyes x {cpu_steps} steps, oracle port of fv_step"),
+                config=f"{n_eyes} eyes sharing a synthetic flyvis-shaped model (N={N}, E={E}, dt 20 ms), own "
+                       "luminance inputs; one launch per step, state [N][eyes] in HBM")
 
 
 def run_batched(g, args, n_trials=256, seed=7):

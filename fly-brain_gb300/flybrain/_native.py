@@ -139,6 +139,15 @@ SIGNATURES = {
     "fb_diff_batch_raster": (C.c_int, [P, I32, I32, P, P]),
     "fb_diff_batch_backward": (C.c_int, [P, P, P, P, I32, I32, C.POINTER(FbDiffGrads)]),
     "fb_diff_batch_edge_sum": (C.c_int, [P, I32, P, P]),
+    "fb_flyvis_create": (C.c_int, [I32, I64, P, P, P, P, P, I32, C.POINTER(P)]),
+    "fb_flyvis_destroy": (C.c_int, [P]),
+    "fb_flyvis_reset": (C.c_int, [P, I32]),
+    "fb_flyvis_set_input": (C.c_int, [P, I32, I32, P, P]),
+    "fb_flyvis_write": (C.c_int, [P, I32, I32, P]),
+    "fb_flyvis_read": (C.c_int, [P, I32, I32, P]),
+    "fb_flyvis_step": (C.c_int, [P, I32]),
+    "fb_flyvis_last_ms": (C.c_int, [P, C.POINTER(C.c_float)]),
+    "fb_flyvis_state": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int32)]),
 }
 
 

@@ -391,6 +391,33 @@ int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, const int32
  * backward, summed in list order (the instances must have the same edge count). */
 int fb_diff_batch_edge_sum(fb_diff_batch *b, int32_t n, const int32_t *insts, double *out);
 
+/* ---- flyvis optic lobe ----------------------------------------------------------------------
+ * The rate network of lif.c's fv_step (src/wasm/lif.c:82-93), as src/flyvis.js drives it (one
+ * FlyVis per eye, sharing the model: src/brainsetup.js:21-23): B instances sharing one model
+ * (graph by source: indptr[N+1], target[E], weight[E]; bias[N]; kdt[N] = dt / max(tau, dt) as
+ * f32), each with its own v and input x. fb_flyvis_step advances every instance nsteps times,
+ * each step lif.c's fv_step bit for bit (its per-target sum order kept, no atomics). */
+typedef struct fb_flyvis fb_flyvis;
+#define FB_FV_V 0 /* membrane / activity v */
+#define FB_FV_X 1 /* external input x */
+/* FlyVis constructor (src/flyvis.js:4-17): v starts at bias. Model arrays are host or device. */
+int fb_flyvis_create(int32_t N, int64_t E, const int32_t *indptr, const int32_t *target, const float *weight,
+                     const float *bias, const float *kdt, int32_t B, fb_flyvis **out);
+int fb_flyvis_destroy(fb_flyvis *f);
+/* FlyVis.reset (src/flyvis.js:24): v = bias, of instance b (b < 0: all). */
+int fb_flyvis_reset(fb_flyvis *f, int32_t b);
+/* FlyVis.setInput (src/flyvis.js:20-21) of instance b: x[idx[k]] = values[k] in list order. */
+int fb_flyvis_set_input(fb_flyvis *f, int32_t b, int32_t n, const int32_t *idx, const float *values);
+/* Whole-array access to instance b's v or x (N floats, host or device). */
+int fb_flyvis_write(fb_flyvis *f, int32_t field, int32_t b, const float *values);
+int fb_flyvis_read(fb_flyvis *f, int32_t field, int32_t b, float *out);
+/* FlyVis.step (src/flyvis.js:22), nsteps times for every instance. */
+int fb_flyvis_step(fb_flyvis *f, int32_t nsteps);
+int fb_flyvis_last_ms(fb_flyvis *f, float *ms);
+/* Device pointers of the current state, layout [N][B] (instance fastest); valid until the next
+ * step (v is double-buffered). */
+int fb_flyvis_state(fb_flyvis *f, float **v, float **x, int32_t *layout_b);
+
 /* ---- allocation-free step ----------------------------------------------------------------- */
 
 /* A caller-owned brain for fb_lif_step_noalloc: the fields of the reference's Brain header

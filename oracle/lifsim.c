@@ -239,3 +239,34 @@ int32_t ob_threads(void) {
   return 1;
 #endif
 }
+
+/* ---- flyvis optic lobe (src/wasm/lif.c:82-93) ------------------------------------------------
+ * The rate network lif.c's fv_step integrates: acc = sum over out-edges of the sources with
+ * v > 0 of weight * v (sources in ascending order, each row in CSR order), then
+ * v += kdt * (-v + bias + acc + x), every operation one f32 rounding in C order. */
+static void fv_step_port(int32_t N, const float *bias, const float *kdt, const int32_t *indptr, const int32_t *target,
+                         const float *weight, float *v, float *acc, const float *x) {
+  for (int32_t i = 0; i < N; i++) acc[i] = 0.f;
+  for (int32_t j = 0; j < N; j++) {
+    const float r = v[j];
+    if (r <= 0.f) continue;
+    for (int32_t k = indptr[j]; k < indptr[j + 1]; k++) acc[target[k]] += weight[k] * r;
+  }
+  for (int32_t i = 0; i < N; i++) v[i] += kdt[i] * (-v[i] + bias[i] + acc[i] + x[i]);
+}
+
+/* B instances (eyes) sharing the model, each v[b*N ..], x[b*N ..], `steps` steps; instances run
+ * in parallel over nthreads host threads (<= 0: the default). */
+void ob_fv_run(int32_t N, const float *bias, const float *kdt, const int32_t *indptr, const int32_t *target,
+               const float *weight, int32_t B, float *v, const float *x, int32_t steps, int32_t nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int32_t b = 0; b < B; b++) {
+    float *acc = (float *)malloc((size_t)(N > 0 ? N : 1) * sizeof(float));
+    for (int32_t s = 0; s < steps; s++)
+      fv_step_port(N, bias, kdt, indptr, target, weight, v + (int64_t)b * N, acc, x + (int64_t)b * N);
+    free(acc);
+  }
+}

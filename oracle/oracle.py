@@ -312,3 +312,26 @@ class OracleBrain:
     @property
     def nAwake(self):
         return self.N
+
+
+def fv_run(model: dict, v, x, steps: int, backend: str = "port", nthreads: int = 0, kdt=None):
+    """B flyvis instances (v, x: float32 [B][N]) advanced `steps` fv_steps in place by the oracle
+    restatement (backend "port") or the reference's own fv_step (backend "ref",
+    src/wasm/lif.c:86-93). kdt defaults to dt / max(tau, dt) rounded to f32 (src/flyvis.js:13)."""
+    L = lib(backend)
+    if not hasattr(L, "_fv_bound"):
+        L.ob_fv_run.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]
+        L._fv_bound = True
+    N = int(model["N"])
+    if kdt is None:
+        dt = float(model.get("dt") or 0.02)
+        kdt = (dt / np.maximum(np.asarray(model["tau"], np.float64), dt)).astype(np.float32)
+    arrs = [np.ascontiguousarray(model["bias"], np.float32), np.ascontiguousarray(kdt, np.float32),
+            np.ascontiguousarray(model["indptr"], np.int32), np.ascontiguousarray(model["target"], np.int32),
+            np.ascontiguousarray(model["weight"], np.float32)]
+    assert v.dtype == np.float32 and v.flags.c_contiguous and x.dtype == np.float32 and x.flags.c_contiguous
+    B = v.size // N
+    L.ob_fv_run(N, *[a.ctypes.data for a in arrs], B, v.ctypes.data, np.ascontiguousarray(x).ctypes.data,
+                int(steps), int(nthreads))
+    return v

@@ -99,3 +99,18 @@ int32_t ob_threads(void) {
   return 1;
 #endif
 }
+
+/* B flyvis instances sharing the model, run by the reference's own fv_step (lif.c:86-93). */
+void ob_fv_run(int32_t N, const float *bias, const float *kdt, const int32_t *indptr, const int32_t *target,
+               const float *weight, int32_t B, float *v, const float *x, int32_t steps, int32_t nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int32_t b = 0; b < B; b++) {
+    float *acc = (float *)malloc((size_t)(N > 0 ? N : 1) * sizeof(float));
+    for (int32_t s = 0; s < steps; s++)
+      fv_step(N, bias, kdt, indptr, target, weight, v + (int64_t)b * N, acc, x + (int64_t)b * N);
+    free(acc);
+  }
+}

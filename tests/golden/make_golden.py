@@ -155,8 +155,35 @@ def adjoint_fixture():
     print(f"real_subgraph_counts: N={n} E={len(ix)} -> {os.path.getsize(path)} bytes")
 
 
+def flyvis_fixture():
+    """A small flyvis-shaped model (630 nodes over 10 hex columns) and three eyes' inputs, run by
+    the reference's own fv_step (src/wasm/lif.c:86-93): v after 1, 10 and 100 steps."""
+    from flybrain.flyvis import synth_flyvis
+    m = synth_flyvis(N=630, seed=5, columns=10)
+    rng = np.random.default_rng(55)
+    B = 3
+    x = np.zeros((B, m["N"]), np.float32)
+    for b in range(B):
+        for ix in m["inputIdx"].values():
+            x[b, ix] = rng.uniform(0, 1, ix.shape[0]).astype(np.float32)
+    x[2, :40] = -0.5  # negative drive: nodes fall below zero and stop sending (lif.c:89)
+    v = np.tile(m["bias"], (B, 1)).astype(np.float32)
+    snaps, done = [], 0
+    for upto in (1, 10, 100):
+        O.fv_run(m, v, x, upto - done, backend="ref")
+        done = upto
+        snaps.append(v.copy())
+    os.makedirs(os.path.join(HERE, "flyvis"), exist_ok=True)
+    path = os.path.join(HERE, "flyvis", "flyvis_synth.npz")
+    np.savez_compressed(path, N=np.int32(m["N"]), E=np.int64(m["E"]), indptr=m["indptr"], target=m["target"],
+                        weight=m["weight"], bias=m["bias"], tau=m["tau"], dt=np.float64(m["dt"]), x=x,
+                        steps=np.array([1, 10, 100], np.int32), v=np.stack(snaps))
+    print(f"flyvis_synth: N={m['N']} E={m['E']} -> {os.path.getsize(path)} bytes")
+
+
 def main():
     O.build(ref=True)
+    flyvis_fixture()
     adjoint_fixture()
     for name, g, params, seed, script in cases():
         brain = O.OracleBrain(len(g["sign"]), g["indptr"], g["indices"], g["W"], g["sign"], params,
