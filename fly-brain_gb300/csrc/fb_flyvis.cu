@@ -63,19 +63,19 @@ __global__ void __launch_bounds__(kFvThreads) fv_step_kernel(int32_t N, int32_t 
     const int32_t lo = __ldg(cscPtr + i), hi = __ldg(cscPtr + i + 1);
     float acc = 0.f;
     int32_t e = lo;
-    // four in-edges per round: their loads are issued together, the sum stays in edge order
-    for (; e + 4 <= hi; e += 4) {
-      int32_t j[4];
-      float w[4], r[4];
+    // eight in-edges per round: their loads are issued together, the sum stays in edge order
+    for (; e + 8 <= hi; e += 8) {
+      int32_t j[8];
+      float w[8], r[8];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
+      for (int u = 0; u < 8; u++) {
         j[u] = __ldg(cscSrc + e + u);
         w[u] = __ldg(cscW + e + u);
       }
 #pragma unroll
-      for (int u = 0; u < 4; u++) r[u] = vin[(int64_t)j[u] * B + b];
+      for (int u = 0; u < 8; u++) r[u] = vin[(int64_t)j[u] * B + b];
 #pragma unroll
-      for (int u = 0; u < 4; u++)
+      for (int u = 0; u < 8; u++)
         if (!(r[u] <= 0.f)) acc = __fadd_rn(acc, __fmul_rn(w[u], r[u]));  // lif.c:90-91
     }
     for (; e < hi; e++) {

@@ -33,7 +33,7 @@ def test_golden_run_bit_for_bit():
             assert fv.v(b).tobytes() == z["v"][k][b].tobytes(), (int(upto), b)
 
 
-@pytest.mark.parametrize("B", [1, 2, 5, 33])
+@pytest.mark.parametrize("B", [1, 2, 5, 33, 64])
 def test_full_size_eyes_match_the_oracle(B):
     from oracle import oracle as O
     from flybrain.flyvis import FlyVis, synth_flyvis
