@@ -549,116 +549,153 @@ __device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, fl
   if (n > (uint32_t)kDBucket) D.ovfHead[i] = kNil;
 }
 
-// Integrate and spike (src/lifdiff.js:313-344), one thread per neuron, tiles of kDB neurons; with
-// `row` >= 0 it also records the replay arena (:439-456). In a forward pass the spikes above the
-// tape threshold are staged per tile. exact32 (forward): lif.c's expression with one f32 rounding
-// per C operation and the header's f32 scalars (:317-326). driveSoft: a driven neuron's spike is
-// sd + (1 - sd) s with sd = min(0.999, drive dt/1000) (:338).
+// A neuron's inputs to its update, loaded for two neurons per lane before either is written.
+struct UIn {
+  float ge, gi, v, refr, ad, res, sc, thr;
+  uint32_t n;
+  uint8_t forced;
+};
+__device__ __forceinline__ void load_in(const DiffDev &D, int i, UIn &u) {
+  u.ge = D.gE[i];
+  u.gi = D.gI[i];
+  u.n = D.cnt[i];
+  u.v = D.v[i];
+  u.refr = D.refr[i];
+  u.forced = D.isForced[i];
+  u.ad = D.adapt[i];
+  u.res = D.res[i];
+  u.sc = D.spikeCount[i];
+  u.thr = D.thrOffset[i];
+}
+
+// One neuron's integrate and spike (src/lifdiff.js:313-344); with `row` >= 0 the replay arena
+// (:439-456). Returns whether the spike goes on the tape (amplitude in *amp). exact32 (forward):
+// lif.c's expression with one f32 rounding per C operation and the header's f32 scalars
+// (:317-326). driveSoft: a driven neuron's spike is sd + (1 - sd) s, sd = min(0.999, drive
+// dt/1000) (:338).
+template <typename R>
+__device__ __forceinline__ bool upd_neuron(const DiffDev &D, const DP<R> &P, int i, int t, int row, bool ex,
+                                           const UIn &u, float &amp) {
+  float geF = u.ge, giF = u.gi;
+  if (u.n) {
+    d_apply<R>(D, P, i, u.n, geF, giF, ex);
+    D.cnt[i] = 0;
+  }
+  const R vReset = ex ? (R)P.xvReset : P.vReset, aInc = ex ? (R)P.xadaptInc : P.adaptInc;
+  const R ge = geF, gi = giF;
+  const int64_t off = row >= 0 ? (int64_t)row * D.N + i : 0;
+  R vi = u.v, s = 0;
+  int md = 0;
+  if (row >= 0) {
+    D.aV[off] = u.v;
+    D.aGE[off] = geF;
+    D.aGI[off] = giF;
+  }
+  float refr = u.refr;
+  const bool forced = u.forced != 0;
+  if (forced) D.isForced[i] = 0;
+  const bool wasRefr = refr > 0;
+  if (wasRefr) {
+    refr = ex ? refr - P.xdt : (float)((R)refr - P.dt);
+    vi = vReset;
+    if (forced) {
+      md = 2;
+      s = 1;
+    } else {
+      md = 1;
+    }
+  } else if (ex) {
+    const float vf = u.v;
+    float acc = P.xvRest - vf;
+    if (D.coba) {
+      acc = acc + (geF * (P.xeExc - vf)) * P.xcE;
+      acc = acc + (giF * (vf - P.xeInh)) * P.xcI;
+    } else {
+      acc = acc + geF;
+      acc = acc + giF;
+    }
+    const float lam = (D.biasMask && D.biasMask[i]) ? P.xlaminaBias : 0.f;
+    acc = D.biasArr ? (float)((double)acc + ((double)lam + (double)D.biasArr[i])) : acc + lam;
+    vi = vf + acc * P.xkM;
+  } else {
+    vi = d_u<R>(D, P, vi, ge, gi, d_bias<R>(D, P, i, nullptr));
+  }
+  geF = ex ? geF * P.xdE : (float)(ge * P.dE);
+  giF = ex ? giF * P.xdE : (float)(gi * P.dE);
+  float ad = ex ? u.ad * P.xdA : (float)((R)u.ad * P.dA);
+  const float rsF = u.res;
+  D.res[i] = ex ? rsF + (1.f - rsF) * P.xkRec : (float)((R)rsF + (R(1) - (R)rsF) * P.kRec);
+  if (row >= 0) D.aAd[off] = ad;
+  bool emit = false;
+  if (!wasRefr) {
+    const R thr = ex ? (R)((P.xvThresh + ad) + u.thr) : P.vThresh + (R)ad + d_kc<R>(D, P, i) + (R)u.thr;
+    s = D.soft ? R(1) / (R(1) + exp(-(vi - thr) / d_beta<R>(D, P, i))) : (vi >= thr ? R(1) : R(0));
+    if (D.driveSoft) {
+      const float dr = d_drive(D, i, t);
+      if (dr > 0.f) {
+        const R x = (R)dr * P.dtS, sd = x < (R)kDriveMax ? x : (R)kDriveMax;
+        s = sd + (R(1) - sd) * s;
+        md = 3;
+      }
+    }
+    if (s > 0) {
+      vi = s * vReset + (R(1) - s) * vi;
+      if (!D.soft) refr = ex ? P.xtRef : (float)P.tRef;
+      ad = (float)((R)ad + s * aInc);
+    }
+    D.spikeCount[i] = (float)((R)u.sc + s);
+    if (s > (D.soft ? R(1e-4) : R(0.5))) {
+      emit = true;
+      amp = (float)s;
+    }
+  }
+  if (row >= 0) {
+    D.aMode[off] = (uint8_t)md;
+    D.aSp[off] = (float)s;
+  }
+  D.gE[i] = geF;
+  D.gI[i] = giF;
+  D.adapt[i] = ad;
+  D.refr[i] = refr;
+  D.v[i] = (float)vi;
+  return emit;
+}
+
+// Integrate and spike for every neuron, warp tiles of kWT = 64 neurons (two per lane, both
+// loaded before either is written). In a forward pass the spikes above the tape threshold are
+// staged per warp tile in ascending order (ballots; no block barrier).
+constexpr int kWT = 64;
 template <typename R>
 __global__ void __launch_bounds__(kDB, 4) k_update(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
   __shared__ DiffDev D;
-  __shared__ uint32_t scan[33];
   load_dev(Ds, D);
   if (t >= D.steps) return;
-  const int tid = threadIdx.x;
   const bool ex = row < 0 && D.exact32;
-  const R vReset = ex ? (R)P.xvReset : P.vReset, aInc = ex ? (R)P.xadaptInc : P.adaptInc;
-  for (int tl = blockIdx.x; tl < D.nTiles; tl += gridDim.x) {
-    const int i = tl * kDB + tid;
-    bool emit = false;
-    float amp = 0.f;
-    if (i < D.N) {
-      float geF = D.gE[i], giF = D.gI[i];
-      const uint32_t n = D.cnt[i];
-      if (n) {
-        d_apply<R>(D, P, i, n, geF, giF, ex);
-        D.cnt[i] = 0;
-      }
-      const R ge = geF, gi = giF;
-      const int64_t off = row >= 0 ? (int64_t)row * D.N + i : 0;
-      R vi = D.v[i], s = 0;
-      int md = 0;
-      if (row >= 0) {
-        D.aV[off] = D.v[i];
-        D.aGE[off] = geF;
-        D.aGI[off] = giF;
-      }
-      float refr = D.refr[i];
-      const bool forced = D.isForced[i] != 0;
-      if (forced) D.isForced[i] = 0;
-      const bool wasRefr = refr > 0;
-      if (wasRefr) {
-        refr = ex ? refr - P.xdt : (float)((R)refr - P.dt);
-        vi = vReset;
-        if (forced) {
-          md = 2;
-          s = 1;
-        } else {
-          md = 1;
-        }
-      } else if (ex) {
-        const float vf = D.v[i];
-        float acc = P.xvRest - vf;
-        if (D.coba) {
-          acc = acc + (geF * (P.xeExc - vf)) * P.xcE;
-          acc = acc + (giF * (vf - P.xeInh)) * P.xcI;
-        } else {
-          acc = acc + geF;
-          acc = acc + giF;
-        }
-        const float lam = (D.biasMask && D.biasMask[i]) ? P.xlaminaBias : 0.f;
-        acc = D.biasArr ? (float)((double)acc + ((double)lam + (double)D.biasArr[i])) : acc + lam;
-        vi = vf + acc * P.xkM;
-      } else {
-        vi = d_u<R>(D, P, vi, ge, gi, d_bias<R>(D, P, i, nullptr));
-      }
-      geF = ex ? geF * P.xdE : (float)(ge * P.dE);
-      giF = ex ? giF * P.xdE : (float)(gi * P.dE);
-      float ad = ex ? D.adapt[i] * P.xdA : (float)((R)D.adapt[i] * P.dA);
-      const float rsF = D.res[i];
-      D.res[i] = ex ? rsF + (1.f - rsF) * P.xkRec : (float)((R)rsF + (R(1) - (R)rsF) * P.kRec);
-      if (row >= 0) D.aAd[off] = ad;
-      if (!wasRefr) {
-        const R thr = ex ? (R)((P.xvThresh + ad) + D.thrOffset[i])
-                         : P.vThresh + (R)ad + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
-        s = D.soft ? R(1) / (R(1) + exp(-(vi - thr) / d_beta<R>(D, P, i))) : (vi >= thr ? R(1) : R(0));
-        if (D.driveSoft) {
-          const float dr = d_drive(D, i, t);
-          if (dr > 0.f) {
-            const R x = (R)dr * P.dtS, sd = x < (R)kDriveMax ? x : (R)kDriveMax;
-            s = sd + (R(1) - sd) * s;
-            md = 3;
-          }
-        }
-        if (s > 0) {
-          vi = s * vReset + (R(1) - s) * vi;
-          if (!D.soft) refr = ex ? P.xtRef : (float)P.tRef;
-          ad = (float)((R)ad + s * aInc);
-        }
-        D.spikeCount[i] = (float)((R)D.spikeCount[i] + s);
-        if (s > (D.soft ? R(1e-4) : R(0.5))) {
-          emit = true;
-          amp = (float)s;
-        }
-      }
-      if (row >= 0) {
-        D.aMode[off] = (uint8_t)md;
-        D.aSp[off] = (float)s;
-      }
-      D.gE[i] = geF;
-      D.gI[i] = giF;
-      D.adapt[i] = ad;
-      D.refr[i] = refr;
-      D.v[i] = (float)vi;
-    }
+  const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+  const int nWT = (D.N + kWT - 1) / kWT;
+  const int wpb = blockDim.x >> 5;
+  for (int wt = blockIdx.x * wpb + (int)(threadIdx.x >> 5); wt < nWT; wt += gridDim.x * wpb) {
+    const int i0 = wt * kWT + (int)lane, i1 = i0 + 32;
+    UIn u0, u1;
+    if (i0 < D.N) load_in(D, i0, u0);
+    if (i1 < D.N) load_in(D, i1, u1);
+    float a0 = 0.f, a1 = 0.f;
+    const bool e0 = i0 < D.N && upd_neuron<R>(D, P, i0, t, row, ex, u0, a0);
+    const bool e1 = i1 < D.N && upd_neuron<R>(D, P, i1, t, row, ex, u1, a1);
     if (row >= 0) continue;  // replay: the tape already holds the spikes
-    uint32_t tot;
-    const uint32_t pos = block_exclusive_scan(emit ? 1u : 0u, &tot, scan);
-    if (emit) {
-      D.stage[(int64_t)tl * kDB + pos] = i;
-      D.stageAmp[(int64_t)tl * kDB + pos] = amp;
+    const uint32_t b0 = __ballot_sync(0xffffffffu, e0), b1 = __ballot_sync(0xffffffffu, e1);
+    const int64_t base = (int64_t)wt * kWT;
+    if (e0) {
+      const uint32_t p = __popc(b0 & lt);
+      D.stage[base + p] = i0;
+      D.stageAmp[base + p] = a0;
     }
-    if (tid == 0) D.tileCnt[tl] = (int32_t)tot;
+    if (e1) {
+      const uint32_t p = __popc(b0) + __popc(b1 & lt);
+      D.stage[base + p] = i1;
+      D.stageAmp[base + p] = a1;
+    }
+    if (lane == 0) D.tileCnt[wt] = (int32_t)(__popc(b0) + __popc(b1));
   }
 }
 
@@ -671,17 +708,18 @@ __global__ void k_emit(const DiffDev *Ds, int32_t t) {
   if (t >= D.steps) return;
   const int tid = threadIdx.x;
   int64_t carry = D.tOff[t] + D.tForced[t];
-  for (int t0 = 0; t0 < D.nTiles; t0 += blockDim.x) {
+  const int nWT = (D.N + kWT - 1) / kWT;
+  for (int t0 = 0; t0 < nWT; t0 += blockDim.x) {
     const int tl = t0 + tid;
-    const uint32_t c = tl < D.nTiles ? (uint32_t)D.tileCnt[tl] : 0u;
+    const uint32_t c = tl < nWT ? (uint32_t)D.tileCnt[tl] : 0u;
     uint32_t tot;
     const uint32_t pre = block_exclusive_scan(c, &tot, scan);
     if (c) {
       const int64_t o = carry + pre;
       for (uint32_t p = 0; p < c; p++) {
         if (o + p < D.tapeCap) {
-          D.tIdx[o + p] = D.stage[(int64_t)tl * kDB + p];
-          D.tAmp[o + p] = D.stageAmp[(int64_t)tl * kDB + p];
+          D.tIdx[o + p] = D.stage[(int64_t)tl * kWT + p];
+          D.tAmp[o + p] = D.stageAmp[(int64_t)tl * kWT + p];
         } else {
           atomicCAS(D.err, 0, FB_EOVERFLOW);
         }
@@ -721,11 +759,127 @@ __global__ void __launch_bounds__(kDB, 4) k_truncate(const DiffDev *Ds, int32_t 
   for (int64_t i = s0; i < (int64_t)D.nslots * N; i += ns) D.lsRing[i] = 0.f;
 }
 
-// Reverse of integrate-and-spike at step t (src/lifdiff.js:555-617), with the adjoint clip
-// (:623-629) fused: one thread per neuron. Scalar terms accumulate per neuron in double. The
-// gradient of a scheduled drive (:565-573, :587-604) accumulates per neuron into its column of the
-// step's epoch: a forced spike through ds/d(sd) = 1, a soft drive through ds/d(sd) = 1 - st, with
-// d(sd)/d(rate) = dt/1000 (the min's clamp is not differentiated, as in the reference).
+// A neuron's inputs to its reverse step, loaded for two neurons per lane before either is written.
+struct BIn {
+  float lad, lgE, lgI, lres, lv, ls, aV, aGE, aGI, aAd, aSp, thr;
+  double accA, accV, gBias;
+  int md;
+};
+__device__ __forceinline__ void load_bin(const DiffDev &D, const float *ls, int64_t off, int i, BIn &u) {
+  u.md = D.aMode[off];
+  u.lad = D.lad[i];
+  u.lgE = D.lgE[i];
+  u.lgI = D.lgI[i];
+  u.lres = D.lres[i];
+  u.lv = D.lv[i];
+  if (u.md != 1) {
+    u.ls = ls[i];
+    u.accA = D.accA[i];
+    if (u.md != 2) {
+      u.aV = D.aV[off];
+      u.aGE = D.aGE[off];
+      u.aGI = D.aGI[off];
+      u.aAd = D.aAd[off];
+      u.aSp = D.aSp[off];
+      u.thr = D.thrOffset[i];
+      u.accV = D.accV[i];
+      u.gBias = D.gBias[i];
+    }
+  }
+}
+
+// Reverse of integrate-and-spike for neuron i at step t (src/lifdiff.js:555-617), with the adjoint
+// clip (:623-629) fused. Scalar terms accumulate per neuron in double. The gradient of a scheduled
+// drive (:565-573, :587-604) accumulates per neuron into its column of the step's epoch: a forced
+// spike through ds/d(sd) = 1, a soft drive through ds/d(sd) = 1 - st, with d(sd)/d(rate) = dt/1000
+// (the min's clamp is not differentiated, as in the reference).
+template <typename R>
+__device__ __forceinline__ void bneuron(const DiffDev &D, const DP<R> &P, int i, int t, int32_t scored, float *ls,
+                                        float *gDrv, const BIn &u) {
+  const int md = u.md;
+  const R lpA = u.lad;
+  const R lE = (R)u.lgE * P.dE, lI = (R)u.lgI * P.dE, lA = lpA * P.dA;
+  const R lR = (R)u.lres * (R(1) - P.kRec);
+  float lvF = u.lv, lgEF = (float)lE, lgIF = (float)lI, ladF = (float)lA, lresF = (float)lR;
+  if (md == 1) {
+    lvF = 0.f;
+  } else {
+    R dl = 0;
+    if (scored && D.dL) {
+      if (D.roMap) {
+        const int c = D.roMap[i];
+        if (c >= 0) dl = D.dL[(int64_t)t * D.nro + c];
+      } else {
+        dl = D.dL[i];
+      }
+    }
+    const int slot = gDrv ? D.dSlot[i] : -1;
+    if (md == 2) {
+      D.accA[i] = u.accA + (double)lA;
+      if (slot >= 0) gDrv[slot] = (float)((R)gDrv[slot] + (lA * P.adaptInc + ((R)u.ls + dl)) * P.dtS);
+      lvF = 0.f;
+      ls[i] = 0.f;
+    } else {
+      const R vv = u.aV, gEv = u.aGE, gIv = u.aGI;
+      R lam;
+      const R bias = d_bias<R>(D, P, i, &lam);
+      const R uu = d_u<R>(D, P, vv, gEv, gIv, bias);
+      const R thr = P.vThresh + (R)u.aAd + d_kc<R>(D, P, i) + (R)u.thr;
+      const R d = uu - thr;
+      const R s = u.aSp;
+      // a soft drive's composite spike split back into sd and the threshold's st
+      R sd = 0, st = s;
+      if (md == 3) {
+        const R x = (R)d_drive(D, i, t) * P.dtS;
+        sd = x < (R)kDriveMax ? x : (R)kDriveMax;
+        st = (s - sd) / (R(1) - sd);
+      }
+      const R beta = d_beta<R>(D, P, i);
+      R sg;
+      if (D.soft) sg = st * (R(1) - st) / beta;
+      else {
+        const R tt = R(1) + fabs(d) / beta;
+        sg = R(1) / (beta * tt * tt);
+      }
+      const R lspike = (R)u.ls + dl;
+      const R lvNew = lvF;
+      const R lsTot = (P.vReset - uu) * lvNew + lpA * P.adaptInc + lspike;
+      const R lt = lsTot * (R(1) - sd) * sg;
+      const R lu = lvNew * (R(1) - s) + lt;
+      const R lthr = -lt;
+      if (slot >= 0) gDrv[slot] = (float)((R)gDrv[slot] + lsTot * (R(1) - st) * P.dtS);
+      D.accA[i] = u.accA + (double)(lpA * s);
+      D.accV[i] = u.accV + (double)lthr;
+      if (D.thrMask && D.thrMask[i]) D.accKc[i] += (double)lthr;
+      ladF = (float)(lA + lthr * P.dA);
+      if (D.coba) {
+        lvF = (float)(lu * (R(1) + P.kM * (R(-1) - gEv * P.cE + gIv * P.cI)));
+        lgEF = (float)(lE + lu * P.kM * (P.eExc - vv) * P.cE);
+        lgIF = (float)(lI + lu * P.kM * (vv - P.eInh) * P.cI);
+        D.accEI[i] += (double)(lu * P.kM * gIv * P.cI * (R(-1) + (vv - P.eInh) * P.cI));
+      } else {
+        lvF = (float)(lu * (R(1) - P.kM));
+        lgEF = (float)(lE + lu * P.kM);
+        lgIF = (float)(lI + lu * P.kM);
+      }
+      if (lam != 0) D.accLa[i] += (double)(lu * P.kM);
+      D.gBias[i] = u.gBias + (double)(lu * P.kM);
+      ls[i] = 0.f;
+    }
+  }
+  const R c = P.adjClip;
+  if (c > 0) {
+    auto cl = [c](float x) { return (float)((R)x > c ? c : ((R)x < -c ? -c : (R)x)); };
+    lvF = cl(lvF); lgEF = cl(lgEF); lgIF = cl(lgIF); ladF = cl(ladF); lresF = cl(lresF);
+  }
+  D.lv[i] = lvF;
+  D.lgE[i] = lgEF;
+  D.lgI[i] = lgIF;
+  D.lad[i] = ladF;
+  D.lres[i] = lresF;
+}
+
+// The reverse neuron pass of step t over warp tiles of kWT neurons (two per lane).
 template <typename R>
 __global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row, int32_t scored) {
   __shared__ DiffDev D;
@@ -733,89 +887,17 @@ __global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, 
   if (t >= D.steps) return;
   float *ls = D.lsRing + (int64_t)(t % D.nslots) * D.N;
   float *gDrv = D.gDrive ? D.gDrive + (int64_t)(t / D.driveEpoch) * D.nDS : nullptr;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += gridDim.x * blockDim.x) {
-    const int64_t off = (int64_t)row * D.N + i;
-    const int md = D.aMode[off];
-    const R lpA = D.lad[i];
-    const R lE = (R)D.lgE[i] * P.dE, lI = (R)D.lgI[i] * P.dE, lA = lpA * P.dA;
-    const R lR = (R)D.lres[i] * (R(1) - P.kRec);
-    float lvF = D.lv[i], lgEF = (float)lE, lgIF = (float)lI, ladF = (float)lA, lresF = (float)lR;
-    if (md == 1) {
-      lvF = 0.f;
-    } else {
-      R dl = 0;
-      if (scored && D.dL) {
-        if (D.roMap) {
-          const int c = D.roMap[i];
-          if (c >= 0) dl = D.dL[(int64_t)t * D.nro + c];
-        } else {
-          dl = D.dL[i];
-        }
-      }
-      const int slot = gDrv ? D.dSlot[i] : -1;
-      if (md == 2) {
-        D.accA[i] += (double)lA;
-        if (slot >= 0) gDrv[slot] = (float)((R)gDrv[slot] + (lA * P.adaptInc + ((R)ls[i] + dl)) * P.dtS);
-        lvF = 0.f;
-        ls[i] = 0.f;
-      } else {
-        const R vv = D.aV[off], gEv = D.aGE[off], gIv = D.aGI[off];
-        R lam;
-        const R bias = d_bias<R>(D, P, i, &lam);
-        const R u = d_u<R>(D, P, vv, gEv, gIv, bias);
-        const R thr = P.vThresh + (R)D.aAd[off] + d_kc<R>(D, P, i) + (R)D.thrOffset[i];
-        const R d = u - thr;
-        const R s = D.aSp[off];
-        // a soft drive's composite spike split back into sd and the threshold's st
-        R sd = 0, st = s;
-        if (md == 3) {
-          const R x = (R)d_drive(D, i, t) * P.dtS;
-          sd = x < (R)kDriveMax ? x : (R)kDriveMax;
-          st = (s - sd) / (R(1) - sd);
-        }
-        const R beta = d_beta<R>(D, P, i);
-        R sg;
-        if (D.soft) sg = st * (R(1) - st) / beta;
-        else {
-          const R tt = R(1) + fabs(d) / beta;
-          sg = R(1) / (beta * tt * tt);
-        }
-        const R lspike = (R)ls[i] + dl;
-        const R lvNew = lvF;
-        const R lsTot = (P.vReset - u) * lvNew + lpA * P.adaptInc + lspike;
-        const R lt = lsTot * (R(1) - sd) * sg;
-        const R lu = lvNew * (R(1) - s) + lt;
-        const R lthr = -lt;
-        if (slot >= 0) gDrv[slot] = (float)((R)gDrv[slot] + lsTot * (R(1) - st) * P.dtS);
-        D.accA[i] += (double)(lpA * s);
-        D.accV[i] += (double)lthr;
-        if (D.thrMask && D.thrMask[i]) D.accKc[i] += (double)lthr;
-        ladF = (float)(lA + lthr * P.dA);
-        if (D.coba) {
-          lvF = (float)(lu * (R(1) + P.kM * (R(-1) - gEv * P.cE + gIv * P.cI)));
-          lgEF = (float)(lE + lu * P.kM * (P.eExc - vv) * P.cE);
-          lgIF = (float)(lI + lu * P.kM * (vv - P.eInh) * P.cI);
-          D.accEI[i] += (double)(lu * P.kM * gIv * P.cI * (R(-1) + (vv - P.eInh) * P.cI));
-        } else {
-          lvF = (float)(lu * (R(1) - P.kM));
-          lgEF = (float)(lE + lu * P.kM);
-          lgIF = (float)(lI + lu * P.kM);
-        }
-        if (lam != 0) D.accLa[i] += (double)(lu * P.kM);
-        D.gBias[i] += (double)(lu * P.kM);
-        ls[i] = 0.f;
-      }
-    }
-    const R c = P.adjClip;
-    if (c > 0) {
-      auto cl = [c](float x) { return (float)((R)x > c ? c : ((R)x < -c ? -c : (R)x)); };
-      lvF = cl(lvF); lgEF = cl(lgEF); lgIF = cl(lgIF); ladF = cl(ladF); lresF = cl(lresF);
-    }
-    D.lv[i] = lvF;
-    D.lgE[i] = lgEF;
-    D.lgI[i] = lgIF;
-    D.lad[i] = ladF;
-    D.lres[i] = lresF;
+  const int lane = threadIdx.x & 31;
+  const int nWT = (D.N + kWT - 1) / kWT;
+  const int wpb = blockDim.x >> 5;
+  const int64_t rowOff = (int64_t)row * D.N;
+  for (int wt = blockIdx.x * wpb + (threadIdx.x >> 5); wt < nWT; wt += gridDim.x * wpb) {
+    const int i0 = wt * kWT + lane, i1 = i0 + 32;
+    BIn u0, u1;
+    if (i0 < D.N) load_bin(D, ls, rowOff + i0, i0, u0);
+    if (i1 < D.N) load_bin(D, ls, rowOff + i1, i1, u1);
+    if (i0 < D.N) bneuron<R>(D, P, i0, t, scored, ls, gDrv, u0);
+    if (i1 < D.N) bneuron<R>(D, P, i1, t, scored, ls, gDrv, u1);
   }
 }
 
@@ -1012,6 +1094,7 @@ struct Inst {
   int32_t recordedSteps = 0;
   float *dLbuf = nullptr;
   int32_t *roMap = nullptr;
+  std::vector<int32_t> roList;  // the readout set roMap holds
   // host copies for the drive schedule's set edits and the exact32 check
   std::vector<int32_t> driven0, driveIdx;
   bool thrMaskAny = false;
@@ -1254,7 +1337,8 @@ int create_instance(fb_diff_batch *b, Inst &I, const fb_diff_net *net, int64_t t
   c.add(&D.refr, N); c.add(&D.spikeCount, N); c.add(&D.isForced, N); c.add(&D.rng, 1);
   c.add(&D.cnt, N); c.add(&D.bucket, N * kDBucket); c.add(&D.ovfHead, N); c.add(&D.ovfTop, 1);
   c.add(&D.ovf, D.ovfCap); c.add(&D.effK, N);
-  c.add(&D.stage, (size_t)D.nTiles * kDB); c.add(&D.stageAmp, (size_t)D.nTiles * kDB); c.add(&D.tileCnt, D.nTiles);
+  c.add(&D.stage, (size_t)D.nTiles * kDB); c.add(&D.stageAmp, (size_t)D.nTiles * kDB);
+  c.add(&D.tileCnt, (size_t)D.nTiles * (kDB / kWT));  // warp tiles of kWT neurons
   c.add(&D.lv, N); c.add(&D.lgE, N); c.add(&D.lgI, N); c.add(&D.lad, N); c.add(&D.lres, N);
   c.add(&D.accA, N); c.add(&D.accV, N); c.add(&D.accKc, N); c.add(&D.accLa, N); c.add(&D.accEI, N);
   c.add(&D.accW, N); c.add(&D.accD, N); c.add(&D.gLog, N); c.add(&D.gBias, N); c.add(&D.gEdge, E);
@@ -1426,13 +1510,19 @@ int set_readout(fb_diff_batch *b, Inst &I, int32_t nro, const int32_t *ro) {
     int rc = talloc(b, &I.roMap, D.N);
     if (rc) return rc;
   }
-  std::vector<int32_t> map(D.N, -1), h(std::max(nro, 1));
+  std::vector<int32_t> h(nro);
   if (nro) DCU(cudaMemcpy(h.data(), ro, (size_t)nro * 4, cudaMemcpyDefault));
+  if (D.roMap == I.roMap && h == I.roList) {  // the map already on the device
+    D.nro = nro;
+    return FB_OK;
+  }
+  std::vector<int32_t> map(D.N, -1);
   for (int32_t c = 0; c < nro; c++) {
     if (h[c] < 0 || h[c] >= D.N) return dfail(FB_EINVAL, "readout[%d]=%d out of range", c, h[c]);
     map[h[c]] = c;
   }
   DCU(cudaMemcpy(I.roMap, map.data(), (size_t)D.N * 4, cudaMemcpyHostToDevice));
+  I.roList = std::move(h);
   D.roMap = I.roMap;
   D.nro = nro;
   return FB_OK;
