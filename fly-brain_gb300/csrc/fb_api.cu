@@ -821,9 +821,9 @@ static bool lag_applies(fb_brains *br, int32_t steps, const char **why) {
   else if (T.mode != FB_DELIVER_EXACT || (T.flags & kHasPreInh)) *why = "a delivery mode other than exact without presynaptic inhibition";
   else if (br->profiling && br->schedule != FB_SCHEDULE_LAGGED) *why = "phase profiling";
   else if (br->logging && steps > kLagRing) *why = "per-step logging of a launch longer than 64 steps";
-  // a block's wait at step s (for step s - L, L = D - kHelp) must not need its own completion of
+  // a block's wait at step s (for step s - L, L = D - help) must not need its own completion of
   // that step, which it publishes at step s - L + 1: L >= 2
-  else if (T.nslots - 1 < kHelp + 2 || T.nslots - 1 > 32) *why = "a ring depth outside 5..33 slots";
+  else if (T.nslots - 1 < 4 || T.nslots - 1 > 32) *why = "a ring depth outside 5..33 slots";
   else if (T.bgEvents > (float)(1 << 20)) *why = "more than 2^20 background events per step";
   return *why == nullptr;
 }
@@ -938,7 +938,9 @@ static int run_lagged(fb_brains *br, int32_t steps) {
   a.T = steps;
   a.D = R.D;
   a.S = R.S;
-  a.L = R.D - kHelp;
+  a.help = lag_help(R.D);
+  a.dbPub = a.help - 1;
+  a.L = R.D - a.help;
   a.nTB = R.nTB;
   a.cap = R.cap;
   a.nD = R.nD;

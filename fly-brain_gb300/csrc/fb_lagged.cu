@@ -5,13 +5,13 @@
 // contributions are known at emission, so they are pushed then into per-arrival-step buckets;
 // a block updating step t only needs every block to have finished step t - D (plus the helper
 // delay below), not step t - 1. Blocks therefore advance on their own and synchronise through
-// per-step completion counters with up to L = D - kHelp steps of slack.
+// per-step completion counters with up to L = D - help steps of slack.
 //
 //  - Tile blocks (all but block 0) own fixed sets of non-driven neurons (contiguous ascending id
 //    ranges), their state held in shared memory for the whole launch.
 //  - The driven block (block 0) owns every Poisson-driven neuron and the generator: the
 //    background draws and one draw per non-refractory driven neuron in list order (lif.c:46-52),
-//    then those neurons' updates. Its spikes are pushed by the tile blocks kHelp steps later.
+//    then those neurons' updates. Its spikes are pushed by the tile blocks `help` steps later.
 //  - The summation order of lif.c is kept per target: each contribution carries its arrival's
 //    rank in the fired list (forced spikes first in list order, then threshold spikes by
 //    ascending id, lif.c:51-52, 73-76), and the target adds them in rank order.
@@ -173,18 +173,19 @@ __device__ __forceinline__ float predict_amp(const LagArgs &a, float sign, float
 }
 
 // One warp pushes the contributions W[j]*amp (lif.c:41-42) of edges [lo, hi) of one presynaptic
-// neuron into the buckets of arrival slot `slot`, keyed by (rank << 1) | inhibitory. Each edge's
-// record holds its target's count slot, its first bucket entry and their end. Up to kPushChunks
-// edges per lane are in flight at once: their loads, then their slot claims, then their stores.
+// neuron into the buckets of arrival slot `slot`, keyed by (rank << 1) | inhibitory; of the row's
+// 32-edge chunks it takes c0, c0 + cs, ... (several warps can share a row). Each edge's record
+// holds its target's count slot, its first bucket entry and their end. Up to kPushChunks edges per
+// lane are in flight at once: their loads, then their slot claims, then their stores.
 constexpr int kPushChunks = 1;
 __device__ __forceinline__ void push_edges(const LagArgs &a, uint32_t lo, uint32_t hi, uint32_t rank, float amp,
-                                           int slot) {
+                                           int slot, uint32_t c0 = 0, uint32_t cs = 1) {
   if (amp == 0.f) return;  // lif.c:37: nothing delivered, no depression
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t key = (rank << 1) | (amp > 0 ? 0u : 1u);
   uint32_t *cnt = a.cnt + (int64_t)slot * a.cntStride;
   uint2 *buf = a.buf + (int64_t)slot * a.E;
-  for (uint32_t j0 = lo; j0 < hi; j0 += 32 * kPushChunks) {
+  for (uint32_t j0 = lo + 32u * kPushChunks * c0; j0 < hi; j0 += 32u * kPushChunks * cs) {
     uint4 er[kPushChunks];
     float w[kPushChunks];
     uint32_t pos[kPushChunks];
@@ -585,17 +586,27 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   uint64_t tp = a.prof != nullptr ? global_ns() : 0;
   const int pb = drivenBlock ? 0 : 5;  // phase slots of this block
   int sEnd = a.T;                      // the steps run (fewer after a failed wait)
+  const int publisher = (int)blockDim.x - (drivenBlock ? 32 : 64);
   for (int s = 0; s < a.T; s++) {
     const int slot = s % a.S;
     const int ring = s & (kLagRing - 1);
     // lag: every block has finished step s - L (and, for the background, the driven block has
     // published this step's draws)
     if (tid == 0) {
+      // every block has finished step s + ahead - L, so the counts prefetched two steps ahead
+      // are final (ahead = 2 unless the lag is too short; a block's own completion of step s - 1
+      // is published only after this wait, so need <= s - 2). One look further ahead first: its
+      // round trip, when it succeeds, covers the next few steps as well.
       bool ok = true;
-      const int need = s - a.L;
+      const int need = s + min(2, a.L - 2) - a.L;
       if (need >= 0 && sh.known < need) {
-        ok = wait_geq(a, a.done + (need & (kLagRing - 1)), done_target(need, gridDim.x));
-        if (ok) sh.known = need;
+        const int far = min(need + 4, s - 2);
+        if (far > need && ld_acquire(a.done + (far & (kLagRing - 1))) >= done_target(far, gridDim.x)) {
+          sh.known = far;
+        } else {
+          ok = wait_geq(a, a.done + (need & (kLagRing - 1)), done_target(need, gridDim.x));
+          if (ok) sh.known = need;
+        }
       }
       if (ok && !drivenBlock && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s + 1));
       sh.stopP[s & 1] = ok ? 0 : 1;
@@ -607,15 +618,19 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     }
     // step s - 1 is complete in this block (the barrier above): its completion is published now,
     // so the release's wait for the block's writes overlaps this step's work. The publishing
-    // thread is in the second-last warp, which has the fewest neurons (thread 0 checks the lag).
-    if ((int)tid == (int)blockDim.x - 64 && s > 0) {
+    // thread is in a warp with few neurons (thread 0 checks the lag): the second-last warp of a
+    // tile block, the last warp of the driven block (one list entry per lane, then the generator)
+    if ((int)tid == publisher && s > 0) {
       const int sp = s - 1;
       if (drivenBlock) {
         const uint32_t n = sh.dbCnt2[sp & 1];
         sh.dbCnt2[sp & 1] = 0;
         a.dbCnt[sp & (kLagRing - 1)] = (int32_t)n;
         if (a.log) atomicAdd(a.stepTot + sp, (int32_t)n);
-        st_release(a.dbDone, (uint32_t)s);  // the spike list and count of step s - 1
+        // the spike lists and counts of the steps before s, released every other step: the
+        // release holds up its warp about as long as the rest of a step, and the tile blocks push
+        // these spikes `help` steps later
+        if (s % a.dbPub == 0) st_release(a.dbDone, (uint32_t)s);
         atomicAdd(a.done + (sp & (kLagRing - 1)), 1u);  // the driven block pushes nothing itself
       } else {
         red_release(a.done + (sp & (kLagRing - 1)), 1u);
@@ -780,19 +795,25 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       fired = before;
     }
     lap(a, 6, tp);
-    // own spikes: one warp each, into the slot of step s + D
+    // own spikes into the slot of step s + D: their 32-edge chunks dealt round-robin over the
+    // block's warps, so a large row is spread over the block
+    const uint32_t warp = tid >> 5, nwarps = blockDim.x >> 5;
     if (fired) {
       __syncthreads();
       const int32_t *st = a.tStage + ((int64_t)ring * a.nTB + b) * a.cap;
-      for (uint32_t w = tid >> 5; w < fired; w += blockDim.x >> 5) {
-        const int k = ldcg(st + w);
-        push_edges(a, S.row0[k], S.row1[k], (uint32_t)(a.nD + S.id[k]), S.amp[k], (s + a.D) % a.S);
+      uint32_t base = 0;
+      for (uint32_t f = 0; f < fired; f++) {
+        const int k = ldcg(st + f);
+        const uint32_t lo = S.row0[k], hi = S.row1[k];
+        push_edges(a, lo, hi, (uint32_t)(a.nD + S.id[k]), S.amp[k], (s + a.D) % a.S,
+                   (warp + nwarps - base % nwarps) % nwarps, nwarps);
+        base += (hi - lo + 31) / 32;
       }
     }
     lap(a, 7, tp);
-    // the driven block's spikes of step s - kHelp, shared out over the tile blocks
-    if (s >= kHelp) {
-      const int sp = s - kHelp, rp = sp & (kLagRing - 1);
+    // the driven block's spikes of step s - help, shared out over the tile blocks
+    if (s >= a.help) {
+      const int sp = s - a.help, rp = sp & (kLagRing - 1);
       if (tid == 0) {
         bool ok = true;
         if (dbKnown < (uint32_t)(sp + 1)) ok = wait_geq(a, a.dbDone, (uint32_t)(sp + 1), &dbKnown);
@@ -803,11 +824,18 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         sEnd = s;
         break;
       }
+      // spike e goes to tile block (e + 61 sp) mod nTB: the assignment rotates from step to
+      // step, so no block carries a push every step; its chunks are dealt over the block's warps
       const int nsp = ldcg(a.dbCnt + rp);
-      for (int e = b + a.nTB * (tid >> 5); e < nsp; e += a.nTB * (blockDim.x >> 5)) {
+      int e0 = b - (int)(((int64_t)sp * 61) % a.nTB);
+      if (e0 < 0) e0 += a.nTB;
+      uint32_t base = 0;
+      for (int e = e0; e < nsp; e += a.nTB) {
         const uint4 x = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2);
         const uint4 row = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2 + 1);
-        push_edges(a, row.x, row.y, x.y, __uint_as_float(x.z), (sp + a.D) % a.S);
+        push_edges(a, row.x, row.y, x.y, __uint_as_float(x.z), (sp + a.D) % a.S,
+                   (warp + nwarps - base % nwarps) % nwarps, nwarps);
+        base += (row.y - row.x + 31) / 32;
       }
     }
     if (tid == 0) {
@@ -820,7 +848,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
 
   // ---------------- epilogue ----------------
   __syncthreads();
-  if (drivenBlock && (int)tid == (int)blockDim.x - 64 && a.T > 0 && sEnd == a.T) {  // the last step's count
+  if (drivenBlock && (int)tid == publisher && a.T > 0 && sEnd == a.T) {  // the last step's count
     const int sp = a.T - 1;
     a.dbCnt[sp & (kLagRing - 1)] = (int32_t)sh.dbCnt2[sp & 1];
     if (a.log) atomicAdd(a.stepTot + sp, (int32_t)sh.dbCnt2[sp & 1]);

@@ -9,7 +9,13 @@ namespace fb {
 constexpr int kLagRing = 64;  // ring depth of the per-step counters and lists (a power of two)
 constexpr int kLagThreads = 1024;  // threads per block
 constexpr int kLagPer = 2;        // neurons per thread at most (tile and driven blocks)
-constexpr int kHelp = 2;      // steps after which the tile blocks push the driven block's spikes
+// The tile blocks push the driven block's spikes `help` steps late. With a delay of at least
+// kLagPairDelay steps the driven block releases its spike lists every other step (the release
+// holds up its warp about as long as the rest of a step) and help = 3; otherwise every step and
+// help = 2. The lag bound is L = D - help >= 2 (a block's own completion of step s - 1 is
+// published at step s, after its wait).
+constexpr int kLagPairDelay = 6;
+inline int lag_help(int D) { return D >= kLagPairDelay ? 3 : 2; }
 
 struct LagArgs {
   Trial *G;  // the brain's device header: scalars are written back at the end
@@ -18,7 +24,9 @@ struct LagArgs {
   int32_t T;      // steps of this launch
   int32_t D;      // arrival delay in steps (nslots - 1)
   int32_t S;      // arrival slots of the contribution buffer (2 D)
-  int32_t L;      // lag bound D - kHelp
+  int32_t L;      // lag bound D - help
+  int32_t help;   // steps after which the tile blocks push the driven block's spikes
+  int32_t dbPub;  // steps per release of the driven block's spike lists (help - 1)
   int32_t nTB;    // tile blocks (grid - 1)
   int32_t cap;    // neurons per tile block (capacity)
   int32_t nD;     // driven-list length
