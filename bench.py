@@ -255,7 +255,8 @@ def run_ours(args, rank, world):
         brain = None
     if os.environ.get("FB_BENCH_ADJOINT_BATCH", "1") == "1":
         plain_per_trial_s = dev_s / sim_s
-        ab = run_adjoint_batched(g, idx, hz, n_trials=int(os.environ.get("FB_ADJ_TRIALS", "64")))
+        ab = run_adjoint_batched(g, idx, hz, n_trials=int(os.environ.get("FB_ADJ_TRIALS", "64")),
+                                 steps=int(os.environ.get("FB_ADJ_STEPS", "5000")))
         ab["plain_single_trial_forward_per_trial_s"] = plain_per_trial_s
         ab["cost_vs_plain_single_trial_forward"] = ab["fwd_bwd_per_trial_s"] / plain_per_trial_s
         res["adjoint_batched"] = ab
