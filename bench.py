@@ -38,7 +38,7 @@ L2_FLUSH_BYTES = 512 << 20
 # capture of a 100-step launch of each kernel (profiles/); traffic grows in proportion to steps.
 DRAM_BYTES_PER_STEP_SINGLE = {
     "grid": 16.826112e6 / 100,    # fb::step_kernel
-    "lagged": 53.68704e6 / 100,   # fb::lagged_kernel
+    "lagged": (53.468928e6 + 0.851456e6) / 100,   # fb::lagged_kernel
 }
 KERNEL_NAME = {
     "grid": "fb::step_kernel (persistent, two grid barriers per step)",
