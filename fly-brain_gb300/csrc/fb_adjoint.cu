@@ -761,9 +761,9 @@ __global__ void __launch_bounds__(kDB, 4) k_truncate(const DiffDev *Ds, int32_t 
 
 // A neuron's inputs to its reverse step, loaded for two neurons per lane before either is written.
 struct BIn {
-  float lad, lgE, lgI, lres, lv, ls, aV, aGE, aGI, aAd, aSp, thr;
+  float lad, lgE, lgI, lres, lv, ls, aV, aGE, aGI, aAd, aSp, thr, dl;
   double accA, accV, gBias;
-  int md;
+  int md, ro;
 };
 __device__ __forceinline__ void load_bin(const DiffDev &D, const float *ls, int64_t off, int i, BIn &u) {
   u.md = D.aMode[off];
@@ -786,6 +786,18 @@ __device__ __forceinline__ void load_bin(const DiffDev &D, const float *ls, int6
       u.gBias = D.gBias[i];
     }
   }
+  u.ro = (u.md != 1 && D.dL && D.roMap) ? D.roMap[i] : -1;  // the loss gradient's column, if read out
+}
+
+// The step's loss gradient for a neuron (second load phase: it depends on the readout column).
+__device__ __forceinline__ void load_dl(const DiffDev &D, int i, int t, int32_t scored, BIn &u) {
+  u.dl = 0.f;
+  if (!scored || !D.dL || u.md == 1) return;
+  if (D.roMap) {
+    if (u.ro >= 0) u.dl = D.dL[(int64_t)t * D.nro + u.ro];
+  } else {
+    u.dl = D.dL[i];
+  }
 }
 
 // Reverse of integrate-and-spike for neuron i at step t (src/lifdiff.js:555-617), with the adjoint
@@ -804,15 +816,7 @@ __device__ __forceinline__ void bneuron(const DiffDev &D, const DP<R> &P, int i,
   if (md == 1) {
     lvF = 0.f;
   } else {
-    R dl = 0;
-    if (scored && D.dL) {
-      if (D.roMap) {
-        const int c = D.roMap[i];
-        if (c >= 0) dl = D.dL[(int64_t)t * D.nro + c];
-      } else {
-        dl = D.dL[i];
-      }
-    }
+    const R dl = u.dl;
     const int slot = gDrv ? D.dSlot[i] : -1;
     if (md == 2) {
       D.accA[i] = u.accA + (double)lA;
@@ -896,6 +900,8 @@ __global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, 
     BIn u0, u1;
     if (i0 < D.N) load_bin(D, ls, rowOff + i0, i0, u0);
     if (i1 < D.N) load_bin(D, ls, rowOff + i1, i1, u1);
+    if (i0 < D.N) load_dl(D, i0, t, scored, u0);
+    if (i1 < D.N) load_dl(D, i1, t, scored, u1);
     if (i0 < D.N) bneuron<R>(D, P, i0, t, scored, ls, gDrv, u0);
     if (i1 < D.N) bneuron<R>(D, P, i1, t, scored, ls, gDrv, u1);
   }
