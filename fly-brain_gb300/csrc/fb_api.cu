@@ -64,6 +64,11 @@ static int fail(int code, const char *fmt, ...) {
     }                                                                                  \
   } while (0)
 
+// Constant-state flags of a brain whose state was just reset (adapt 0, res 1).
+static int32_t rest_flags(const Trial &T) {
+  return (T.adaptInc == 0.f ? kAdaptZero : 0) | (T.depU == 0.f ? kResRest : 0);
+}
+
 extern "C" const char *fb_last_error(void) { return g_err.c_str(); }
 extern "C" int fb_version(void) { return 100; }
 
@@ -464,7 +469,8 @@ static void fill_constants(Trial &T, const fb_params &p, int32_t N) {
   T.bgEvents = (float)((double)N * p.bgRate * p.dt / 1000);
   T.bgAmp = (float)p.bgAmp;
   T.preInh = (float)p.preInh;
-  T.flags = (T.bgEvents > 0 ? kHasBg : 0) | (T.depU != 0.f ? kHasDep : 0) | (T.preInh > 0.f ? kHasPreInh : 0);
+  T.flags = (T.bgEvents > 0 ? kHasBg : 0) | (T.depU != 0.f ? kHasDep : 0) | (T.preInh > 0.f ? kHasPreInh : 0) |
+            rest_flags(T);  // the state starts at rest (launch_reset below)
 }
 
 // JS: (seed * 2654435761) >>> 0 || 1, the product formed in double (src/lifwasm.js:52).
@@ -537,7 +543,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     size_t o_cnt = take((size_t)N * 4), o_bucket = take((size_t)N * kBucket * 8);
     size_t o_ovfHead = take((size_t)N * 4), o_bg = take((size_t)N * 4), o_arr = take((size_t)N);
     size_t o_stage = take((size_t)T.nTiles * kTile * 4), o_stageDeg = take((size_t)T.nTiles * kTile * 4);
-    size_t o_tileCnt = take((size_t)T.nTiles * 4), o_tileDeg = take((size_t)T.nTiles * 4);
+    size_t o_tileCnt = take((size_t)T.nTiles * kSubPerTile * 4), o_tileDeg = take((size_t)T.nTiles * kSubPerTile * 4);
     size_t o_dStage = take((size_t)2 * T.maxDch * kBlock * 4), o_dStageDeg = take((size_t)2 * T.maxDch * kBlock * 4);
     size_t o_dCnt = take((size_t)2 * T.maxDch * 4), o_dDeg = take((size_t)2 * T.maxDch * 4);
     size_t o_live = take((size_t)T.maxDch * 8);
@@ -791,6 +797,11 @@ extern "C" int fb_reset(fb_brains *br, int32_t b) {
   int rc = flush(br);
   if (rc) return rc;
   CU(launch_reset(br->trials, b < 0 ? 0 : b, b < 0 ? br->B : b + 1, br->stream));
+  for (int32_t k = b < 0 ? 0 : b; k < (b < 0 ? br->B : b + 1); k++) {  // adapt 0 and res 1 again
+    Trial &T = br->host[k];
+    T.flags = (T.flags & ~(kAdaptZero | kResRest)) | rest_flags(T);
+    CU(cudaMemcpyAsync(&br->trials[k].flags, &T.flags, 4, cudaMemcpyHostToDevice, br->stream));
+  }
   CU(cudaStreamSynchronize(br->stream));
   return FB_OK;
 }
@@ -1189,6 +1200,11 @@ extern "C" int fb_write(fb_brains *br, int32_t field, int32_t b, const void *src
   if (field == FB_FIELD_DRIVE) return fail(FB_EINVAL, "fb_write: the drive field is written through fb_set_drive, which keeps the driven set");
   rc = flush(br);
   if (rc) return rc;
+  const int32_t clear = field == FB_FIELD_ADAPT ? kAdaptZero : field == FB_FIELD_RES ? kResRest : 0;
+  if (br->host[b].flags & clear) {  // the field may no longer be at rest: the update reads it again
+    br->host[b].flags &= ~clear;
+    CU(cudaMemcpyAsync(&br->trials[b].flags, &br->host[b].flags, 4, cudaMemcpyHostToDevice, br->stream));
+  }
   CU(cudaMemcpyAsync(dst, src, (size_t)br->host[b].N * 4, cudaMemcpyDefault, br->stream));
   CU(cudaStreamSynchronize(br->stream));
   return FB_OK;

@@ -10,6 +10,9 @@ namespace fb {
 constexpr int kBlock = 512;          // threads per block of the persistent step kernel
 constexpr int kNPT = 2;              // neurons per thread in the update phase
 constexpr int kTile = kBlock * kNPT; // neurons per update tile
+constexpr int kSub = 64;             // neurons per warp sub-tile (a warp's share of a tile, 2 per lane)
+constexpr int kSubPerTile = kTile / kSub;  // the unit of spike staging, one per warp of the block
+static_assert(kSubPerTile * 32 == kBlock, "one warp per sub-tile");
 constexpr int kDrivenPer = 8;        // driven-list entries per thread and round
 constexpr int kChunk = 32;           // edges per delivery work item (one per lane)
 constexpr int kBucket = 8;           // in-place contribution slots per target and step
@@ -19,6 +22,12 @@ constexpr uint32_t kNil = 0xffffffffu;
 // Per-brain flags (Trial::flags).
 constexpr int32_t kHasBg = 1;        // background events enabled (bgEvents > 0)
 constexpr int32_t kHasDep = 2;       // synaptic depression enabled (depU != 0)
+// Constant state: with adaptInc == 0 an adapt field that is exactly 0 everywhere stays 0
+// (0 * dA = 0, 0 + 0 = 0), and with depU == 0 a res field that is exactly 1 stays 1
+// (1 + (1 - 1) kRec = 1): the update neither reads nor writes it. Set at reset, cleared when the
+// host writes the field.
+constexpr int32_t kAdaptZero = 8;
+constexpr int32_t kResRest = 16;
 constexpr int32_t kHasPreInh = 4;    // presynaptic inhibition (forces sequential delivery)
 
 // One brain of a batch: header constants (f32, rounded once from f64 on the host, the values
@@ -52,7 +61,7 @@ struct Trial {
   // threshold-spike staging per update tile (compacted list + out-degree prefix)
   int32_t *stage;
   uint32_t *stageDeg;
-  int32_t *tileCnt;    // [nTiles], indexed by the brain-local tile
+  int32_t *tileCnt;    // [nTiles * kSubPerTile], indexed by the brain-local warp sub-tile
   uint32_t *tileDeg;
   // forced-spike staging per driven-list chunk of kBlock entries, two step parities:
   // dStage/dStageDeg [2][maxDch * kBlock], dCnt/dDeg [2][maxDch]; liveTag[maxDch] publishes each

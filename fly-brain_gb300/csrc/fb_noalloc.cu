@@ -79,8 +79,8 @@ Layout noalloc_layout(int64_t N, int64_t E, int64_t ns) {
   L.arrived = take((size_t)N);
   L.stage = take((size_t)nTiles * kTile * 4);
   L.stageDeg = take((size_t)nTiles * kTile * 4);
-  L.tileCnt = take((size_t)nTiles * 4);
-  L.tileDeg = take((size_t)nTiles * 4);
+  L.tileCnt = take((size_t)nTiles * kSubPerTile * 4);
+  L.tileDeg = take((size_t)nTiles * kSubPerTile * 4);
   L.dStage = take((size_t)2 * maxDch * kBlock * 4);
   L.dStageDeg = take((size_t)2 * maxDch * kBlock * 4);
   L.dCnt = take((size_t)2 * maxDch * 4);

@@ -205,7 +205,7 @@ __device__ void materialize_brain(const StepArgs &a, const Trial &T, Trial *G, i
   const int tid = threadIdx.x;
   const int N = T.N;
   const int64_t dpar = (int64_t)(gstep & 1) * T.maxDch;
-  const int nUnits = nDch + T.nTiles;
+  const int nUnits = nDch + T.nTiles * kSubPerTile;
   int32_t *out = T.ring + (int64_t)slot * N;
   uint32_t *outOff = T.ringOff + (int64_t)slot * (N + 1);
   uint32_t *outRow = T.ringRow + (int64_t)slot * N;
@@ -221,7 +221,7 @@ __device__ void materialize_brain(const StepArgs &a, const Trial &T, Trial *G, i
         m = (uint32_t)ldcg(T.dCnt + dpar + u);
         dsum = ldcg(T.dDeg + dpar + u);
       } else {
-        m = (uint32_t)ldcg(T.tileCnt + (u - nDch));  // brain-local tile index
+        m = (uint32_t)ldcg(T.tileCnt + (u - nDch));  // brain-local warp sub-tile
         dsum = ldcg(T.tileDeg + (u - nDch));
       }
     }
@@ -240,8 +240,8 @@ __device__ void materialize_brain(const StepArgs &a, const Trial &T, Trial *G, i
     for (uint32_t z = tid >> 5; z < nz; z += blockDim.x >> 5) {
       const uint32_t uu = uIdx[z], mm = uCnt[z], before = uOff[z], dbefore = uDeg[z];
       const bool drv = (int)uu < nDch;
-      const int32_t *stage = drv ? T.dStage + (dpar + uu) * kBlock : T.stage + (int64_t)(uu - nDch) * kTile;
-      const uint32_t *stageDeg = drv ? T.dStageDeg + (dpar + uu) * kBlock : T.stageDeg + (int64_t)(uu - nDch) * kTile;
+      const int32_t *stage = drv ? T.dStage + (dpar + uu) * kBlock : T.stage + (int64_t)(uu - nDch) * kSub;
+      const uint32_t *stageDeg = drv ? T.dStageDeg + (dpar + uu) * kBlock : T.stageDeg + (int64_t)(uu - nDch) * kSub;
       for (uint32_t p = tid & 31; p < mm; p += 32) {
         const int32_t i = ldcg(stage + p);
         const uint32_t k = before + p, o = dbefore + ldcg(stageDeg + p);
@@ -296,7 +296,7 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T,
   // the edge's loads are issued with the presynaptic ones, before the zero-amplitude test
   const uint32_t q = __ldg(T.indices + j);
   const float wj = __ldg(T.W + j);
-  const float amp = __fmul_rn(__ldg(T.sign + pre), ldcg(T.res + pre));  // lif.c:37
+  const float amp = __fmul_rn(__ldg(T.sign + pre), (T.flags & kResRest) ? 1.f : ldcg(T.res + pre));  // lif.c:37
   if (amp == 0.f) return;
   const float w = __fmul_rn(wj, amp);  // lif.c:41-42, one rounding
   const bool inh = !(amp > 0);
@@ -394,8 +394,8 @@ __device__ __forceinline__ NState load_neuron(const Trial &T, int i) {
   x.ge = ldcg(T.gE + i);
   x.gi = ldcg(T.gI + i);
   x.tr = ldcg(T.trace + i);
-  x.ad = ldcg(T.adapt + i);
-  x.rs = ldcg(T.res + i);
+  x.ad = (T.flags & kAdaptZero) ? 0.f : ldcg(T.adapt + i);
+  x.rs = (T.flags & kResRest) ? 1.f : ldcg(T.res + i);
   x.bias = ldcg(T.bias + i);
   x.thr = ldcg(T.thr + i);
   x.n = T.mode == FB_DELIVER_EXACT ? ldcg(T.cnt + i) : 0u;
@@ -456,52 +456,63 @@ __device__ __forceinline__ uint32_t update_neuron(const StepArgs &a, const Trial
   T.gE[i] = ge;
   T.gI[i] = gi;
   T.trace[i] = tr;
-  T.adapt[i] = ad;
-  T.res[i] = rs;
+  if (!(T.flags & kAdaptZero)) T.adapt[i] = ad;
+  if (!(T.flags & kResRest)) T.res[i] = rs;
   return fired;
 }
 
-// One tile of kTile neurons: thread t updates local neurons t and t + kBlock. The tile's spikes
-// are compacted in ascending order with their out-degree prefix (skipped when none fired).
-__device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, uint32_t gparity, uint32_t *scan,
-                            uint64_t *scan64) {
-  const int tid = threadIdx.x;
+// One tile of kTile neurons, one warp sub-tile of kSub neurons per warp: lane l updates the
+// sub-tile's neurons l and l + 32, both loaded before either is stored. Each warp stages its
+// spikes in ascending order with their out-degree prefix (ballots and a warp scan), so no block
+// barrier paces the tile loop; materialization concatenates the sub-tiles in order.
+__device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, uint32_t gparity) {
+  const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
   const int local = t - T.tileBase;
   FB_GUARD(a, local >= 0 && local < T.nTiles, 8, local, t, return);
-  const int i0 = local * kTile + tid, i1 = i0 + kBlock;
+  const int sub = local * kSubPerTile + (int)(threadIdx.x >> 5);
+  const int i0 = sub * kSub + (int)lane, i1 = i0 + 32;
   const int N = T.N;
   // both neurons' loads are issued before either is stored (the stores could alias them)
   const NState x0 = load_neuron(T, i0 < N ? i0 : 0);
   const NState x1 = load_neuron(T, i1 < N ? i1 : 0);
   const uint32_t f0 = i0 < N ? update_neuron(a, T, G, i0, x0, gparity) : 0;
   const uint32_t f1 = i1 < N ? update_neuron(a, T, G, i1, x1, gparity) : 0;
-  if (!__syncthreads_or(f0 | f1)) {
-    if (tid == 0) {
-      T.tileCnt[local] = 0;
-      T.tileDeg[local] = 0;
+  const uint32_t b0 = __ballot_sync(0xffffffffu, f0 != 0), b1 = __ballot_sync(0xffffffffu, f1 != 0);
+  if (!(b0 | b1)) {
+    if (lane == 0) {
+      T.tileCnt[sub] = 0;
+      T.tileDeg[sub] = 0;
     }
     return;
   }
-  const uint32_t c0 = f0 ? 1u : 0u, c1 = f1 ? 1u : 0u;
+  // out-degree prefix in ascending order: the lanes' first neurons, then their second ones
   const uint32_t d0 = f0 ? f0 - 1 : 0u, d1 = f1 ? f1 - 1 : 0u;
-  uint32_t ctot;
-  const uint32_t cpre = block_exclusive_scan(c0 | (c1 << 16), &ctot, scan);
-  uint64_t dtot;
-  const uint64_t dpre = block_exclusive_scan((uint64_t)d0 | ((uint64_t)d1 << 32), &dtot, scan64);
-  const uint32_t n0 = ctot & 0xffffu, dsum0 = (uint32_t)dtot;
-  int32_t *stage = T.stage + (int64_t)local * kTile;
-  uint32_t *stageDeg = T.stageDeg + (int64_t)local * kTile;
+  uint32_t s0 = d0, s1 = d1;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y0 = __shfl_up_sync(0xffffffffu, s0, o), y1 = __shfl_up_sync(0xffffffffu, s1, o);
+    if ((int)lane >= o) {
+      s0 += y0;
+      s1 += y1;
+    }
+  }
+  const uint32_t tot0 = __shfl_sync(0xffffffffu, s0, 31), tot1 = __shfl_sync(0xffffffffu, s1, 31);
+  const uint32_t n0 = __popc(b0);
+  int32_t *stage = T.stage + (int64_t)sub * kSub;
+  uint32_t *stageDeg = T.stageDeg + (int64_t)sub * kSub;
   if (f0) {
-    stage[cpre & 0xffffu] = i0;
-    stageDeg[cpre & 0xffffu] = (uint32_t)dpre;
+    const uint32_t p = __popc(b0 & lt);
+    stage[p] = i0;
+    stageDeg[p] = s0 - d0;
   }
   if (f1) {
-    stage[n0 + (cpre >> 16)] = i1;
-    stageDeg[n0 + (cpre >> 16)] = dsum0 + (uint32_t)(dpre >> 32);
+    const uint32_t p = n0 + __popc(b1 & lt);
+    stage[p] = i1;
+    stageDeg[p] = tot0 + s1 - d1;
   }
-  if (tid == 0) {
-    T.tileCnt[local] = (int32_t)(n0 + (ctot >> 16));
-    T.tileDeg[local] = dsum0 + (uint32_t)(dtot >> 32);
+  if (lane == 0) {
+    T.tileCnt[sub] = (int32_t)(n0 + __popc(b1));
+    T.tileDeg[sub] = tot0 + tot1;
   }
 }
 
@@ -655,7 +666,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
     if (blockIdx.x == 0 && tid == 0) a.ovfTop[(s + 1) & 1] = 0;
     for (int t = blockIdx.x; t < a.nTilesTotal; t += gridDim.x) {
       const int b = tile_brain(t);
-      if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (uint32_t)(s & 1), scan, scan64);
+      if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (uint32_t)(s & 1));
     }
     lap(3);
     if (!grid_sync(a)) return;
