@@ -461,15 +461,15 @@ __device__ __forceinline__ uint32_t update_neuron(const StepArgs &a, const Trial
   return fired;
 }
 
-// One tile of kTile neurons, one warp sub-tile of kSub neurons per warp: lane l updates the
-// sub-tile's neurons l and l + 32, both loaded before either is stored. Each warp stages its
+// Warp sub-tile w (kSub neurons) of tile t: lane l updates the sub-tile's neurons l and l + 32,
+// both loaded before either is stored. Each warp stages its
 // spikes in ascending order with their out-degree prefix (ballots and a warp scan), so no block
 // barrier paces the tile loop; materialization concatenates the sub-tiles in order.
-__device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, uint32_t gparity) {
+__device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, int w, uint32_t gparity) {
   const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
   const int local = t - T.tileBase;
   FB_GUARD(a, local >= 0 && local < T.nTiles, 8, local, t, return);
-  const int sub = local * kSubPerTile + (int)(threadIdx.x >> 5);
+  const int sub = local * kSubPerTile + w;
   const int i0 = sub * kSub + (int)lane, i1 = i0 + 32;
   const int N = T.N;
   // both neurons' loads are issued before either is stored (the stores could alias them)
@@ -664,9 +664,11 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
     // the overflow pool alternates with the launch-local step parity; the half used next step
     // was last read in the update phase of the step before this one
     if (blockIdx.x == 0 && tid == 0) a.ovfTop[(s + 1) & 1] = 0;
-    for (int t = blockIdx.x; t < a.nTilesTotal; t += gridDim.x) {
+    // warp sub-tiles dealt over every warp of the grid (a warp per sub-tile, no block barrier)
+    for (int64_t gs = gwarp; gs < (int64_t)a.nTilesTotal * kSubPerTile; gs += nwarps) {
+      const int t = (int)(gs / kSubPerTile);
       const int b = tile_brain(t);
-      if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (uint32_t)(s & 1));
+      if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (int)(gs % kSubPerTile), (uint32_t)(s & 1));
     }
     lap(3);
     if (!grid_sync(a)) return;
