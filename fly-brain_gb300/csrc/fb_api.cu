@@ -435,6 +435,7 @@ struct fb_brains {
   size_t smem = 0;
   int blocksPerSm = 0, maxBlocksPerSm = 0, sms = 0;  // the persistent grid: sms x blocksPerSm
   int32_t itemChunks = 1;
+  int32_t subGrab = 4;
   int logging = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float lastMs = 0.f;
@@ -470,7 +471,7 @@ static void fill_constants(Trial &T, const fb_params &p, int32_t N) {
   T.bgAmp = (float)p.bgAmp;
   T.preInh = (float)p.preInh;
   T.flags = (T.bgEvents > 0 ? kHasBg : 0) | (T.depU != 0.f ? kHasDep : 0) | (T.preInh > 0.f ? kHasPreInh : 0) |
-            rest_flags(T);  // the state starts at rest (launch_reset below)
+            rest_flags(T) | kBiasZero | kThrZero;  // the state starts at rest (launch_reset below)
 }
 
 // JS: (seed * 2654435761) >>> 0 || 1, the product formed in double (src/lifwasm.js:52).
@@ -582,7 +583,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
       cudaMalloc(&br->d_err, sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&br->d_dbg, sizeof(uint32_t) * 4) != cudaSuccess ||
       cudaMalloc(&br->d_bar, sizeof(uint32_t) * fb_brains::kBarWords) != cudaSuccess ||
-      cudaMalloc(&br->d_ovfTop, sizeof(uint32_t) * 2) != cudaSuccess)
+      cudaMalloc(&br->d_ovfTop, sizeof(uint32_t) * 4) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: batch buffers"));
   // overflow pool: 1M records per parity plus one per 16 edges of the largest graph
   int64_t maxE = 0;
@@ -594,7 +595,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
   if (cudaMemsetAsync(br->d_err, 0, 4, br->stream) != cudaSuccess ||
       cudaMemsetAsync(br->d_dbg, 0, 16, br->stream) != cudaSuccess ||
       cudaMemsetAsync(br->d_bar, 0, sizeof(uint32_t) * fb_brains::kBarWords, br->stream) != cudaSuccess ||
-      cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream) != cudaSuccess ||
+      cudaMemsetAsync(br->d_ovfTop, 0, 16, br->stream) != cudaSuccess ||
       cudaMemcpyAsync(br->d_tileTrial, br->tileTrial.data(), sizeof(int32_t) * nTiles, cudaMemcpyHostToDevice, br->stream) != cudaSuccess ||
       cudaMemcpyAsync(br->trials, br->host.data(), sizeof(Trial) * B, cudaMemcpyHostToDevice, br->stream) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: upload failed"));
@@ -649,14 +650,16 @@ extern "C" int fb_brains_set_schedule(fb_brains *br, int32_t schedule) {
 
 extern "C" int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t) {
   if (!br || !t) return fail(FB_EINVAL, "fb_brains_set_tuning: null argument");
-  if (t->blocks_per_sm < 0 || t->blocks_per_sm > br->maxBlocksPerSm || t->item_chunks < 0 || t->item_chunks > 64)
-    return fail(FB_EINVAL, "fb_brains_set_tuning: blocks_per_sm %d (1..%d), item_chunks %d (1..64)", t->blocks_per_sm,
-                br->maxBlocksPerSm, t->item_chunks);
+  if (t->blocks_per_sm < 0 || t->blocks_per_sm > br->maxBlocksPerSm || t->item_chunks < 0 || t->item_chunks > 64 ||
+      t->sub_grab < -1 || t->sub_grab > 256)
+    return fail(FB_EINVAL, "fb_brains_set_tuning: blocks_per_sm %d (1..%d), item_chunks %d (1..64), sub_grab %d (-1, 1..256)",
+                t->blocks_per_sm, br->maxBlocksPerSm, t->item_chunks, t->sub_grab);
   if (t->blocks_per_sm) {
     br->blocksPerSm = t->blocks_per_sm;
     br->grid = br->sms * br->blocksPerSm;
   }
   if (t->item_chunks) br->itemChunks = t->item_chunks;
+  if (t->sub_grab) br->subGrab = t->sub_grab < 0 ? 0 : t->sub_grab;
   return FB_OK;
 }
 
@@ -664,6 +667,8 @@ extern "C" int fb_brains_tuning(fb_brains *br, fb_tuning *t) {
   if (!br || !t) return fail(FB_EINVAL, "fb_brains_tuning: null argument");
   t->blocks_per_sm = br->blocksPerSm;
   t->item_chunks = br->itemChunks;
+  t->sub_grab = br->subGrab ? br->subGrab : -1;
+  t->pad = 0;
   t->max_blocks_per_sm = br->maxBlocksPerSm;
   t->sms = br->sms;
   return FB_OK;
@@ -751,6 +756,19 @@ static int queue(fb_brains *br, int32_t b, int32_t field, const int32_t *idx, co
       return fail(FB_EINVAL, "%s: value %g is not finite", fn, val[k]);
   }
   for (int32_t k = 0; k < n; k++) br->deltas.push_back(Delta{b, field, idx[k], 0, val[k]});
+  if (field == FB_FIELD_BIAS || field == FB_FIELD_THR) {  // a word other than +0: the update reads the field
+    const int32_t zf = field == FB_FIELD_BIAS ? kBiasZero : kThrZero;
+    Trial &T = br->host[b];
+    for (int32_t k = 0; k < n && (T.flags & zf); k++) {
+      const float f = (float)val[k];
+      uint32_t bits;
+      std::memcpy(&bits, &f, 4);
+      if (bits != 0u) {
+        T.flags &= ~zf;
+        CU(cudaMemcpyAsync(&br->trials[b].flags, &T.flags, 4, cudaMemcpyHostToDevice, br->stream));
+      }
+    }
+  }
   return FB_OK;
 }
 
@@ -1036,6 +1054,8 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     a.ovfCap = br->ovfCap;
     a.log = br->logging;
     a.itemChunks = br->itemChunks;
+    a.subGrab = br->subGrab;
+    a.subNext = br->d_ovfTop + 2;
     a.timeoutNs = 5000000000LL;
     a.dbg = br->d_dbg;
     CU(cudaEventRecord(br->ev0, br->stream));
@@ -1049,7 +1069,7 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
       // leave the handle launchable: clear the flag, the barrier and the overflow pool
       cudaMemsetAsync(br->d_err, 0, 4, br->stream);
       cudaMemsetAsync(br->d_bar, 0, sizeof(uint32_t) * fb_brains::kBarWords, br->stream);
-      cudaMemsetAsync(br->d_ovfTop, 0, 8, br->stream);
+      cudaMemsetAsync(br->d_ovfTop, 0, 16, br->stream);
       cudaStreamSynchronize(br->stream);
       uint32_t dbg[4] = {0, 0, 0, 0};
       cudaMemcpy(dbg, br->d_dbg, 16, cudaMemcpyDeviceToHost);
@@ -1200,7 +1220,8 @@ extern "C" int fb_write(fb_brains *br, int32_t field, int32_t b, const void *src
   if (field == FB_FIELD_DRIVE) return fail(FB_EINVAL, "fb_write: the drive field is written through fb_set_drive, which keeps the driven set");
   rc = flush(br);
   if (rc) return rc;
-  const int32_t clear = field == FB_FIELD_ADAPT ? kAdaptZero : field == FB_FIELD_RES ? kResRest : 0;
+  const int32_t clear = field == FB_FIELD_ADAPT ? kAdaptZero : field == FB_FIELD_RES ? kResRest
+                        : field == FB_FIELD_BIAS ? kBiasZero : field == FB_FIELD_THR ? kThrZero : 0;
   if (br->host[b].flags & clear) {  // the field may no longer be at rest: the update reads it again
     br->host[b].flags &= ~clear;
     CU(cudaMemcpyAsync(&br->trials[b].flags, &br->host[b].flags, 4, cudaMemcpyHostToDevice, br->stream));

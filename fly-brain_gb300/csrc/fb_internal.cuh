@@ -29,6 +29,11 @@ constexpr int32_t kHasDep = 2;       // synaptic depression enabled (depU != 0)
 constexpr int32_t kAdaptZero = 8;
 constexpr int32_t kResRest = 16;
 constexpr int32_t kHasPreInh = 4;    // presynaptic inhibition (forces sequential delivery)
+// Zero parameters: a bias (thr) field whose every word is +0.0f, as at creation, is not read; the
+// update adds the literal +0.0f in its place, the same IEEE operation on the same operands.
+// Cleared when the host stores a word other than +0.0f into the field.
+constexpr int32_t kBiasZero = 32;
+constexpr int32_t kThrZero = 64;
 
 // One brain of a batch: header constants (f32, rounded once from f64 on the host, the values
 // LIFWasm._writeHeader stores), graph and state pointers, delivery scratch, dynamic scalars.
@@ -108,7 +113,8 @@ struct StepArgs {
   uint32_t ovfCap;
   int32_t log;               // 1: record per-step fired counts / lists
   int32_t itemChunks;        // kChunk-edge delivery chunks per warp work item (>= 1)
-  int32_t pad1;
+  int32_t subGrab;           // update sub-tiles per dynamic grab (0: every sub-tile dealt statically)
+  uint32_t *subNext;         // [2] per step parity: next dynamically dealt sub-tile
   int64_t timeoutNs;
   uint32_t *dbg;             // checked builds: [site, value, value, count] of the first bad index
 };

@@ -396,8 +396,8 @@ __device__ __forceinline__ NState load_neuron(const Trial &T, int i) {
   x.tr = ldcg(T.trace + i);
   x.ad = (T.flags & kAdaptZero) ? 0.f : ldcg(T.adapt + i);
   x.rs = (T.flags & kResRest) ? 1.f : ldcg(T.res + i);
-  x.bias = ldcg(T.bias + i);
-  x.thr = ldcg(T.thr + i);
+  x.bias = (T.flags & kBiasZero) ? 0.f : ldcg(T.bias + i);
+  x.thr = (T.flags & kThrZero) ? 0.f : ldcg(T.thr + i);
   x.n = T.mode == FB_DELIVER_EXACT ? ldcg(T.cnt + i) : 0u;
   x.hits = (T.flags & kHasBg) ? ldcg(T.bgHits + i) : 0u;
   x.arrived = ((T.flags & kHasDep) && T.mode != FB_DELIVER_SEQUENTIAL) ? ldcg(T.arrived + i) : (uint8_t)0;
@@ -451,11 +451,16 @@ __device__ __forceinline__ uint32_t update_neuron(const StepArgs &a, const Trial
     T.spikeCount[i] = ldcg(T.spikeCount + i) + 1u;
     fired = 1 + __ldg(T.indptr + i + 1) - __ldg(T.indptr + i);
   }
-  T.v[i] = v;
-  T.refr[i] = r;
-  T.gE[i] = ge;
-  T.gI[i] = gi;
-  T.trace[i] = tr;
+  // Words that provably keep their bits are not stored, so sectors no neuron changed cost no DRAM
+  // write: the refractory count of a neuron neither refractory nor firing (r = r), a trace of +0
+  // without a spike (0 * dTr = +0), a conductance of +0 with no contribution or background hit
+  // (0 * dE = +0), a membrane potential that came out bit-identical.
+  const bool input = x.n != 0u || x.hits != 0u;
+  if (__float_as_uint(v) != __float_as_uint(x.v)) T.v[i] = v;
+  if (refractory || fired) T.refr[i] = r;
+  if (__float_as_uint(x.ge) != 0u || input) T.gE[i] = ge;
+  if (__float_as_uint(x.gi) != 0u || input) T.gI[i] = gi;
+  if (__float_as_uint(x.tr) != 0u || fired) T.trace[i] = tr;
   if (!(T.flags & kAdaptZero)) T.adapt[i] = ad;
   if (!(T.flags & kResRest)) T.res[i] = rs;
   return fired;
@@ -591,6 +596,8 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
   const uint32_t gwarp = blockIdx.x * warpsPerBlock + (tid >> 5);
   const uint32_t nwarps = gridDim.x * warpsPerBlock;
 
+  // the first step's grab counter; later ones are cleared a step ahead in the update phase
+  if (blockIdx.x == 0 && tid == 0 && a.subGrab) a.subNext[0] = 0;
   uint64_t tp = a.phaseNs != nullptr ? global_ns() : 0;
   auto lap = [&](int k) { prof_lap(a, k, tp); };
   for (int s = 0; s <= a.maxSteps; s++) {
@@ -664,11 +671,29 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
     // the overflow pool alternates with the launch-local step parity; the half used next step
     // was last read in the update phase of the step before this one
     if (blockIdx.x == 0 && tid == 0) a.ovfTop[(s + 1) & 1] = 0;
-    // warp sub-tiles dealt over every warp of the grid (a warp per sub-tile, no block barrier)
-    for (int64_t gs = gwarp; gs < (int64_t)a.nTilesTotal * kSubPerTile; gs += nwarps) {
-      const int t = (int)(gs / kSubPerTile);
-      const int b = tile_brain(t);
-      if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (int)(gs % kSubPerTile), (uint32_t)(s & 1));
+    if (blockIdx.x == 0 && tid == 0 && a.subGrab) a.subNext[(s + 1) & 1] = 0;
+    // warp sub-tiles (a warp per sub-tile, no block barrier): with many sub-tiles per warp the
+    // first 5/8 are dealt over every warp of the grid and the rest taken subGrab at a time from a
+    // counter, so warps that drew slow sub-tiles take fewer of the rest
+    {
+      const int64_t total = (int64_t)a.nTilesTotal * kSubPerTile;
+      const bool dyn = a.subGrab > 0 && total >= 8 * (int64_t)nwarps;
+      int64_t gs = gwarp, end = dyn ? total * 5 / 8 : total, stride = nwarps;
+      for (;;) {
+        if (gs >= end) {
+          if (!dyn) break;
+          uint32_t g0 = 0;
+          if ((tid & 31) == 0) g0 = atomicAdd(a.subNext + (s & 1), (uint32_t)a.subGrab);
+          gs = total * 5 / 8 + (int64_t)__shfl_sync(0xffffffffu, g0, 0);
+          end = min(total, gs + a.subGrab);
+          stride = 1;
+          if (gs >= total) break;
+        }
+        const int t = (int)(gs / kSubPerTile);
+        const int b = tile_brain(t);
+        if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (int)(gs % kSubPerTile), (uint32_t)(s & 1));
+        gs += stride;
+      }
     }
     lap(3);
     if (!grid_sync(a)) return;

@@ -71,7 +71,7 @@ class FbDiffGrads(C.Structure):
 
 
 class FbTuning(C.Structure):
-    _fields_ = [(k, C.c_int32) for k in ("blocks_per_sm", "item_chunks", "max_blocks_per_sm", "sms")]
+    _fields_ = [(k, C.c_int32) for k in ("blocks_per_sm", "item_chunks", "max_blocks_per_sm", "sms", "sub_grab", "pad")]
 
 
 class FbDiffTuning(C.Structure):

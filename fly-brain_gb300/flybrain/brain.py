@@ -155,15 +155,15 @@ class BrainBatch:
         nat.check(self.L.fb_last_schedule(self.h, C.byref(x)))
         return x.value
 
-    def set_tuning(self, blocks_per_sm: int = 0, item_chunks: int = 0):
+    def set_tuning(self, blocks_per_sm: int = 0, item_chunks: int = 0, sub_grab: int = 0):
         """Launch shape of the grid schedule (fb_brains_set_tuning); 0 keeps a knob."""
-        t = nat.FbTuning(int(blocks_per_sm), int(item_chunks), 0, 0)
+        t = nat.FbTuning(int(blocks_per_sm), int(item_chunks), 0, 0, int(sub_grab), 0)
         nat.check(self.L.fb_brains_set_tuning(self.h, C.byref(t)))
 
     def tuning(self) -> dict:
         t = nat.FbTuning()
         nat.check(self.L.fb_brains_tuning(self.h, C.byref(t)))
-        return {k: getattr(t, k) for k, _ in nat.FbTuning._fields_}
+        return {k: getattr(t, k) for k, _ in nat.FbTuning._fields_ if k != "pad"}
 
     def step(self, nsteps: int = 1) -> np.ndarray:
         out = np.zeros(self.B, dtype=np.int32)

@@ -151,11 +151,16 @@ int fb_last_schedule(fb_brains *br, int32_t *schedule);
 /* Launch shape of the grid schedule's persistent kernel, the knobs the autotuner
  * (flybrain.autotune) searches: resident CTAs per SM (1 .. max_blocks_per_sm; the grid is
  * sms x blocks_per_sm, 512 threads each) and kChunk = 32-edge delivery chunks per warp work item
- * (edges per warp item = 32 x item_chunks, 1 .. 64). fb_brains_set_tuning ignores max_blocks_per_sm
- * and sms; 0 in a field keeps its current value. Results do not depend on the shape. */
+ * (edges per warp item = 32 x item_chunks, 1 .. 64), and how the update phase's 64-neuron warp
+ * sub-tiles reach the warps when each warp has many (a batch): 5/8 dealt round-robin, the rest
+ * taken sub_grab at a time from a counter, or all dealt (-1). fb_brains_set_tuning ignores
+ * max_blocks_per_sm and sms; 0 in a field keeps its current value. Results do not depend on the
+ * shape. */
 typedef struct fb_tuning {
   int32_t blocks_per_sm, item_chunks;
   int32_t max_blocks_per_sm, sms; /* read only */
+  int32_t sub_grab;               /* update sub-tiles per dynamic grab, 1 .. 256; -1: all dealt statically */
+  int32_t pad;
 } fb_tuning;
 int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t);
 int fb_brains_tuning(fb_brains *br, fb_tuning *t);

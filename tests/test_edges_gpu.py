@@ -135,3 +135,18 @@ def test_flyvis_without_edges():
     O.fv_run(m, v, x, 10)
     for b in range(2):
         assert fv.v(b).tobytes() == v[b].tobytes()
+
+
+def test_signed_zero_and_restored_parameters():
+    """bias and thr written as -0.0, as nonzero values and back to +0.0: each write leaves the
+    step's arithmetic that of lif.c (the update stops treating the field as all +0.0 once a word
+    other than +0.0 is stored)."""
+    from flybrain import SYNTH_PARAMS
+    g = _graph(400, 12, seed=9)
+    N = g.N
+    every = list(range(N))
+    script = [["drive", list(range(0, N, 5)), [220.0] * len(range(0, N, 5))],
+              ["bias", every, -0.0], ["thr", [3], [-0.0]], ["step", 120],
+              ["bias", list(range(0, N, 3)), 2.5], ["thr", list(range(1, N, 4)), [-1.5] * len(range(1, N, 4))],
+              ["step", 120], ["bias", every, 0.0], ["thr", every, [0.0] * N], ["step", 120]]
+    _both_schedules(g, dict(SYNTH_PARAMS), script)

@@ -46,6 +46,48 @@ def test_grid_launch_shape_keeps_the_oracle_raster(shape):
         assert ob.v.tobytes() == batch.read("v", b).tobytes()
 
 
+def test_dynamic_sub_tile_dealing_keeps_the_rasters():
+    """160 brains, enough sub-tiles per warp for the update phase to hand the last 3/8 out from a
+    counter: every brain's raster and state equal the all-dealt launch's, and two brains the
+    oracle's."""
+    from oracle import oracle as O
+    from flybrain import BrainBatch, DeviceGraph, SYNTH_PARAMS, synth_graph
+    from flybrain import _native as nat
+    g = synth_graph(12000, 91)
+    B, steps = 160, 200
+    rng = np.random.default_rng(5)
+    drives = [(np.sort(rng.choice(g.N, 150, replace=False)).astype(np.int32), rng.uniform(80, 300, 150))
+              for _ in range(B)]
+    p = dict(SYNTH_PARAMS, wSyn=1.6)
+    out = []
+    for grab in (-1, 3):
+        topo = DeviceGraph(g)
+        batch = BrainBatch([topo] * B, p, list(range(11, 11 + B)))
+        for b, (idx, hz) in enumerate(drives):
+            batch.set_drive(b, idx, hz)
+        batch.set_tuning(1, 2, grab)
+        assert batch.tuning()["sub_grab"] == grab
+        batch.set_schedule(nat.FB_SCHEDULE_GRID)
+        batch.record(steps, 1 << 18)
+        batch.step(steps)
+        out.append([(batch.spike_log(b, steps, 1 << 18), batch.read("v", b)) for b in range(B)])
+    for b in range(B):
+        (c0, r0), v0 = out[0][b]
+        (c1, r1), v1 = out[1][b]
+        np.testing.assert_array_equal(c0, c1)
+        np.testing.assert_array_equal(r0, r1)
+        assert v0.tobytes() == v1.tobytes()
+    for b in (0, B - 1):
+        ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, p, seed=11 + b)
+        for i, h in zip(*drives[b]):
+            ob.setDriveOne(int(i), float(h))
+        c, r = ob.run(steps, raster=True)
+        (c1, r1), v1 = out[1][b]
+        np.testing.assert_array_equal(c1, c)
+        np.testing.assert_array_equal(r1, r)
+        assert ob.v.tobytes() == v1.tobytes()
+
+
 def test_tuning_is_validated():
     from flybrain import _native as nat
     batch, _, _ = _batch()
@@ -54,6 +96,10 @@ def test_tuning_is_validated():
         batch.set_tuning(t["max_blocks_per_sm"] + 1, 1)
     with pytest.raises(nat.FlyBrainError):
         batch.set_tuning(1, 65)
+    with pytest.raises(nat.FlyBrainError):
+        batch.set_tuning(1, 1, 257)
+    with pytest.raises(nat.FlyBrainError):
+        batch.set_tuning(1, 1, -2)
 
 
 def test_tune_brains_applies_a_valid_shape(tmp_path, monkeypatch):
