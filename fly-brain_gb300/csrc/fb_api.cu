@@ -603,7 +603,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: reset launch failed"));
   // persistent grid: every SM, as many blocks as stay co-resident
   br->smem = step_smem_bytes(B);
-  if (br->smem > 48 * 1024 && set_step_smem(br->smem) != cudaSuccess)
+  if (set_step_smem(br->smem) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ECUDA, "step kernel: %zu bytes of shared memory refused", br->smem));
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, br->dev);

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <mutex>
 
 #include "fb_internal.cuh"
 
@@ -829,13 +830,32 @@ size_t step_smem_bytes(int B) {
   return (size_t)B * 8 * 2 + (size_t)B * 4 * 4 + (size_t)(B + 1) * 4 * 3;
 }
 
+// The kernel's dynamic shared-memory limit, raised (never lowered) per device to the largest
+// size asked for, so a batch's launch never runs under a limit another batch set lower.
+cudaError_t set_step_smem(size_t bytes) {
+  static std::mutex mu;
+  static size_t limit[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[dev & 63];
+  if (bytes <= cur || bytes <= 48 * 1024) return cudaSuccess;
+  e = cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 int step_kernel_blocks_per_sm(size_t smem) {
+  if (set_step_smem(smem) != cudaSuccess) return 0;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel, kBlock, smem) != cudaSuccess) return 0;
   return n;
 }
 
 cudaError_t launch_step(const StepArgs &a, int grid, size_t smem, cudaStream_t st) {
+  const cudaError_t e = set_step_smem(smem);
+  if (e != cudaSuccess) return e;
   void *args[] = {(void *)&a};
   return cudaLaunchCooperativeKernel((const void *)step_kernel, dim3(grid), dim3(kBlock), args, smem, st);
 }
@@ -846,9 +866,6 @@ cudaError_t launch_deltas(Trial *trials, const Delta *d, const int32_t *gs, int3
   return cudaGetLastError();
 }
 
-cudaError_t set_step_smem(size_t bytes) {
-  return cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
 
 cudaError_t launch_rebuild_slots(Trial *Td, int nslots, int32_t *err, cudaStream_t st) {
   rebuild_slots_kernel<<<nslots, kBlock, 0, st>>>(Td, err);

@@ -244,3 +244,20 @@ def test_synchronous_burst_into_one_target():
     assert c0.max() > 100
     for k in ("v", "gE", "gI"):
         assert getattr(ob, k).tobytes() == getattr(gb, k).tobytes(), k
+
+
+def test_large_batches_created_in_either_order():
+    """Two batches whose per-brain launch tables need more than 48 KB of shared memory, the
+    larger created first: both still launch and step like a lone brain of the same seed."""
+    from flybrain import BrainBatch, DeviceGraph, SYNTH_PARAMS, synth_graph
+    g = synth_graph(60, 3)
+    dg = DeviceGraph(g)
+    big = BrainBatch([dg] * 1300, SYNTH_PARAMS, list(range(1, 1301)))
+    small = BrainBatch([dg] * 1150, SYNTH_PARAMS, list(range(1, 1151)))
+    lone = BrainBatch([dg], SYNTH_PARAMS, [7])
+    for batch in (big, small, lone):
+        batch.set_drive(0 if batch is lone else 6, np.arange(0, 60, 3, dtype=np.int32), 400.0)
+        batch.step(50)
+    for batch in (big, small):
+        assert batch.read("v", 6).tobytes() == lone.read("v", 0).tobytes()
+        assert batch.read("spikeCount", 6).tobytes() == lone.read("spikeCount", 0).tobytes()
