@@ -46,6 +46,10 @@ class FbBrainView(C.Structure):
                 + [("E", C.c_int64)])
 
 
+class FbFlygHeader(C.Structure):
+    _fields_ = [(k, C.c_uint32) for k in ("N", "E", "min_weight", "pad")]
+
+
 class FbDiffParams(C.Structure):
     _fields_ = [(k, C.c_double) for k in (
         "dt", "vRest", "vThresh", "vReset", "tauM", "tauSyn", "tRef", "delay", "wSyn", "adaptInc",
@@ -148,6 +152,10 @@ SIGNATURES = {
     "fb_flyvis_step": (C.c_int, [P, I32]),
     "fb_flyvis_last_ms": (C.c_int, [P, C.POINTER(C.c_float)]),
     "fb_flyvis_state": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int32)]),
+    "fb_flyg_sizes": (C.c_int, [P, C.c_size_t, C.POINTER(FbFlygHeader)]),
+    "fb_flyg_decode": (C.c_int, [P, C.c_size_t, P, P, P]),
+    "fb_flyn_count": (C.c_int, [P, C.c_size_t, PU32]),
+    "fb_flyn_decode": (C.c_int, [P, C.c_size_t, P, P, P, P, P, P]),
 }
 
 

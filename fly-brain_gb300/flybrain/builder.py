@@ -17,7 +17,7 @@ CSRC = os.path.join(ROOT, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libflybrain.so")
 CHECK_LIB = os.path.join(OUT_DIR, "libflybrain_check.so")
-SOURCES = ["fb_step.cu", "fb_api.cu", "fb_graph.cu", "fb_noalloc.cu", "fb_adjoint.cu", "fb_lagged.cu", "fb_flyvis.cu"]
+SOURCES = ["fb_step.cu", "fb_api.cu", "fb_graph.cu", "fb_noalloc.cu", "fb_adjoint.cu", "fb_lagged.cu", "fb_flyvis.cu", "fb_codec.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--fmad=false"]
 

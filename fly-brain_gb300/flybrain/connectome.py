@@ -10,6 +10,10 @@ Layouts (scripts/prep_graph.py:46-56, read by scripts/lib_node.mjs:3-13 and src/
   neuron_size.bin        f32[N] (relative volume; <= 0 when unknown)
   ntsign.bin             f32[N] (transmitter sign, graded when unknown)
 
+  graph.flyg / neurons.flyn the same graph and table range coded (src/codec/graph.js,
+                         src/codec/neurons.js): what the web app loads (src/data.js:21-34); decoded
+                         by the native library (fb_flyg_decode, fb_flyn_decode) into the arrays above
+
 load_connectome(dir) returns the tables; to_device_graph(c, params, ...) compiles them on the GPU
 the way writeGraph does (src/lifwasm.js:14-34) with the transmitter signs of src/lif.js:5.
 """
@@ -49,6 +53,39 @@ def load_graph(path: str, N: int | None = None) -> dict:
     return dict(N=n, E=E, indptr=indptr, indices=indices, counts=counts)
 
 
+def load_flyg(path: str) -> dict:
+    """graph.flyg decoded: {N, E, min_weight, indptr u32[N+1], indices u32[E], counts u16[E]}, the
+    arrays of graph_w{min_weight}.bin (src/codec/graph.js:70-108)."""
+    import ctypes as C
+    from . import _native as nat
+    L = nat.load()
+    raw = np.fromfile(path, dtype=np.uint8)
+    h = nat.FbFlygHeader()
+    nat.check(L.fb_flyg_sizes(nat.ptr(raw), raw.shape[0], C.byref(h)))
+    indptr = np.zeros(h.N + 1, np.uint32)
+    indices = np.zeros(h.E, np.uint32)
+    counts = np.zeros(h.E, np.uint16)
+    nat.check(L.fb_flyg_decode(nat.ptr(raw), raw.shape[0], nat.ptr(indptr), nat.ptr(indices), nat.ptr(counts)))
+    return dict(N=int(h.N), E=int(h.E), min_weight=int(h.min_weight), indptr=indptr, indices=indices, counts=counts)
+
+
+def load_flyn(path: str) -> dict:
+    """neurons.flyn decoded: {N, bodyIds, soma, cls, nt, sc, side} as in neurons.bin, soma NaN where
+    absent (src/codec/neurons.js:25-37). In- and out-degrees follow from the graph."""
+    import ctypes as C
+    from . import _native as nat
+    L = nat.load()
+    raw = np.fromfile(path, dtype=np.uint8)
+    n = C.c_uint32()
+    nat.check(L.fb_flyn_count(nat.ptr(raw), raw.shape[0], C.byref(n)))
+    N = int(n.value)
+    out = dict(N=N, bodyIds=np.zeros(N, np.int64), soma=np.zeros((N, 3), np.float32), cls=np.zeros(N, np.uint16),
+               nt=np.zeros(N, np.uint8), sc=np.zeros(N, np.uint8), side=np.zeros(N, np.uint8))
+    nat.check(L.fb_flyn_decode(nat.ptr(raw), raw.shape[0], *(nat.ptr(out[k]) for k in
+                                                              ("bodyIds", "soma", "cls", "nt", "sc", "side"))))
+    return out
+
+
 def load_neurons(path: str, N: int) -> dict:
     """neurons.bin: per-neuron annotations in the layout of scripts/prep_graph.py:54."""
     hdr = _read(path, np.uint32, 2, 0)
@@ -72,11 +109,28 @@ def load_connectome(data_dir: str, min_weight: int | None = None) -> dict:
         meta = json.load(f)
     N = int(meta["N"])
     mw = int(min_weight if min_weight is not None else meta["minWeight"])
-    g = load_graph(os.path.join(data_dir, f"graph_w{mw}.bin"), N)
+    gpath, fpath = os.path.join(data_dir, f"graph_w{mw}.bin"), os.path.join(data_dir, "graph.flyg")
+    if not os.path.exists(gpath) and os.path.exists(fpath):  # the app's compressed copy
+        f = load_flyg(fpath)
+        if f["N"] != N or f["min_weight"] != mw:
+            raise ValueError(f"graph.flyg holds N={f['N']}, minWeight={f['min_weight']}; asked for N={N}, minWeight={mw}")
+        g = {k: f[k] for k in ("N", "E", "indptr", "indices", "counts")}
+    else:
+        g = load_graph(gpath, N)
     if "edges" in meta and min_weight is None and int(meta["edges"]) != g["E"]:
-        raise ValueError(f"graph_w{mw}.bin has {g['E']} edges, the metadata says {meta['edges']}")
+        raise ValueError(f"graph_w{mw} has {g['E']} edges, the metadata says {meta['edges']}")
     c = dict(meta=meta, min_weight=mw, **g)
-    c.update(load_neurons(os.path.join(data_dir, "neurons.bin"), N))
+    npath, fpath = os.path.join(data_dir, "neurons.bin"), os.path.join(data_dir, "neurons.flyn")
+    if not os.path.exists(npath) and os.path.exists(fpath):
+        t = load_flyn(fpath)
+        if t["N"] != N:
+            raise ValueError(f"neurons.flyn holds N={t['N']}, the metadata says {N}")
+        t.pop("N")
+        t["outdeg"] = np.diff(g["indptr"].astype(np.int64)).astype(np.uint32)
+        t["indeg"] = np.bincount(g["indices"], minlength=N).astype(np.uint32)
+        c.update(t)
+    else:
+        c.update(load_neurons(npath, N))
     for name, fn in (("size", "neuron_size.bin"), ("ntsign", "ntsign.bin")):
         p = os.path.join(data_dir, fn)
         c[name] = _read(p, np.float32, N, 0) if os.path.exists(p) else None

@@ -465,6 +465,24 @@ typedef struct fb_brain_view {
  * the GPU race on the array: serialise them. */
 int fb_lif_step_noalloc(fb_brain_view *brain, int32_t nsteps, void *stream);
 
+/* ---- the reference's compressed data files (host decoders, no device work) -------------------
+ * FLYG, the connectome CSR the web app loads (graph.flyg; src/codec/graph.js:70-108, read by
+ * src/data.js:28), and FLYN, its per-neuron table (neurons.flyn; src/codec/neurons.js:25-37), both
+ * range coded (src/codec/rc.js). The decoded arrays are those of graph_w{min_weight}.bin (rows by
+ * presynaptic neuron, each ascending by target; weights = synapse counts) and neurons.bin.
+ * fb_flyg_sizes reads the sizes to allocate: indptr[N+1], indices[E], weights[E]. A corrupt
+ * stream returns FB_EINVAL (the outputs are then undefined). */
+typedef struct fb_flyg_header {
+  uint32_t N, E, min_weight, pad;
+} fb_flyg_header;
+int fb_flyg_sizes(const uint8_t *buf, size_t len, fb_flyg_header *h);
+int fb_flyg_decode(const uint8_t *buf, size_t len, uint32_t *indptr, uint32_t *indices, uint16_t *weights);
+/* FLYN: N, then per neuron body_ids[N], soma[N][3] (voxels; NaN when absent), cls[N], nt[N],
+ * superclass[N], side[N]. */
+int fb_flyn_count(const uint8_t *buf, size_t len, uint32_t *N);
+int fb_flyn_decode(const uint8_t *buf, size_t len, int64_t *body_ids, float *soma, uint16_t *cls, uint8_t *nt,
+                   uint8_t *superclass, uint8_t *side);
+
 #ifdef __cplusplus
 }
 #endif
