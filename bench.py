@@ -202,8 +202,11 @@ def run_ours(args, rank, world):
 
     # ---- end to end through the C ABI with host buffers ----
     brain.reset()
-    h_idx = np.ascontiguousarray(idx, dtype=np.int32)
-    h_hz = np.ascontiguousarray(hz, dtype=np.float64)
+    # inputs and results in pinned host memory
+    h_idx = torch.from_numpy(np.ascontiguousarray(idx, dtype=np.int32)).pin_memory().numpy()
+    h_hz = torch.from_numpy(np.ascontiguousarray(hz, dtype=np.float64)).pin_memory().numpy()
+    h_sc = torch.empty(g.N, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    h_fired = torch.empty(g.N, dtype=torch.int32).pin_memory().numpy()
     e2e_events, h2d, d2h = 0.0, 0, 0
     sc_prev = np.zeros(g.N, dtype=np.int64)
     barrier(world)
@@ -212,8 +215,8 @@ def run_ours(args, rank, world):
         brain._batch.set_drive(0, h_idx, h_hz)
         h2d += h_idx.nbytes + h_hz.nbytes
         brain.run(S)
-        sc = brain._batch.read("spikeCount", 0).astype(np.int64)
-        fired = brain._batch.fired(0)
+        sc = brain._batch.read("spikeCount", 0, out=h_sc).astype(np.int64)
+        fired = brain._batch.fired(0, out=h_fired)
         d2h += g.N * 4 + fired.nbytes
         e2e_events += float(((sc - sc_prev) * outdeg).sum())
         sc_prev = sc

@@ -204,12 +204,19 @@ class BrainBatch:
                                       raster.shape[0], C.byref(ns), C.byref(nk)))
         return counts, raster
 
-    def fired(self, b: int = 0) -> np.ndarray:
+    def fired(self, b: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        """The last step's fired list. out: an int32 buffer of capacity N (e.g. pinned host
+        memory) read in one call; the result is a view of its first entries."""
         n = C.c_int32()
+        if out is not None:
+            if out.dtype != np.int32 or not out.flags.c_contiguous or out.shape[0] < self.N[b]:
+                raise ValueError("fired: out must be a contiguous int32 array of at least N entries")
+            nat.check(self.L.fb_fired(self.h, b, nat.ptr(out), out.shape[0], C.byref(n)))
+            return out[:n.value]
         nat.check(self.L.fb_fired(self.h, b, None, 0, C.byref(n)))
-        out = np.zeros(n.value, dtype=np.int32)
-        nat.check(self.L.fb_fired(self.h, b, nat.ptr(out), n.value, C.byref(n)))
-        return out
+        res = np.zeros(n.value, dtype=np.int32)
+        nat.check(self.L.fb_fired(self.h, b, nat.ptr(res), n.value, C.byref(n)))
+        return res
 
     def _list(self, fn, b, idx, vals):
         idx = np.ascontiguousarray(np.atleast_1d(idx), dtype=np.int32)
@@ -240,9 +247,13 @@ class BrainBatch:
     def set_background(self, b, rate_hz, amp_mv):
         nat.check(self.L.fb_set_background(self.h, b, float(rate_hz), float(amp_mv)))
 
-    def read(self, field: str, b: int = 0) -> np.ndarray:
+    def read(self, field: str, b: int = 0, out: np.ndarray | None = None) -> np.ndarray:
+        """A state field of brain b; out: a contiguous destination of N entries (e.g. pinned)."""
         dt = np.uint32 if field == "spikeCount" else np.float32
-        out = np.zeros(self.N[b], dtype=dt)
+        if out is None:
+            out = np.zeros(self.N[b], dtype=dt)
+        elif out.dtype != dt or not out.flags.c_contiguous or out.shape[0] != self.N[b]:
+            raise ValueError(f"read: out must be a contiguous {np.dtype(dt).name} array of N entries")
         nat.check(self.L.fb_read(self.h, nat.FIELDS[field], b, nat.ptr(out)))
         return out
 
