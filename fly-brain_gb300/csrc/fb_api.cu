@@ -420,6 +420,17 @@ struct fb_brains {
   int32_t *d_tileTrial = nullptr, *d_steps = nullptr, *d_err = nullptr, *d_groups = nullptr;
   Delta *d_deltas = nullptr;
   size_t deltaCap = 0, groupCap = 0;
+  // pinned staging of a call's small transfers: queued writes and their group starts, the step
+  // counts, the error flag and fired counts read back. A flush's copies leave the staging before
+  // the next flush refills it (flushDone); the step counts are copied only when they change.
+  Delta *h_deltas = nullptr;
+  int32_t *h_groups = nullptr;
+  size_t hDeltaCap = 0, hGroupCap = 0;
+  int32_t *h_small = nullptr;  // [2 + B]: error flag, unused, fired count of each brain
+  int32_t *h_steps = nullptr;  // [B]
+  std::vector<int32_t> stepsUploaded, groupStarts;
+  cudaEvent_t flushDone = nullptr;
+  bool flushPending = false;
   uint32_t *d_bar = nullptr;   // the grid barrier's counter word (own 128-byte line)
   static constexpr size_t kBarWords = 32;
   unsigned long long *d_phase = nullptr;  // per-phase ns accumulators when profiling
@@ -614,6 +625,10 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
   br->blocksPerSm = br->maxBlocksPerSm = per;
   cudaEventCreate(&br->ev0);
   cudaEventCreate(&br->ev1);
+  cudaEventCreateWithFlags(&br->flushDone, cudaEventDisableTiming);
+  if (cudaMallocHost(&br->h_small, sizeof(int32_t) * (2 + (size_t)B)) != cudaSuccess ||
+      cudaMallocHost(&br->h_steps, sizeof(int32_t) * (size_t)B) != cudaSuccess)
+    return brains_fail_cleanup(br, fail(FB_ENOMEM, "fb_brains_create: pinned host staging"));
   if (cudaStreamSynchronize(br->stream) != cudaSuccess)
     return brains_fail_cleanup(br, fail(FB_ECUDA, "fb_brains_create: %s", cudaGetErrorString(cudaGetLastError())));
   *out = br;
@@ -636,6 +651,11 @@ extern "C" int fb_brains_destroy(fb_brains *br) {
   for (void *p : br->lag.allocs) cudaFree(p);
   if (br->ev0) cudaEventDestroy(br->ev0);
   if (br->ev1) cudaEventDestroy(br->ev1);
+  if (br->flushDone) cudaEventDestroy(br->flushDone);
+  cudaFreeHost(br->h_deltas);
+  cudaFreeHost(br->h_groups);
+  cudaFreeHost(br->h_small);
+  cudaFreeHost(br->h_steps);
   if (br->stream) cudaStreamDestroy(br->stream);
   delete br;
   return FB_OK;
@@ -699,20 +719,30 @@ static int check_brain(fb_brains *br, int32_t b, const char *fn) {
 }
 
 // Applies queued injections (in call order) and re-uploads changed driven lists.
-static int flush(fb_brains *br) {
+// Applies the queued host writes and the driven set. sync: wait for the writes to land (callers
+// that go on with copies outside the brains' stream); the step path leaves them in stream order.
+static int flush(fb_brains *br, bool sync = true) {
   if (!br->deltas.empty()) {
     std::vector<Delta> &d = br->deltas;
-    std::stable_sort(d.begin(), d.end(), [](const Delta &x, const Delta &y) {
+    auto before = [](const Delta &x, const Delta &y) {
       if (x.brain != y.brain) return x.brain < y.brain;
       if (x.field != y.field) return x.field < y.field;
       return x.idx < y.idx;
-    });
-    std::vector<int32_t> gs;
+    };
+    // groups of one (brain, field, index) in call order; lists written in ascending index order
+    // (the usual case) need no sort
+    if (!std::is_sorted(d.begin(), d.end(), before)) std::stable_sort(d.begin(), d.end(), before);
+    std::vector<int32_t> &gs = br->groupStarts;
+    gs.clear();
     for (size_t k = 0; k < d.size(); k++)
       if (k == 0 || d[k].brain != d[k - 1].brain || d[k].field != d[k - 1].field || d[k].idx != d[k - 1].idx)
         gs.push_back((int32_t)k);
     const int32_t ng = (int32_t)gs.size();
     gs.push_back((int32_t)d.size());
+    if (br->flushPending) {  // the last flush's copies have left the staging (and its kernel ran)
+      CU(cudaEventSynchronize(br->flushDone));
+      br->flushPending = false;
+    }
     if (d.size() > br->deltaCap) {
       cudaFree(br->d_deltas);
       br->deltaCap = std::max<size_t>(d.size(), 1024);
@@ -723,10 +753,25 @@ static int flush(fb_brains *br) {
       br->groupCap = std::max<size_t>(gs.size(), 1025);
       CU(cudaMalloc(&br->d_groups, sizeof(int32_t) * br->groupCap));
     }
-    CU(cudaMemcpyAsync(br->d_deltas, d.data(), sizeof(Delta) * d.size(), cudaMemcpyHostToDevice, br->stream));
-    CU(cudaMemcpyAsync(br->d_groups, gs.data(), sizeof(int32_t) * gs.size(), cudaMemcpyHostToDevice, br->stream));
+    if (d.size() > br->hDeltaCap) {
+      cudaFreeHost(br->h_deltas);
+      br->h_deltas = nullptr;
+      br->hDeltaCap = std::max<size_t>(d.size(), 1024);
+      CU(cudaMallocHost(&br->h_deltas, sizeof(Delta) * br->hDeltaCap));
+    }
+    if (gs.size() > br->hGroupCap) {
+      cudaFreeHost(br->h_groups);
+      br->h_groups = nullptr;
+      br->hGroupCap = std::max<size_t>(gs.size(), 1025);
+      CU(cudaMallocHost(&br->h_groups, sizeof(int32_t) * br->hGroupCap));
+    }
+    std::memcpy(br->h_deltas, d.data(), sizeof(Delta) * d.size());
+    std::memcpy(br->h_groups, gs.data(), sizeof(int32_t) * gs.size());
+    CU(cudaMemcpyAsync(br->d_deltas, br->h_deltas, sizeof(Delta) * d.size(), cudaMemcpyHostToDevice, br->stream));
+    CU(cudaMemcpyAsync(br->d_groups, br->h_groups, sizeof(int32_t) * gs.size(), cudaMemcpyHostToDevice, br->stream));
     CU(launch_deltas(br->trials, br->d_deltas, br->d_groups, ng, br->stream));
-    CU(cudaStreamSynchronize(br->stream));  // host vectors are reused by the next flush
+    CU(cudaEventRecord(br->flushDone, br->stream));
+    br->flushPending = true;
     d.clear();
   }
   for (int b = 0; b < br->B; b++) {
@@ -740,6 +785,10 @@ static int flush(fb_brains *br) {
     CU(cudaMemcpyAsync(&br->trials[b].nDriven, &T.nDriven, 4, cudaMemcpyHostToDevice, br->stream));
     CU(cudaStreamSynchronize(br->stream));
     ds.dirty = false;
+  }
+  if (sync && br->flushPending) {
+    CU(cudaEventSynchronize(br->flushDone));
+    br->flushPending = false;
   }
   return FB_OK;
 }
@@ -1006,7 +1055,7 @@ static int run_lagged(fb_brains *br, int32_t steps) {
 }
 
 static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
-  int rc = flush(br);
+  int rc = flush(br, false);
   if (rc) return rc;
   bool lagged = false;
   if (maxSteps > 0 && br->schedule != FB_SCHEDULE_GRID) {
@@ -1021,11 +1070,20 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
       if (!lagged) g_err.clear();
     }
   }
+  // the error flag and the fired counts come back in one synchronisation
+  auto read_back = [&]() -> int {
+    CU(cudaMemcpyAsync(br->h_small, br->d_err, 4, cudaMemcpyDeviceToHost, br->stream));
+    if (out_nfired)
+      for (int b = 0; b < br->B; b++)
+        CU(cudaMemcpyAsync(br->h_small + 2 + b, &br->trials[b].nFired, 4, cudaMemcpyDeviceToHost, br->stream));
+    CU(cudaStreamSynchronize(br->stream));
+    br->flushPending = false;
+    return FB_OK;
+  };
   if (lagged) {
     if ((rc = run_lagged(br, maxSteps))) return rc;
-    int32_t err = 0;
-    CU(cudaMemcpyAsync(&err, br->d_err, 4, cudaMemcpyDeviceToHost, br->stream));
-    CU(cudaStreamSynchronize(br->stream));
+    if ((rc = read_back())) return rc;
+    const int32_t err = br->h_small[0];
     cudaEventElapsedTime(&br->lastMs, br->ev0, br->ev1);
     if (err) {
       cudaMemsetAsync(br->d_err, 0, 4, br->stream);
@@ -1035,7 +1093,11 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     }
   } else if (maxSteps > 0) {
     br->lastSchedule = FB_SCHEDULE_GRID;
-    CU(cudaMemcpyAsync(br->d_steps, br->stepsHost.data(), sizeof(int32_t) * br->B, cudaMemcpyHostToDevice, br->stream));
+    if (br->stepsUploaded != br->stepsHost) {  // the last launch's counts stay on the device otherwise
+      std::memcpy(br->h_steps, br->stepsHost.data(), sizeof(int32_t) * br->B);
+      CU(cudaMemcpyAsync(br->d_steps, br->h_steps, sizeof(int32_t) * br->B, cudaMemcpyHostToDevice, br->stream));
+      br->stepsUploaded = br->stepsHost;
+    }
     StepArgs a;
     memset(&a, 0, sizeof a);
     a.trials = br->trials;
@@ -1061,9 +1123,8 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     CU(cudaEventRecord(br->ev0, br->stream));
     CU(launch_step(a, br->grid, br->smem, br->stream));
     CU(cudaEventRecord(br->ev1, br->stream));
-    int32_t err = 0;
-    CU(cudaMemcpyAsync(&err, br->d_err, 4, cudaMemcpyDeviceToHost, br->stream));
-    CU(cudaStreamSynchronize(br->stream));
+    if ((rc = read_back())) return rc;
+    const int32_t err = br->h_small[0];
     cudaEventElapsedTime(&br->lastMs, br->ev0, br->ev1);
     if (err) {
       // leave the handle launchable: clear the flag, the barrier and the overflow pool
@@ -1082,9 +1143,12 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     }
   }
   if (out_nfired) {
-    for (int b = 0; b < br->B; b++)
-      CU(cudaMemcpyAsync(out_nfired + b, &br->trials[b].nFired, 4, cudaMemcpyDefault, br->stream));
-    CU(cudaStreamSynchronize(br->stream));
+    if (maxSteps > 0) {
+      std::memcpy(out_nfired, br->h_small + 2, sizeof(int32_t) * br->B);
+    } else {  // nothing ran: the counts of the last step before
+      if ((rc = read_back())) return rc;
+      std::memcpy(out_nfired, br->h_small + 2, sizeof(int32_t) * br->B);
+    }
   }
   return FB_OK;
 }
