@@ -10,6 +10,9 @@ steps) from rest. One bench step = 1,000 brain steps (100 ms simulated) in one p
           set from host memory, runs, and reads spike counts + the last fired list back
   cpu_baseline : the oracle port of lif_step (1 core: the reference kernel is serial) on a
           bounded sample of the same workload
+  extra legs (each switchable by FB_BENCH_<LEG>=0): adjoint, adjoint_batched, adjoint_uneven,
+          batched (256 trials), flyvis (64 eyes), embodied (the per-millisecond call pattern of
+          the simulated fly: drive rewritten, 2 steps, spike counts read back, every ms)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -275,6 +278,9 @@ def run_ours(args, rank, world):
     if os.environ.get("FB_BENCH_FLYVIS", "1") == "1":
         torch.cuda.empty_cache()
         res["flyvis"] = run_flyvis(n_eyes=int(os.environ.get("FB_FLYVIS_EYES", "64")))
+    if os.environ.get("FB_BENCH_EMBODIED", "1") == "1":
+        torch.cuda.empty_cache()
+        res["embodied"] = run_embodied(g)
     if rank == 0:
         sample = int(os.environ.get("FB_CPU_SAMPLE_STEPS", "4000"))
         v, secs, ev = cpu_baseline(g, idx, hz, SYNTH_PARAMS, sample)
@@ -282,6 +288,44 @@ def run_ours(args, rank, world):
                                    sample=f"{sample} brain steps of the same workload from rest "
                                           f"({secs:.1f} s, oracle port of lif_step, 1 thread)")
         print(json.dumps(res), flush=True)
+
+
+def run_embodied(g, ms=1000, sensory=3000, seed=3):
+    """The embodied loop's call pattern (src/sim/fly.js:151-192): every simulated millisecond the
+    host rewrites the drive of the sensory neurons (setDrive), the brain takes two steps of
+    dt 0.5 ms, and the spike counts come back for the motor readout, all through the public API
+    with pinned host buffers. Reports microseconds per simulated millisecond (wall clock, every
+    transfer and launch inside) and the real-time factor."""
+    import torch
+    from flybrain import SYNTH_PARAMS, DeviceGraph, LIFCuda
+    rng = np.random.default_rng(seed)
+    brain = LIFCuda(DeviceGraph(g), dict(SYNTH_PARAMS, dt=0.5), seed=seed)
+    b = brain._batch
+    sens = torch.from_numpy(np.sort(rng.choice(g.N, sensory, replace=False)).astype(np.int32)).pin_memory().numpy()
+    rates = torch.from_numpy(rng.uniform(0, 200, (ms, sensory))).pin_memory().numpy()
+    h_sc = torch.empty(g.N, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    outdeg = g.outdeg().astype(np.int64)
+
+    def loop(n):
+        for t in range(n):
+            b.set_drive(0, sens, rates[t % ms])
+            b.step(2)
+            b.read("spikeCount", 0, out=h_sc)
+
+    loop(50)  # warm-up
+    sc0 = h_sc.astype(np.int64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop(ms)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ev = float(((h_sc.astype(np.int64) - sc0) * outdeg).sum())
+    return dict(sim_ms=ms, brain_steps_per_ms=2, sensory_drives_per_ms=sensory,
+                us_per_sim_ms=wall / ms * 1e6, realtime_factor=(ms / 1000.0) / wall, events_per_s=ev / wall,
+                h2d_bytes_per_ms=sens.nbytes + rates[0].nbytes, d2h_bytes_per_ms=h_sc.nbytes,
+                gpu_launches_per_ms=2,
+                config=f"N={g.N:,} synthetic connectome at dt 0.5 ms; per simulated ms: drive of {sensory:,} "
+                       "sensory neurons rewritten, 2 brain steps, all spike counts read back (pinned buffers)")
 
 
 def run_flyvis(n_eyes=64, steps=200, seed=1):

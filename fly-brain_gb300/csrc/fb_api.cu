@@ -889,7 +889,11 @@ extern "C" int fb_set_background(fb_brains *br, int32_t b, double rate_hz, doubl
 
 // ---- the delay-scheduled kernel ----------------------------------------------------------------
 
-constexpr int kLagMinSteps = 16;  // AUTO: shorter launches take the grid kernel
+// AUTO: shorter launches take the grid kernel. The delay-scheduled launch carries a fixed ~110 us
+// (clearing its buffers, loading every block's state into shared memory and writing it back, the
+// ring bookkeeping) against the grid kernel's ~15 us; at the full graph they break even near 6
+// steps (grid 20-26 us per step, delay-scheduled 4-7).
+constexpr int kLagMinSteps = 8;
 
 // Whether the delay-scheduled kernel applies to this launch (why not, in *why).
 static bool lag_applies(fb_brains *br, int32_t steps, const char **why) {

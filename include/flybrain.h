@@ -137,9 +137,9 @@ int fb_brains_set_mode(fb_brains *br, int32_t mode);
 /* Kernel schedules of fb_step (both exact). No counterpart in the reference, whose lif_step is a
  * serial loop. GRID: the persistent two-phase kernel with two grid barriers per step (any batch,
  * mode and logging). LAGGED: for one brain in exact mode without presynaptic inhibition, blocks
- * synchronise only at the synaptic delay (nslots - 1 >= 3 steps; per-step logging only in
+ * synchronise only at the synaptic delay (4 <= nslots - 1 <= 32 steps; per-step logging only in
  * launches of at most 64 steps). AUTO (default) takes LAGGED where it applies and the launch has
- * at least 16 steps, GRID otherwise; forcing LAGGED where it does not apply fails with
+ * at least 8 steps, GRID otherwise; forcing LAGGED where it does not apply fails with
  * FB_EINVAL at fb_step. */
 #define FB_SCHEDULE_AUTO 0
 #define FB_SCHEDULE_GRID 1
