@@ -674,12 +674,15 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
     if (blockIdx.x == 0 && tid == 0) a.ovfTop[(s + 1) & 1] = 0;
     if (blockIdx.x == 0 && tid == 0 && a.subGrab) a.subNext[(s + 1) & 1] = 0;
     // warp sub-tiles (a warp per sub-tile, no block barrier): with many sub-tiles per warp the
-    // first 5/8 are dealt over every warp of the grid and the rest taken subGrab at a time from a
-    // counter, so warps that drew slow sub-tiles take fewer of the rest
+    // first 5/8 go to the warps as equal contiguous runs (a run stays within few brains, so their
+    // headers stay in L1) and the rest is taken subGrab at a time from a counter, so warps that
+    // drew slow sub-tiles take fewer of the rest; otherwise every warp takes every nwarps-th
     {
       const int64_t total = (int64_t)a.nTilesTotal * kSubPerTile;
       const bool dyn = a.subGrab > 0 && total >= 8 * (int64_t)nwarps;
-      int64_t gs = gwarp, end = dyn ? total * 5 / 8 : total, stride = nwarps;
+      const int64_t s0 = dyn ? total * 5 / 8 : total, run = (s0 + nwarps - 1) / nwarps;
+      int64_t gs = dyn ? (int64_t)gwarp * run : gwarp, end = dyn ? min(s0, gs + run) : total,
+              stride = dyn ? 1 : nwarps;
       for (;;) {
         if (gs >= end) {
           if (!dyn) break;
