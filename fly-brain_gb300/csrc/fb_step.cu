@@ -683,6 +683,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
       const int64_t s0 = dyn ? total * 5 / 8 : total, run = (s0 + nwarps - 1) / nwarps;
       int64_t gs = dyn ? (int64_t)gwarp * run : gwarp, end = dyn ? min(s0, gs + run) : total,
               stride = dyn ? 1 : nwarps;
+      int cb = 0, cLo = 0, cHi = 0;  // the brain of the last tile and its tile range
       for (;;) {
         if (gs >= end) {
           if (!dyn) break;
@@ -694,7 +695,12 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
           if (gs >= total) break;
         }
         const int t = (int)(gs / kSubPerTile);
-        const int b = tile_brain(t);
+        if (t < cLo || t >= cHi) {
+          cb = tile_brain(t);
+          cLo = sTile0[cb];
+          cHi = sTile0[cb + 1];
+        }
+        const int b = cb;
         if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (int)(gs % kSubPerTile), (uint32_t)(s & 1));
         gs += stride;
       }
