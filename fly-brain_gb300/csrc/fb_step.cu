@@ -591,7 +591,6 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
     }
     return lo;
   };
-  auto tile_brain = [&](int t) { return find(sTile0, t); };
   const int nDItems = sDch0[a.B];
   const int warpsPerBlock = blockDim.x >> 5;
   const uint32_t gwarp = blockIdx.x * warpsPerBlock + (tid >> 5);
@@ -673,35 +672,60 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
     // was last read in the update phase of the step before this one
     if (blockIdx.x == 0 && tid == 0) a.ovfTop[(s + 1) & 1] = 0;
     if (blockIdx.x == 0 && tid == 0 && a.subGrab) a.subNext[(s + 1) & 1] = 0;
-    // warp sub-tiles (a warp per sub-tile, no block barrier): with many sub-tiles per warp the
-    // first 5/8 go to the warps as equal contiguous runs (a run stays within few brains, so their
-    // headers stay in L1) and the rest is taken subGrab at a time from a counter, so warps that
-    // drew slow sub-tiles take fewer of the rest; otherwise every warp takes every nwarps-th
+    // warp sub-tiles (a warp per sub-tile, no block barrier) of the brains still stepping, numbered
+    // through a prefix over brains (sPre, free again after the delivery). With many sub-tiles per
+    // warp the first 5/8 go to the warps as equal contiguous runs (a run stays within few brains,
+    // whose headers stay in L1, and a warp keeps the brain of its last sub-tile) and the rest is
+    // taken subGrab at a time from a counter, so warps that drew slow sub-tiles take fewer of the
+    // rest; otherwise every warp takes every nwarps-th
     {
-      const int64_t total = (int64_t)a.nTilesTotal * kSubPerTile;
+      int64_t total;
+      if (a.B > 1) {
+        uint32_t carry = 0;
+        for (int b0 = 0; b0 < a.B; b0 += blockDim.x) {
+          const int b = b0 + tid;
+          const uint32_t n = (b < a.B && s < sSteps[b]) ? (uint32_t)(sTile0[b + 1] - sTile0[b]) * kSubPerTile : 0u;
+          uint32_t tot;
+          const uint32_t ex = block_exclusive_scan(n, &tot, scan);
+          if (b < a.B) sPre[b] = carry + ex;
+          carry += tot;
+        }
+        if (tid == 0) sPre[a.B] = carry;
+        __syncthreads();
+        total = carry;
+      } else {
+        total = s < sSteps[0] ? (int64_t)a.nTilesTotal * kSubPerTile : 0;
+      }
       const bool dyn = a.subGrab > 0 && total >= 8 * (int64_t)nwarps;
       const int64_t s0 = dyn ? total * 5 / 8 : total, run = (s0 + nwarps - 1) / nwarps;
       int64_t gs = dyn ? (int64_t)gwarp * run : gwarp, end = dyn ? min(s0, gs + run) : total,
               stride = dyn ? 1 : nwarps;
-      int cb = 0, cLo = 0, cHi = 0;  // the brain of the last tile and its tile range
+      int cb = 0;
+      int64_t cLo = 0, cHi = a.B > 1 ? 0 : total;  // the brain of the last sub-tile and its range
       for (;;) {
         if (gs >= end) {
           if (!dyn) break;
           uint32_t g0 = 0;
           if ((tid & 31) == 0) g0 = atomicAdd(a.subNext + (s & 1), (uint32_t)a.subGrab);
-          gs = total * 5 / 8 + (int64_t)__shfl_sync(0xffffffffu, g0, 0);
+          gs = s0 + (int64_t)__shfl_sync(0xffffffffu, g0, 0);
           end = min(total, gs + a.subGrab);
           stride = 1;
           if (gs >= total) break;
         }
-        const int t = (int)(gs / kSubPerTile);
-        if (t < cLo || t >= cHi) {
-          cb = tile_brain(t);
-          cLo = sTile0[cb];
-          cHi = sTile0[cb + 1];
+        if (gs < cLo || gs >= cHi) {  // largest b with sPre[b] <= gs (brains with no sub-tile skipped)
+          int lo = 0, hi = a.B;
+          while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if ((int64_t)sPre[mid] <= gs) lo = mid;
+            else hi = mid;
+          }
+          cb = lo;
+          cLo = sPre[lo];
+          cHi = sPre[lo + 1];
         }
-        const int b = cb;
-        if (s < sSteps[b]) update_tile(a, hdr(b), a.trials + b, t, (int)(gs % kSubPerTile), (uint32_t)(s & 1));
+        const int64_t local = gs - cLo;
+        update_tile(a, hdr(cb), a.trials + cb, sTile0[cb] + (int)(local / kSubPerTile), (int)(local % kSubPerTile),
+                    (uint32_t)(s & 1));
         gs += stride;
       }
     }
