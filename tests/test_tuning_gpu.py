@@ -88,6 +88,47 @@ def test_dynamic_sub_tile_dealing_keeps_the_rasters():
         assert ob.v.tobytes() == v1.tobytes()
 
 
+def test_uneven_batch_with_dynamic_dealing_keeps_the_rasters():
+    """160 brains stepped unevenly (60-200 steps) in one launch: as brains finish, the update's
+    sub-tiles are renumbered over the ones still stepping and the counter-dealt tail switches off;
+    every brain's raster and state equal those of the all-dealt launch, two brains the oracle's."""
+    from oracle import oracle as O
+    from flybrain import BrainBatch, DeviceGraph, SYNTH_PARAMS, synth_graph
+    from flybrain import _native as nat
+    g = synth_graph(12000, 93)
+    B = 160
+    rng = np.random.default_rng(6)
+    steps = rng.integers(60, 201, B).astype(np.int32)
+    drives = [(np.sort(rng.choice(g.N, 150, replace=False)).astype(np.int32), rng.uniform(80, 300, 150))
+              for _ in range(B)]
+    p = dict(SYNTH_PARAMS, wSyn=1.6)
+    out = []
+    for grab in (-1, 4):
+        batch = BrainBatch([DeviceGraph(g)] * B, p, list(range(21, 21 + B)))
+        for b, (idx, hz) in enumerate(drives):
+            batch.set_drive(b, idx, hz)
+        batch.set_tuning(1, 2, grab)
+        batch.set_schedule(nat.FB_SCHEDULE_GRID)
+        batch.record(200, 1 << 18)
+        batch.step_uneven(steps)
+        out.append([(batch.spike_log(b, int(steps[b]), 1 << 18), batch.read("v", b)) for b in range(B)])
+    for b in range(B):
+        (c0, r0), v0 = out[0][b]
+        (c1, r1), v1 = out[1][b]
+        np.testing.assert_array_equal(c0, c1)
+        np.testing.assert_array_equal(r0, r1)
+        assert v0.tobytes() == v1.tobytes()
+    for b in (int(np.argmin(steps)), int(np.argmax(steps))):
+        ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, p, seed=21 + b)
+        for i, h in zip(*drives[b]):
+            ob.setDriveOne(int(i), float(h))
+        c, r = ob.run(int(steps[b]), raster=True)
+        (c1, r1), v1 = out[1][b]
+        np.testing.assert_array_equal(c1, c)
+        np.testing.assert_array_equal(r1, r)
+        assert ob.v.tobytes() == v1.tobytes()
+
+
 def test_tuning_is_validated():
     from flybrain import _native as nat
     batch, _, _ = _batch()
