@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -883,6 +884,49 @@ extern "C" int fb_set_background(fb_brains *br, int32_t b, double rate_hz, doubl
   T.flags = (T.flags & ~kHasBg) | (T.bgEvents > 0 ? kHasBg : 0);
   CU(cudaMemcpyAsync(&br->trials[b].bgEvents, &T.bgEvents, 8, cudaMemcpyHostToDevice, br->stream));
   CU(cudaMemcpyAsync(&br->trials[b].flags, &T.flags, 4, cudaMemcpyHostToDevice, br->stream));
+  CU(cudaStreamSynchronize(br->stream));
+  return FB_OK;
+}
+
+// LIFGpu.setParams (src/lifgpu.js:349): new parameters for brain b's header constants, taking
+// effect at the next step. The ring depth round(delay/dt)+1 must not change (the ring and the
+// delay-scheduled buffers are sized by it). Constant-state flags stay only while their condition
+// holds (adapt 0 needs adaptInc 0, res 1 needs depU 0); presynaptic inhibition switches the
+// delivery to the sequential mode and back.
+extern "C" int fb_set_params(fb_brains *br, int32_t b, const fb_params *p) {
+  int rc = check_brain(br, b, "fb_set_params");
+  if (rc) return rc;
+  if (!p) return fail(FB_EINVAL, "fb_set_params: params is null");
+  if (!(p->dt > 0) || !(p->delay >= 0) || !(p->tauM > 0) || !(p->tauSyn > 0))
+    return fail(FB_EINVAL, "fb_set_params: dt, tauM, tauSyn must be > 0");
+  Trial &T = br->host[b];
+  const int ns = (int)std::max(1.0, std::floor(p->delay / p->dt + 0.5)) + 1;
+  if (ns != T.nslots)
+    return fail(FB_EINVAL, "fb_set_params: delay/dt gives a ring of %d slots; the brain was created with %d", ns, T.nslots);
+  if ((rc = flush(br))) return rc;
+  Trial nt = T;
+  fill_constants(nt, *p, T.N);
+  int32_t f = nt.flags & (kHasBg | kHasDep | kHasPreInh);
+  if ((T.flags & kAdaptZero) && nt.adaptInc == 0.f) f |= kAdaptZero;
+  if ((T.flags & kResRest) && nt.depU == 0.f) f |= kResRest;
+  f |= T.flags & (kBiasZero | kThrZero);
+  int32_t mode = T.mode;
+  if (f & kHasPreInh) mode = FB_DELIVER_SEQUENTIAL;
+  else if ((T.flags & kHasPreInh) && mode == FB_DELIVER_SEQUENTIAL) mode = FB_DELIVER_EXACT;
+  T.coba = nt.coba;
+  T.mode = mode;
+  T.flags = f;
+  T.dt = nt.dt; T.vRest = nt.vRest; T.vThresh = nt.vThresh; T.vReset = nt.vReset; T.tRef = nt.tRef;
+  T.adaptInc = nt.adaptInc; T.depU = nt.depU; T.dE = nt.dE; T.dTr = nt.dTr; T.dA = nt.dA; T.kRec = nt.kRec;
+  T.kM = nt.kM; T.dtS = nt.dtS; T.eExc = nt.eExc; T.eInh = nt.eInh; T.cE = nt.cE; T.cI = nt.cI;
+  T.bgEvents = nt.bgEvents; T.bgAmp = nt.bgAmp; T.preInh = nt.preInh;
+  br->dts[b] = p->dt;
+  // the constants, coba, mode and flags only: the device owns the header's dynamic scalars
+  Trial *D = br->trials + b;
+  const size_t c0 = offsetof(Trial, dt), c1 = offsetof(Trial, preInh) + sizeof(float);
+  CU(cudaMemcpyAsync((char *)D + c0, (const char *)&T + c0, c1 - c0, cudaMemcpyHostToDevice, br->stream));
+  CU(cudaMemcpyAsync(&D->coba, &T.coba, 8, cudaMemcpyHostToDevice, br->stream));  // coba, mode
+  CU(cudaMemcpyAsync(&D->flags, &T.flags, 4, cudaMemcpyHostToDevice, br->stream));
   CU(cudaStreamSynchronize(br->stream));
   return FB_OK;
 }

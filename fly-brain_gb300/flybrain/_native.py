@@ -113,6 +113,7 @@ SIGNATURES = {
     "fb_pulse": (C.c_int, [P, I32, P, P, I32]),
     "fb_reset": (C.c_int, [P, I32]),
     "fb_set_background": (C.c_int, [P, I32, D, D]),
+    "fb_set_params": (C.c_int, [P, I32, C.POINTER(FbParams)]),
     "fb_read": (C.c_int, [P, I32, I32, P]),
     "fb_write": (C.c_int, [P, I32, I32, P]),
     "fb_scalars": (C.c_int, [P, I32, PI32, PU32, PI32, PI32, PI32, PI64]),

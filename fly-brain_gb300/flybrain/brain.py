@@ -247,6 +247,13 @@ class BrainBatch:
     def set_background(self, b, rate_hz, amp_mv):
         nat.check(self.L.fb_set_background(self.h, b, float(rate_hz), float(amp_mv)))
 
+    def set_params(self, b, params: dict):
+        """New header constants for brain b from the next step on (fb_set_params)."""
+        merged = dict(DEFAULTS, **params)
+        q = make_params(merged)
+        nat.check(self.L.fb_set_params(self.h, b, C.byref(q)))
+        self.p[b] = merged
+
     def read(self, field: str, b: int = 0, out: np.ndarray | None = None) -> np.ndarray:
         """A state field of brain b; out: a contiguous destination of N entries (e.g. pinned)."""
         dt = np.uint32 if field == "spikeCount" else np.float32
@@ -311,6 +318,20 @@ class LIFCuda:
 
     def setThr(self, i, mv):
         self._batch.set_thr(0, [int(i)], [mv])
+
+    # LIFGpu extras (src/lifgpu.js:348-362)
+    def setParams(self, q: dict):
+        """Merged into the parameters; the header constants follow from the next step (the ring
+        depth round(delay/dt)+1 must stay)."""
+        merged = dict(self.p, **q)
+        self._batch.set_params(0, merged)
+        self.p = merged
+
+    def flush(self):
+        """Nothing to submit: queued writes apply before the next step."""
+
+    def destroy(self):
+        self._batch = None
 
     def addG(self, i, e, ii=0.0):
         self._batch.add_g(0, [int(i)], [e], [ii or 0.0])

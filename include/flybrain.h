@@ -209,6 +209,10 @@ int fb_reset(fb_brains *br, int32_t b);
 
 /* Background synaptic events (setBackground, src/lifwasm.js:69). */
 int fb_set_background(fb_brains *br, int32_t b, double rate_hz, double amp_mv);
+/* LIFGpu.setParams (src/lifgpu.js:349): brain b's header constants recomputed from *params for
+ * the next step (as at creation, src/lifwasm.js:55-68). The ring depth round(delay/dt)+1 must be
+ * unchanged (FB_EINVAL otherwise); the state is kept. */
+int fb_set_params(fb_brains *br, int32_t b, const fb_params *params);
 
 /* Copies field (FB_FIELD_*) of brain b, N elements of 4 bytes, into dst / from src. */
 int fb_read(fb_brains *br, int32_t field, int32_t b, void *dst);

@@ -261,3 +261,43 @@ def test_large_batches_created_in_either_order():
     for batch in (big, small):
         assert batch.read("v", 6).tobytes() == lone.read("v", 0).tobytes()
         assert batch.read("spikeCount", 6).tobytes() == lone.read("spikeCount", 0).tobytes()
+
+
+def test_set_params_between_steps_matches_the_oracle():
+    """LIFGpu.setParams on the device brain (fb_set_params): the membrane and synaptic constants,
+    adaptation, depression, background and COBA change between two runs; the oracle's header
+    gets the same constants (LIFWasm._writeHeader); rasters and state agree bit for bit."""
+    from oracle import oracle as O
+    from flybrain import LIFCuda, SYNTH_PARAMS, synth_graph
+    g = synth_graph(3000, 17)
+    p = dict(SYNTH_PARAMS, wSyn=1.6)
+    brain = LIFCuda(g, p, seed=4)
+    ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, p, seed=4)
+    rng = np.random.default_rng(17)
+    for i in rng.choice(g.N, 60, replace=False):
+        brain.setDriveOne(int(i), 220.0)
+        ob.setDriveOne(int(i), 220.0)
+    brain.setBias([1, 2, 3], 2.0)
+    ob.setBias([1, 2, 3], 2.0)
+    brain._batch.record(300, 1 << 20)
+    c0a, r0a = ob.run(150, raster=True)
+    brain.run(150)
+    q = dict(tauM=15.0, vThresh=-46.0, tauSyn=4.0, adaptInc=0.5, depU=0.1, bgRate=20.0, bgAmp=0.8, coba=True)
+    brain.setParams(q)
+    ob.p.update(q)
+    h = ob._pull()
+    for k, v in enumerate(O.header_constants(ob.p)):
+        h.c[k] = float(v)
+    h.coba = 1
+    h.bgEvents = float(np.float32(g.N * ob.p["bgRate"] * ob.p["dt"] / 1000))
+    h.bgAmp = float(np.float32(ob.p["bgAmp"]))
+    ob._push()
+    c0b, r0b = ob.run(150, raster=True)
+    brain.run(150)
+    c1, r1 = brain._batch.spike_log(0, 300, 1 << 20)
+    np.testing.assert_array_equal(c1, np.concatenate([c0a, c0b]))
+    np.testing.assert_array_equal(r1, np.concatenate([r0a, r0b]))
+    for k in ("v", "gE", "gI", "refr", "trace", "adapt", "res", "spikeCount"):
+        assert getattr(brain, k).tobytes() == np.asarray(getattr(ob, k)).tobytes(), k
+    with pytest.raises(Exception, match="ring"):
+        brain.setParams(dict(delay=3.0))
