@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-REF_DATA = "/root/reference/public/data"
+from refpaths import REF_DATA
 
 
 def _tables():

@@ -13,7 +13,7 @@ import pytest
 
 from flyg_encode import encode_flyg, encode_flyn
 
-REF_DATA = "/root/reference/public/data"
+from refpaths import REF_DATA
 HAVE_REF = os.path.exists(os.path.join(REF_DATA, "graph.flyg"))
 
 

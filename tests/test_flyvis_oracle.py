@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
+from refpaths import REF_LIF_C
 
 
 def _golden():
@@ -29,7 +30,7 @@ def test_oracle_matches_the_reference_golden_run():
     assert np.isfinite(v).all() and (v < 0).any() and (v > 0).any()
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/src/wasm/lif.c"), reason="reference tree absent")
+@pytest.mark.skipif(not os.path.exists(REF_LIF_C), reason="reference tree absent")
 def test_oracle_matches_the_reference_fv_step():
     from oracle import oracle as O
     from flybrain.flyvis import synth_flyvis
