@@ -319,6 +319,11 @@ class LIFCuda:
     def setThr(self, i, mv):
         self._batch.set_thr(0, [int(i)], [mv])
 
+    def setThrList(self, ix, mv):
+        """setThr over a list in one host write (mv: one value or one per index), as a loop of
+        setThr calls in list order would leave it."""
+        self._batch.set_thr(0, np.asarray(ix, np.int32), mv)
+
     # LIFGpu extras (src/lifgpu.js:348-362)
     def setParams(self, q: dict):
         """Merged into the parameters; the header constants follow from the next step (the ring

@@ -22,8 +22,8 @@ Values are computed as the reference computes them: float64 arithmetic, stored t
 reference stores to a Float32Array (inScale once; outScale after every multiply). Math.pow, exp,
 log and cos come from the host's C library here and from the JavaScript engine there; both are
 within an ulp in float64, so a stored float32 can differ from the reference's in rare ties.
-The neuromodulation module itself (src/sim/neuromod.js, the octopamine threshold field) is outside
-the brain step and is not built here.
+The neuromodulation controller that runs beside a calibrated brain (src/sim/neuromod.js, the
+octopamine threshold field) is flybrain.neuromod.
 """
 from __future__ import annotations
 
@@ -219,7 +219,7 @@ def attach_brain(dg, p: dict, c: dict, opts: dict | None = None, seed: int = 1):
     brain = LIFCuda(dg, p, seed=seed)
     (kc, kv), (lam, lv) = class_physiology(c, opts)
     if kc.shape[0]:
-        brain._batch.set_thr(0, kc, np.full(kc.shape[0], kv, np.float32))
+        brain.setThrList(kc, kv)
     if lam.shape[0]:
         brain.setBias(lam, lv)
     return brain

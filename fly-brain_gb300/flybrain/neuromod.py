@@ -217,8 +217,8 @@ class Neuromod:
 
     def _set_thr(self, idx, vals):
         B = self.brain
-        if hasattr(B, "_batch"):  # one list write on the GPU brain (setThr per element)
-            B._batch.set_thr(0, np.asarray(idx, np.int32), np.asarray(vals, np.float64))
+        if hasattr(B, "setThrList"):  # one list write (the same as setThr per element, in order)
+            B.setThrList(idx, np.asarray(vals, np.float64))
         else:
             for i, v in zip(idx.tolist(), vals.tolist()):
                 B.setThr(int(i), v)
