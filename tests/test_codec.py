@@ -152,3 +152,30 @@ def test_data_directory_with_compressed_files_only(tmp_path):
     for k in ("indptr", "indices", "counts", "bodyIds", "cls", "nt", "sc", "side", "indeg", "outdeg"):
         np.testing.assert_array_equal(c[k], ref[k])
     np.testing.assert_array_equal(c["soma"], ref["soma"])
+
+
+def test_loader_reads_compressed_tables_without_the_flat_ones(tmp_path):
+    """A synthetic data directory written both ways: the loader's result from graph.flyg and
+    neurons.flyn alone equals its result from the flat tables."""
+    from flybrain.connectome import load_connectome, load_neurons, write_connectome
+    from flybrain.synth import synth_graph
+    g = synth_graph(1500, 8)
+    nt = np.random.default_rng(8).integers(0, 8, g.N).astype(np.uint8)
+    flat, comp = tmp_path / "flat", tmp_path / "comp"
+    write_connectome(str(flat), g.N, g.indptr, g.indices, g.counts, nt, min_weight=3)
+    ref = load_connectome(str(flat))
+    comp.mkdir()
+    shutil.copy(flat / "meta.json", comp / "meta.json")
+    w = np.minimum(g.counts, 65535).astype(np.uint16)
+    (comp / "graph.flyg").write_bytes(encode_flyg(g.N, g.indptr, g.indices, w, 3,
+                                                  np.random.default_rng(1).permutation(g.N)))
+    t = load_neurons(str(flat / "neurons.bin"), g.N)
+    t["soma"][::7] = np.nan
+    (comp / "neurons.flyn").write_bytes(encode_flyn(t["bodyIds"], t["soma"], t["cls"], t["nt"], t["sc"], t["side"]))
+    c = load_connectome(str(comp))
+    for k in ("N", "E", "min_weight"):
+        assert c[k] == ref[k], k
+    for k in ("indptr", "indices", "counts", "bodyIds", "cls", "nt", "sc", "side", "indeg", "outdeg"):
+        np.testing.assert_array_equal(c[k], ref[k])
+    np.testing.assert_array_equal(c["soma"], t["soma"])
+    assert c["size"] is None and c["ntsign"] is None
