@@ -1,12 +1,15 @@
 // fb_lif_step_noalloc: the brain step for callers that cannot allocate device memory.
 //
-// Some callers may not call cudaMalloc: code running inside a CUDA graph capture, a host framework
-// that owns every byte of device memory through its own pool, or a real-time loop where the
-// implicit device synchronisation of cudaMalloc/cudaFree is not allowed. This entry point takes a
-// view shaped like the reference's Brain header (every array a caller-owned device pointer) and
-// allocates nothing: the step's scratch (delivery buckets, ring bookkeeping, spike staging,
-// barrier words, xorshift jump tables) lives in one file-scope __device__ array of a fixed size,
-// which every GPU that loads this library holds until the process exits.
+// Some callers of the brain step may not call cudaMalloc or cudaFree: a host application that
+// hands every byte of device memory out of its own pool (a physics or rendering engine with a
+// fixed device budget, where an allocation behind its back breaks the budget), or a real-time
+// control loop such as the embodied fly, which steps the brain twice per simulated millisecond
+// and cannot take the implicit device-wide synchronisation that cudaMalloc/cudaFree may perform.
+// This entry point takes a view shaped like the reference's Brain header (every array a
+// caller-owned device pointer) and allocates nothing: the step's scratch (delivery buckets, ring
+// bookkeeping, spike staging, overflow records, barrier words, xorshift jump tables) lives in one
+// file-scope __device__ array of a fixed 64 MiB, which every GPU that loads this library holds
+// until the process exits.
 //
 // The array is shared by every call on a device and keeps the last call's contents, so each call
 // first clears what must start at zero and rebuilds the ring's delivery bookkeeping from the
@@ -35,11 +38,12 @@ int set_error(int code, const char *msg);
 
 using namespace fb;
 
-// The static scratch: 32 MiB, enough for a brain of N = 20,000 neurons and 1.2M edges with a
+// The static scratch: 64 MiB, enough for a brain of N = 20,000 neurons and 1.2M edges with a
 // 19-slot ring (the dt = 0.1 ms, 1.8 ms delay model); the bound a call must fit is computed by
-// noalloc_layout below.
-static constexpr size_t kNoAllocBytes = 32u << 20;
-static constexpr uint32_t kNoAllocOvf = 1u << 15;  // overflow records per step parity
+// noalloc_layout below. Its overflow records (contributions beyond a target's in-place bucket)
+// are sized by E per step parity: a presynaptic neuron arrives at most once per step, so one step
+// never delivers more than E contributions, and no burst can overflow them.
+static constexpr size_t kNoAllocBytes = 64u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
@@ -66,8 +70,8 @@ Layout noalloc_layout(int64_t N, int64_t E, int64_t ns) {
   L.dbg = take(16);
   L.ovfTop = take(8);
   L.steps = take(4);
-  L.ovf0 = take(sizeof(OvfRec) * kNoAllocOvf);
-  L.ovf1 = take(sizeof(OvfRec) * kNoAllocOvf);
+  L.ovf0 = take(sizeof(OvfRec) * (size_t)(E + 1));
+  L.ovf1 = take(sizeof(OvfRec) * (size_t)(E + 1));
   L.ringOff = take((size_t)ns * (N + 1) * 4);
   L.ringRow = take((size_t)ns * N * 4);
   L.chunkK = take((size_t)ns * chunkCap * 16);
@@ -88,6 +92,36 @@ Layout noalloc_layout(int64_t N, int64_t E, int64_t ns) {
   L.liveTag = take((size_t)maxDch * 8);
   L.total = o;
   return L;
+}
+
+// The caller's arrays are not checked by anyone else (fb_graph_create checks its CSR on the host;
+// here the CSR, the driven list and the ring lists are device memory the caller filled). Every
+// index the step dereferences is checked once per call before anything is written: indptr
+// starts at 0, never decreases and ends at E; every target is in [0, N); every driven entry and
+// every ring entry (of its slot's count, itself in [0, N]) is in [0, N). A violation records
+// FB_EINVAL; nothing else is written.
+__global__ void validate_view_kernel(const uint32_t *indptr, const uint32_t *indices, const int32_t *driven,
+                                     const int32_t *ring, const int32_t *ringCount, int32_t N, int64_t E,
+                                     int32_t nDriven, int32_t nslots, int32_t *err) {
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+  bool bad = false;
+  if (t0 == 0) bad = indptr[0] != 0u || (int64_t)indptr[N] != E;
+  for (int64_t i = t0; i < N; i += nt) bad |= indptr[i + 1] < indptr[i];
+  for (int64_t j = t0; j < E; j += nt) bad |= indices[j] >= (uint32_t)N;
+  for (int64_t k = t0; k < nDriven; k += nt) bad |= driven[k] < 0 || driven[k] >= N;
+  for (int32_t sl = 0; sl < nslots; sl++) {
+    const int32_t na = ringCount[sl];
+    if (na < 0 || na > N) {
+      bad = true;
+      continue;
+    }
+    for (int64_t k = t0; k < na; k += nt) {
+      const int32_t x = ring[(int64_t)sl * N + k];
+      bad |= x < 0 || x >= N;
+    }
+  }
+  if (bad) atomicCAS(err, 0, FB_EINVAL);
 }
 
 struct DeviceSetup {
@@ -131,6 +165,9 @@ int setup_device(int dev, DeviceSetup **out) {
     std::vector<uint32_t> tab;
     host_jump_tables(tab);
     NA_CU(cudaMemcpy(ptr, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice));
+    // a copy from pageable memory may return before the data has reached the device; a step on a
+    // non-blocking stream would not be ordered after it
+    NA_CU(cudaDeviceSynchronize());
     d.base = (unsigned char *)ptr;
     d.grid = p.multiProcessorCount * per;
     d.ready = true;
@@ -221,6 +258,16 @@ extern "C" int fb_lif_step_noalloc(fb_brain_view *v, int32_t nsteps, void *strea
   NA_CU(cudaMemsetAsync(B + L.liveTag, 0, (size_t)T.maxDch * 8, st));
   NA_CU(cudaMemcpyAsync(Td, &T, sizeof T, cudaMemcpyHostToDevice, st));
   NA_CU(cudaMemcpyAsync(B + L.steps, &nsteps, 4, cudaMemcpyHostToDevice, st));
+  // the caller's indices, checked before anything of the brain is written
+  validate_view_kernel<<<d->grid, 256, 0, st>>>(v->indptr, v->indices, v->driven, v->ring, v->ringCount, v->N,
+                                               v->E, v->nDriven, v->nslots, errd);
+  NA_CU(cudaGetLastError());
+  int32_t verr = 0;
+  NA_CU(cudaMemcpyAsync(&verr, errd, 4, cudaMemcpyDeviceToHost, st));
+  NA_CU(cudaStreamSynchronize(st));
+  if (verr)
+    return fail_na(FB_EINVAL, "fb_lif_step_noalloc: the view's indptr, indices, driven list or ring lists hold an "
+                   "index outside [0, N) (or indptr does not run from 0 to E); nothing was changed");
   NA_CU(launch_rebuild_slots(Td, v->nslots, errd, st));
 
   StepArgs a;
@@ -239,7 +286,7 @@ extern "C" int fb_lif_step_noalloc(fb_brain_view *v, int32_t nsteps, void *strea
   a.ovf[0] = (OvfRec *)(B + L.ovf0);
   a.ovf[1] = (OvfRec *)(B + L.ovf1);
   a.ovfTop = (uint32_t *)(B + L.ovfTop);
-  a.ovfCap = kNoAllocOvf;
+  a.ovfCap = (uint32_t)(v->E + 1);
   a.log = 0;
   a.timeoutNs = 5000000000LL;
   a.dbg = (uint32_t *)(B + L.dbg);
@@ -252,9 +299,12 @@ extern "C" int fb_lif_step_noalloc(fb_brain_view *v, int32_t nsteps, void *strea
   NA_CU(cudaMemcpyAsync(&err, errd, 4, cudaMemcpyDeviceToHost, st));
   NA_CU(cudaStreamSynchronize(st));
   if (err)
-    return fail_na(err, err == FB_ETIMEOUT ? "fb_lif_step_noalloc: a device-side wait timed out"
-                   : err == FB_EOVERFLOW ? "fb_lif_step_noalloc: delivery overflow (more contributions to one target in one step than the scratch holds)"
-                                         : "fb_lif_step_noalloc: a ring list holds an index outside [0, N)");
+    return fail_na(err, err == FB_ETIMEOUT ? "fb_lif_step_noalloc: a device-side wait timed out; the brain's arrays "
+                                             "may be partly advanced and the view was not updated: rebuild the brain"
+                   : err == FB_EOVERFLOW ? "fb_lif_step_noalloc: delivery overflow; the brain's arrays may be partly "
+                                           "advanced and the view was not updated: rebuild the brain"
+                                         : "fb_lif_step_noalloc: device error %d; the brain's arrays may be partly "
+                                           "advanced and the view was not updated: rebuild the brain", err);
   v->head = out.head;
   v->rng = out.rngP[nsteps & 1];
   v->bgAcc = out.bgAccP[nsteps & 1];

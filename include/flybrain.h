@@ -454,19 +454,25 @@ typedef struct fb_brain_view {
 
 /* nsteps brain steps on caller-owned memory, allocating nothing -- no counterpart in the
  * reference (whose lif_step allocates nothing either, but also runs no GPU kernels). For callers
- * that may not call cudaMalloc/cudaFree: code inside a CUDA graph capture, a host framework that
- * owns all device memory through its own pool, or a real-time loop where the implicit device
- * synchronisation of an allocation is not allowed. The step's scratch is a file-scope __device__
- * array of 32 MiB that every GPU loading this library holds until exit; a brain must fit it
- * (about N = 20,000 neurons with 1.2M edges and a 19-slot ring), larger ones are rejected with
- * FB_EINVAL (use fb_brains_create). Results are those of fb_step, bit for bit. On return the
- * view's head, rng, bgAcc, nFired and lastSlot hold the state after the last step, and
- * ring[lastSlot * N ...] its fired list. stream: a cudaStream_t (NULL: the legacy default stream);
- * the call synchronises it before returning. The first call on a device sets the device up (it
- * looks up the scratch array's device address and writes the xorshift jump tables into it), so
- * make that first call before any stream capture. Every call shares the one array and keeps the
- * last call's contents, so each call clears what must start at zero first; calls that overlap on
- * the GPU race on the array: serialise them. */
+ * that may not call cudaMalloc/cudaFree: a host application that hands out every byte of device
+ * memory from its own pool (an engine with a fixed device budget), or a real-time control loop
+ * (the embodied fly steps its brain twice per simulated millisecond) that cannot take the
+ * device-wide synchronisation an allocation or a free may imply. The step's scratch is a
+ * file-scope __device__ array of 64 MiB that every GPU loading this library holds until exit; a
+ * brain must fit it (about N = 20,000 neurons with 1.2M edges and a 19-slot ring), larger ones are
+ * rejected with FB_EINVAL (use fb_brains_create). Results are those of fb_step, bit for bit.
+ * Before anything is written the call checks, on the device, every index the step will follow
+ * (indptr from 0 to E and non-decreasing, targets, the driven list, the ring lists and counts);
+ * a violation returns FB_EINVAL with the brain untouched. On success the view's head, rng, bgAcc,
+ * nFired and lastSlot hold the state after the last step, and ring[lastSlot * N ...] its fired
+ * list. On FB_ETIMEOUT or FB_EOVERFLOW the device arrays may be partly advanced while the view's
+ * scalars are those from before the call: the brain is no longer consistent and must be rebuilt.
+ * stream: a cudaStream_t (NULL: the legacy default stream); the call synchronises it (once after
+ * the index check, once at the end) before returning. The first call on a device sets the device
+ * up: it looks up the scratch array's device address and writes the xorshift jump tables into it,
+ * then synchronises the device. Every call shares the one array and keeps the last call's
+ * contents, so each call clears what must start at zero first; calls that overlap on the GPU race
+ * on the array: serialise them. */
 int fb_lif_step_noalloc(fb_brain_view *brain, int32_t nsteps, void *stream);
 
 /* ---- the reference's compressed data files (host decoders, no device work) -------------------

@@ -45,11 +45,19 @@ class OHdr(C.Structure):
 
 
 def build(ref: bool | None = None) -> None:
-    """Compile the oracle libraries (and the reference build when the reference tree exists)."""
-    targets = ["port"]
-    if ref or (ref is None and os.path.exists("/root/reference/src/wasm/lif.c")):
-        targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    """Compile the oracle libraries; with ref None the Makefile also builds the reference kernel
+    when it finds the reference tree (FLYBRAIN_REFERENCE, else the Makefile's REF)."""
+    cmd = ["make", "-s", "-C", HERE]
+    root = os.environ.get("FLYBRAIN_REFERENCE")
+    if root:
+        cmd.append(f"REF={root}")
+    targets = ["all"] if ref is None else (["port", "ref"] if ref else ["port"])
+    subprocess.run(cmd + targets, check=True)
+
+
+def have_reference_build() -> bool:
+    """Whether the reference kernel was compiled here (the live-reference tests need it)."""
+    return os.path.exists(REF_LIB)
 
 
 _libs: dict[str, C.CDLL] = {}

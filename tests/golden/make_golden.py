@@ -26,7 +26,9 @@ from oracle import oracle as O  # noqa: E402
 from flybrain.synth import SYNTH_PARAMS, synth_graph  # noqa: E402
 from scenarios import final_state, oracle_runner, run_scenario, save_case  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FLYBRAIN_REFERENCE", "")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: make_golden.py <reference tree> (or set FLYBRAIN_REFERENCE)")
 EXC_SIGN = [0, 1, -1, -1, 1, 1, 1, -1]  # src/lif.js:5
 
 

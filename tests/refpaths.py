@@ -1,8 +1,7 @@
-"""Where the tests find the reference tree when it is present (it is read only: golden runs of its
-kernel, its data files). FLYBRAIN_REFERENCE overrides the location; tests that need it skip when
-it is absent."""
+"""Where the tests find the reference tree when it is present (it is read only: its data files).
+The location comes from FLYBRAIN_REFERENCE alone; tests that need the tree skip when it is unset.
+Tests of the reference kernel itself use its native build (oracle/_ref), made by oracle/Makefile."""
 import os
 
-REFERENCE = os.environ.get("FLYBRAIN_REFERENCE", "/root/reference")
-REF_DATA = os.path.join(REFERENCE, "public", "data")
-REF_LIF_C = os.path.join(REFERENCE, "src", "wasm", "lif.c")
+REFERENCE = os.environ.get("FLYBRAIN_REFERENCE", "")
+REF_DATA = os.path.join(REFERENCE, "public", "data") if REFERENCE else ""

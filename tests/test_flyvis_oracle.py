@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from refpaths import REF_LIF_C
+from oracle import oracle as O
 
 
 def _golden():
@@ -30,7 +30,7 @@ def test_oracle_matches_the_reference_golden_run():
     assert np.isfinite(v).all() and (v < 0).any() and (v > 0).any()
 
 
-@pytest.mark.skipif(not os.path.exists(REF_LIF_C), reason="reference tree absent")
+@pytest.mark.skipif(not O.have_reference_build(), reason="reference kernel not built here")
 def test_oracle_matches_the_reference_fv_step():
     from oracle import oracle as O
     from flybrain.flyvis import synth_flyvis

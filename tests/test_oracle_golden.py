@@ -8,7 +8,6 @@ import pytest
 from conftest import GOLDEN
 from oracle import oracle as O
 from scenarios import final_state, load_case, oracle_runner, run_scenario
-from refpaths import REF_LIF_C
 
 CASES = sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz"))
 
@@ -38,7 +37,7 @@ def test_golden_cases_present():
     assert sum(1 for _ in CASES) >= 4
 
 
-@pytest.mark.skipif(not os.path.exists(REF_LIF_C), reason="reference tree absent")
+@pytest.mark.skipif(not O.have_reference_build(), reason="reference kernel not built here")
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_port_matches_reference_live(seed):
     """Random parameters and drives on random synthetic graphs: port == reference lif.c."""
