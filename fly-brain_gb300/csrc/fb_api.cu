@@ -448,6 +448,8 @@ struct fb_brains {
   int blocksPerSm = 0, maxBlocksPerSm = 0, sms = 0;  // the persistent grid: sms x blocksPerSm
   int32_t itemChunks = 1;
   int32_t subGrab = 4;
+  int64_t timeoutNs = 5000000000LL;  // bound of every device-side wait (fb_tuning.timeout_us)
+  int32_t tripStep = -1;             // test hook (fb_debug_trip_wait): armed for one launch
   int logging = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float lastMs = 0.f;
@@ -672,9 +674,10 @@ extern "C" int fb_brains_set_schedule(fb_brains *br, int32_t schedule) {
 extern "C" int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t) {
   if (!br || !t) return fail(FB_EINVAL, "fb_brains_set_tuning: null argument");
   if (t->blocks_per_sm < 0 || t->blocks_per_sm > br->maxBlocksPerSm || t->item_chunks < 0 || t->item_chunks > 64 ||
-      t->sub_grab < -1 || t->sub_grab > 256)
-    return fail(FB_EINVAL, "fb_brains_set_tuning: blocks_per_sm %d (1..%d), item_chunks %d (1..64), sub_grab %d (-1, 1..256)",
-                t->blocks_per_sm, br->maxBlocksPerSm, t->item_chunks, t->sub_grab);
+      t->sub_grab < -1 || t->sub_grab > 256 || t->timeout_us < 0)
+    return fail(FB_EINVAL, "fb_brains_set_tuning: blocks_per_sm %d (1..%d), item_chunks %d (1..64), sub_grab %d (-1, 1..256), "
+                "timeout_us %d (>= 1)", t->blocks_per_sm, br->maxBlocksPerSm, t->item_chunks, t->sub_grab, t->timeout_us);
+  if (t->timeout_us) br->timeoutNs = (int64_t)t->timeout_us * 1000;
   if (t->blocks_per_sm) {
     br->blocksPerSm = t->blocks_per_sm;
     br->grid = br->sms * br->blocksPerSm;
@@ -689,9 +692,15 @@ extern "C" int fb_brains_tuning(fb_brains *br, fb_tuning *t) {
   t->blocks_per_sm = br->blocksPerSm;
   t->item_chunks = br->itemChunks;
   t->sub_grab = br->subGrab ? br->subGrab : -1;
-  t->pad = 0;
+  t->timeout_us = (int32_t)std::min<int64_t>(br->timeoutNs / 1000, 0x7fffffff);
   t->max_blocks_per_sm = br->maxBlocksPerSm;
   t->sms = br->sms;
+  return FB_OK;
+}
+
+extern "C" int fb_debug_trip_wait(fb_brains *br, int32_t step) {
+  if (!br || step < -1) return fail(FB_EINVAL, "fb_debug_trip_wait: bad arguments");
+  br->tripStep = step;
   return FB_OK;
 }
 
@@ -1094,7 +1103,9 @@ static int run_lagged(fb_brains *br, int32_t steps) {
   a.jumpHex = R.jumpHex;
   a.edgeRec = R.edgeRec;
   a.err = br->d_err;
-  a.timeoutNs = 5000000000LL;
+  a.timeoutNs = br->timeoutNs;
+  a.tripStep = br->tripStep;
+  br->tripStep = -1;  // one launch only
   CU(launch_lagged(a, R.grid, R.smem, br->stream));
   CU(launch_rebuild_slots(br->trials, T.nslots, br->d_err, br->stream));
   CU(cudaEventRecord(br->ev1, br->stream));
@@ -1166,7 +1177,7 @@ static int run_steps(fb_brains *br, int32_t maxSteps, int32_t *out_nfired) {
     a.itemChunks = br->itemChunks;
     a.subGrab = br->subGrab;
     a.subNext = br->d_ovfTop + 2;
-    a.timeoutNs = 5000000000LL;
+    a.timeoutNs = br->timeoutNs;
     a.dbg = br->d_dbg;
     CU(cudaEventRecord(br->ev0, br->stream));
     CU(launch_step(a, br->grid, br->smem, br->stream));
@@ -1292,6 +1303,19 @@ extern "C" int fb_fired(fb_brains *br, int32_t b, int32_t *dst, int32_t cap, int
     const Trial &T = br->host[b];
     CU(cudaMemcpy(dst, T.ring + (int64_t)nf_slot[1] * T.N, sizeof(int32_t) * m, cudaMemcpyDefault));
   }
+  return FB_OK;
+}
+
+extern "C" int fb_ring_read(fb_brains *br, int32_t b, int32_t *ring, int32_t *counts, int32_t *head) {
+  int rc = check_brain(br, b, "fb_ring_read");
+  if (rc) return rc;
+  rc = flush(br);
+  if (rc) return rc;
+  CU(cudaStreamSynchronize(br->stream));
+  const Trial &T = br->host[b];
+  if (ring) CU(cudaMemcpy(ring, T.ring, sizeof(int32_t) * (size_t)T.nslots * T.N, cudaMemcpyDefault));
+  if (counts) CU(cudaMemcpy(counts, T.ringCount, sizeof(int32_t) * T.nslots, cudaMemcpyDefault));
+  if (head) CU(cudaMemcpy(head, &br->trials[b].head, sizeof(int32_t), cudaMemcpyDeviceToHost));
   return FB_OK;
 }
 

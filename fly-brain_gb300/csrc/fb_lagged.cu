@@ -609,6 +609,9 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         }
       }
       if (ok && !drivenBlock && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s + 1));
+      // test hook: a wait that nothing satisfies (the driven block's progress word never reaches
+      // 2^32 - 1), so it runs out after timeoutNs and the launch ends with FB_ETIMEOUT
+      if (ok && s == a.tripStep && blockIdx.x == 1) ok = wait_geq(a, a.dbDone, 0xffffffffu);
       sh.stopP[s & 1] = ok ? 0 : 1;
     }
     __syncthreads();

@@ -78,6 +78,8 @@ struct LagArgs {
   uint32_t *barCount;
   int32_t *err;
   int64_t timeoutNs;
+  int32_t tripStep;  // test hook: tile block 1 waits at this step on a flag nothing sets (-1: off)
+  int32_t pad;
 };
 
 // Jump tables of the driven block: M^(v 16^i) (i < 3, v = 1..15), M^4096, and M^l (l < 32, by lane).

@@ -75,7 +75,7 @@ class FbDiffGrads(C.Structure):
 
 
 class FbTuning(C.Structure):
-    _fields_ = [(k, C.c_int32) for k in ("blocks_per_sm", "item_chunks", "max_blocks_per_sm", "sms", "sub_grab", "pad")]
+    _fields_ = [(k, C.c_int32) for k in ("blocks_per_sm", "item_chunks", "max_blocks_per_sm", "sms", "sub_grab", "timeout_us")]
 
 
 class FbDiffTuning(C.Structure):
@@ -106,6 +106,7 @@ SIGNATURES = {
     "fb_record": (C.c_int, [P, I32, I64]),
     "fb_spike_log": (C.c_int, [P, I32, P, I32, P, I64, PI64, PI64]),
     "fb_fired": (C.c_int, [P, I32, P, I32, PI32]),
+    "fb_ring_read": (C.c_int, [P, I32, P, P, P]),
     "fb_set_drive": (C.c_int, [P, I32, P, P, I32]),
     "fb_set_bias": (C.c_int, [P, I32, P, P, I32]),
     "fb_set_thr": (C.c_int, [P, I32, P, P, I32]),
@@ -134,6 +135,7 @@ SIGNATURES = {
     "fb_last_schedule": (C.c_int, [P, C.POINTER(C.c_int32)]),
     "fb_brains_set_tuning": (C.c_int, [P, C.POINTER(FbTuning)]),
     "fb_brains_tuning": (C.c_int, [P, C.POINTER(FbTuning)]),
+    "fb_debug_trip_wait": (C.c_int, [P, I32]),
     "fb_diff_batch_set_tuning": (C.c_int, [P, C.POINTER(FbDiffTuning)]),
     "fb_diff_batch_create": (C.c_int, [C.POINTER(FbDiffNet), I32, I64, C.POINTER(P)]),
     "fb_diff_batch_destroy": (C.c_int, [P]),

@@ -155,15 +155,22 @@ class BrainBatch:
         nat.check(self.L.fb_last_schedule(self.h, C.byref(x)))
         return x.value
 
-    def set_tuning(self, blocks_per_sm: int = 0, item_chunks: int = 0, sub_grab: int = 0):
-        """Launch shape of the grid schedule (fb_brains_set_tuning); 0 keeps a knob."""
-        t = nat.FbTuning(int(blocks_per_sm), int(item_chunks), 0, 0, int(sub_grab), 0)
+    def set_tuning(self, blocks_per_sm: int = 0, item_chunks: int = 0, sub_grab: int = 0,
+                   timeout_us: int = 0):
+        """Launch shape of the grid schedule and the bound of device-side waits
+        (fb_brains_set_tuning); 0 keeps a knob."""
+        t = nat.FbTuning(int(blocks_per_sm), int(item_chunks), 0, 0, int(sub_grab), int(timeout_us))
         nat.check(self.L.fb_brains_set_tuning(self.h, C.byref(t)))
 
     def tuning(self) -> dict:
         t = nat.FbTuning()
         nat.check(self.L.fb_brains_tuning(self.h, C.byref(t)))
-        return {k: getattr(t, k) for k, _ in nat.FbTuning._fields_ if k != "pad"}
+        return {k: getattr(t, k) for k, _ in nat.FbTuning._fields_}
+
+    def trip_wait(self, step: int):
+        """Test hook (fb_debug_trip_wait): the next delay-scheduled launch waits, at `step`, on a
+        flag nothing sets, and ends with FB_ETIMEOUT after the timeout; -1 disarms."""
+        nat.check(self.L.fb_debug_trip_wait(self.h, int(step)))
 
     def step(self, nsteps: int = 1) -> np.ndarray:
         out = np.zeros(self.B, dtype=np.int32)
@@ -217,6 +224,17 @@ class BrainBatch:
         res = np.zeros(n.value, dtype=np.int32)
         nat.check(self.L.fb_fired(self.h, b, nat.ptr(res), n.value, C.byref(n)))
         return res
+
+    def ring(self, b: int = 0):
+        """Brain b's delay ring: (lists [nslots, N], counts [nslots], head); slot head is
+        delivered next, and the slots after it hold the spikes still in flight."""
+        q = self.p[b]
+        ns = max(1, int(math.floor(q["delay"] / q["dt"] + 0.5))) + 1  # src/lifwasm.js:39
+        lists = np.zeros(ns * self.N[b], dtype=np.int32)
+        counts = np.zeros(ns, dtype=np.int32)
+        head = C.c_int32()
+        nat.check(self.L.fb_ring_read(self.h, b, nat.ptr(lists), nat.ptr(counts), C.byref(head)))
+        return lists.reshape(ns, self.N[b]), counts, int(head.value)
 
     def _list(self, fn, b, idx, vals):
         idx = np.ascontiguousarray(np.atleast_1d(idx), dtype=np.int32)

@@ -160,10 +160,21 @@ typedef struct fb_tuning {
   int32_t blocks_per_sm, item_chunks;
   int32_t max_blocks_per_sm, sms; /* read only */
   int32_t sub_grab;               /* update sub-tiles per dynamic grab, 1 .. 256; -1: all dealt statically */
-  int32_t pad;
+  int32_t timeout_us;             /* bound of every device-side wait of both schedules, microseconds
+                                     (default 5,000,000); a wait that runs out ends the launch with
+                                     FB_ETIMEOUT */
 } fb_tuning;
 int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t);
 int fb_brains_tuning(fb_brains *br, fb_tuning *t);
+
+/* Test hook for the timeout path, no counterpart in the reference (whose kernel has no waits; its
+ * GPU path falls back on a failure, src/brainsetup.js:66-75). Arms the next launch of the
+ * delay-scheduled kernel so that one tile block, at step `step` of that launch, waits on a flag
+ * nothing sets: the wait runs out after timeout_us, every other block leaves its own bounded wait,
+ * and the call returns FB_ETIMEOUT. A failed launch of that kernel leaves the brain as it was
+ * before the call (state lives in shared memory until the launch completes), so the handle steps
+ * on from there. Consumed by that one launch; -1 disarms. */
+int fb_debug_trip_wait(fb_brains *br, int32_t step);
 
 /* Advances every brain by nsteps steps in one persistent launch (lif_step, src/wasm/lif.c:29-80,
  * nsteps times). out_nfired (optional, int32[B]) receives each brain's fired count of its last
@@ -185,6 +196,13 @@ int fb_spike_log(fb_brains *br, int32_t b, int32_t *counts, int32_t cap_steps, i
  * then threshold spikes in ascending index): the view LIFWasm.step returns
  * (src/lifwasm.js:83-84). *n receives the count; at most cap indices are copied. */
 int fb_fired(fb_brains *br, int32_t b, int32_t *dst, int32_t cap, int32_t *n);
+
+/* Brain b's delay ring as lif.c keeps it (src/wasm/lif.c:35,44-45,77-79; the ring LIFWasm lays
+ * out in its memory, src/lifwasm.js:39-49): ring[nslots * N] receives the fired lists, of which
+ * only the first counts[s] entries of slot s are meaningful; counts[nslots] the list lengths; *head
+ * the slot the next step delivers. Slots head .. head + nslots - 2 (mod nslots) hold the spikes
+ * still in flight. Any output may be NULL. */
+int fb_ring_read(fb_brains *br, int32_t b, int32_t *ring, int32_t *counts, int32_t *head);
 
 /* Injections, queued in call order and applied before the next step or read.
  * fb_set_drive: drive[idx[k]] = hz[k]; a positive rate appends the neuron to the driven set if

@@ -94,31 +94,66 @@ def test_golden_mixed_schedules():
     assert_same(blocks, got, state, final_state(brain))
 
 
-def test_small_workload_long_launches():
-    """N=20,000, 150 Hz into 1%: 4,000 steps as four 1,000-step launches (AUTO picks the lagged
-    kernel); after each launch the state, spike counts and the fired lists still in flight (the
-    ring) equal the oracle's."""
+def assert_same_as_oracle(gb, ob, where=""):
+    """Every state word, spike count, the generator state, the ring head and every fired list
+    still in flight of the GPU brain equal the oracle brain's."""
+    s0, s1 = final_state(ob), final_state(gb)
+    for k in s0:
+        assert s0[k].tobytes() == s1[k].tobytes(), (where, k)
+    h = ob._pull()
+    sc = gb._batch.scalars(0)
+    assert (sc["rng"], sc["head"], sc["nFired"], sc["lastSlot"]) == (h.rng, h.head, h.nFired, h.lastSlot), where
+    lists, counts, head = gb._batch.ring(0)
+    assert head == h.head, where
+    np.testing.assert_array_equal(counts, ob.ringCount, err_msg=str(where))
+    N = ob.N
+    for s in range(counts.shape[0]):
+        np.testing.assert_array_equal(lists[s, :counts[s]], ob.ring[s * N: s * N + counts[s]], err_msg=f"{where} slot {s}")
+
+
+def _long_launches(name, launches, length, seed=1):
     from oracle import oracle as O
     from flybrain import SYNTH_PARAMS, DeviceGraph, LIFCuda, workload
     from flybrain import _native as nat
-    g, idx, hz, _ = workload("small")
-    ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, SYNTH_PARAMS, seed=1)
-    gb = LIFCuda(DeviceGraph(g), SYNTH_PARAMS, seed=1)
+    g, idx, hz, _ = workload(name)
+    ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, SYNTH_PARAMS, seed=seed)
+    gb = LIFCuda(DeviceGraph(g), SYNTH_PARAMS, seed=seed)
     for i, h in zip(idx.tolist(), hz.tolist()):
         ob.setDriveOne(i, h)
         gb.setDriveOne(i, h)
-    for _ in range(4):
-        ob.run(1000)
-        gb.run(1000)
+    gb._batch.set_schedule(nat.FB_SCHEDULE_LAGGED)
+    spikes = 0
+    for k in range(launches):
+        ob.run(length)
+        gb.run(length)
         assert gb._batch.last_schedule() == nat.FB_SCHEDULE_LAGGED
-        s0, s1 = final_state(ob), final_state(gb)
-        for k in s0:
-            assert s0[k].tobytes() == s1[k].tobytes(), k
-        h = ob._pull()
-        np.testing.assert_array_equal(gb._batch.fired(0), ob.ring[h.lastSlot * g.N: h.lastSlot * g.N + h.nFired])
-    # the next steps, one launch each (grid kernel), continue from the handed-over ring
+        assert_same_as_oracle(gb, ob, (name, k))
+        spikes = int(ob.spikeCount.sum())
+    return ob, gb, spikes
+
+
+def test_small_workload_long_launches():
+    """N=20,000, 150 Hz into 1%: the whole 1,000 ms window (10,000 steps) as ten 1,000-step
+    launches of the delay-scheduled kernel; after each launch the state, spike counts, generator
+    state and every fired list still in flight (the ring) equal the oracle's. The next steps, one
+    grid-kernel launch each, continue from the handed-over ring."""
+    from flybrain import _native as nat
+    ob, gb, spikes = _long_launches("small", 10, 1000)
+    assert spikes > 0
+    gb._batch.set_schedule(nat.FB_SCHEDULE_AUTO)
     for _ in range(30):
         np.testing.assert_array_equal(gb.step(), ob.step())
+
+
+@pytest.mark.slow
+def test_full_scale_whole_window_long_launches():
+    """The headline workload: N=165,122 (~11M edges), 2,000 drivers at 100-200 Hz, the whole
+    2,000 ms window (20,000 steps) as twenty unlogged 1,000-step launches of the delay-scheduled
+    kernel -- the launches the throughput figures are measured on. After every launch every state
+    word, the spike counts, the generator state, the ring head and every fired list still in
+    flight equal the oracle's, bit for bit, from step 0."""
+    ob, gb, spikes = _long_launches("full", 20, 1000)
+    assert spikes > 400_000
 
 
 def test_lagged_refuses_presynaptic_inhibition():

@@ -96,7 +96,7 @@ def _case(name):
         bias = rng.uniform(-1.0, 4.0, g.N).astype(np.float32)
         thr = rng.uniform(-2.0, 2.0, g.N).astype(np.float32)
     elif name == "no_drive":
-        p = dict(SYNTH_PARAMS, bgRate=60.0, bgAmp=2.5)
+        p = dict(SYNTH_PARAMS, bgRate=400.0, bgAmp=5.0)  # background alone drives the network
         idx = np.zeros(0, np.int32)
         hz = np.zeros(0)
     elif name == "every_neuron_driven":
