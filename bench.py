@@ -10,11 +10,18 @@ steps) from rest. One bench step = 1,000 brain steps (100 ms simulated) in one p
           set from host memory, runs, and reads spike counts + the last fired list back
   cpu_baseline : the oracle port of lif_step (1 core: the reference kernel is serial) on a
           bounded sample of the same workload
-  extra legs (each switchable by FB_BENCH_<LEG>=0): adjoint, adjoint_batched, adjoint_uneven,
-          batched (256 trials), flyvis (64 eyes), embodied (the per-millisecond call pattern of
-          the simulated fly: drive rewritten, 2 steps, spike counts read back, every ms)
+  extra legs (each switchable by FB_BENCH_<LEG>=0), each with its own cpu_baseline:
+          high_activity (the headline plus a 6 mV tonic bias: ~97% of spikes recurrent),
+          adjoint, adjoint_batched, adjoint_uneven (float32 and, beside it, float64 -- the
+          reference's arithmetic), batched (256 trials; split over ranks when N > 1), flyvis
+          (64 eyes), embodied (the per-millisecond call pattern of the simulated fly)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Over N GPUs (torchrun, one rank per GPU): the single-trial legs run as independent replicas
+(value = all ranks' events over the slowest rank's time); the batched ensemble's trials are split
+over the ranks (rank r runs trials r, r + N, ...), the batched adjoint's in contiguous blocks whose
+per-edge gradients are summed in global trial order by a chained hand-over (flybrain.shard).
 """
 from __future__ import annotations
 
@@ -43,6 +50,12 @@ DRAM_BYTES_PER_STEP_SINGLE = {
     "grid": 16.826112e6 / 100,    # fb::step_kernel
     "lagged": (53.468928e6 + 0.851456e6) / 100,   # fb::lagged_kernel
 }
+# DRAM bytes (read + write) per trial-step of the batched grid kernel, from one ncu capture of a
+# 100-step launch over 32 full-scale trials (profiles/step_kernel_batched_32_trials.txt:
+# 12.51 GB read + 6.95 GB written over 3,200 trial-steps); the bench's launch is scaled by its
+# trial-steps (the update streams every trial's state, so traffic grows in proportion).
+DRAM_BYTES_PER_TRIAL_STEP_BATCHED = (12.51e9 + 6.95e9) / 3200
+HIGH_ACTIVITY_BIAS_MV = 6.0
 KERNEL_NAME = {
     "grid": "fb::step_kernel (persistent, two grid barriers per step)",
     "lagged": "fb::lagged_kernel (persistent, delay-scheduled)",
@@ -149,20 +162,80 @@ def algorithmic_bytes(N, steps, spikes, events):
     return 64.0 * N * steps + 20.0 * spikes + 16.0 * events + 16.0 * spikes
 
 
-def cpu_baseline(g, idx, hz, params, sample_steps):
-    """The oracle port of lif_step on one host core over sample_steps brain steps."""
+def cpu_baseline(g, idx, hz, params, sample_steps, bias_mv=0.0, warm_steps=200):
+    """The oracle port of lif_step on one host core over sample_steps brain steps (after
+    warm_steps from rest)."""
     from oracle import oracle as O
     O.build(ref=False)
     ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, params, seed=1, backend="port")
     for i, h in zip(idx.tolist(), hz.tolist()):
         ob.setDriveOne(i, h)
-    ob.run(200)  # warm caches
+    if bias_mv:
+        ob.setBias(np.arange(g.N, dtype=np.int32), bias_mv)
+    ob.run(warm_steps)  # warm caches (and, with a bias, the activity)
     sc0 = ob.spikeCount.astype(np.int64)
     t0 = time.perf_counter()
     ob.run(sample_steps)
     dt = time.perf_counter() - t0
     ev = float(((ob.spikeCount.astype(np.int64) - sc0) * g.outdeg()).sum())
     return ev / dt, dt, ev
+
+
+def cpu_batched(g, spec, params, graphs, trials, sample_steps):
+    """The batched ensemble on the host cores: as many of the trials as there are host threads,
+    each an oracle brain with its own compiled weights (read back from the device), seed and drive,
+    advanced together by ob_run_many (OpenMP, one trial per thread; the reference shares one graph
+    across flies the same way, src/brainsetup.js:10-28). Trial-seconds per wall-second."""
+    from oracle import oracle as O
+    O.build(ref=False)
+    threads = int(O.lib("port").ob_threads())
+    n = min(threads, len(trials))
+    brains = []
+    for k in range(n):
+        b = int(trials[k])
+        w, sg = graphs[k].read()
+        ob = O.OracleBrain(g.N, g.indptr, g.indices, w, sg, params, seed=int(spec["seeds"][b]))
+        idx, hz = spec["drives"][b]
+        for i, h in zip(idx.tolist(), hz.tolist()):
+            ob.setDriveOne(i, h)
+        brains.append(ob)
+    O.run_many(brains, [50] * n)  # warm caches
+    sc0 = [ob.spikeCount.astype(np.int64) for ob in brains]
+    outdeg = g.outdeg().astype(np.int64)
+    t0 = time.perf_counter()
+    O.run_many(brains, [sample_steps] * n)
+    secs = time.perf_counter() - t0
+    ev = sum(float(((ob.spikeCount.astype(np.int64) - c) * outdeg).sum()) for ob, c in zip(brains, sc0))
+    trial_s = n * sample_steps * params["dt"] / 1000.0
+    return dict(value=trial_s / secs, unit="trial-s per wall-s", cores=n, kind="port", events_per_s=ev / secs,
+                sample=f"{n} of the trials ({sample_steps} brain steps each after 50 warm-up steps), oracle port "
+                       f"of lif_step, one trial per host thread ({secs:.1f} s)")
+
+
+def cpu_adjoint(problems, steps, readouts, label):
+    """The restated CPU adjoint (oracle/lifdiff.c: LIFDiff's forward with tape and checkpoints,
+    replay and reverse sweep, src/lifdiff.js:219-686) on `problems`, one per host thread, each a
+    recorded forward of `steps` steps and its backward with a per-step readout gradient.
+    Trial-seconds of gradient per wall-second."""
+    import concurrent.futures as cf
+
+    def one(k):
+        prob = problems[k]
+        _, tape = prob.forward(steps, seed=k + 1, checkpoint=100)
+        rng = np.random.default_rng(k)
+        dL = np.zeros((steps, prob.N), np.float32)
+        dL[:, readouts[k]] = (rng.standard_normal((steps, readouts[k].shape[0])) * 1e-3).astype(np.float32)
+        prob.backward(tape, dL)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=len(problems)) as ex:
+        list(ex.map(one, range(len(problems))))
+    secs = time.perf_counter() - t0
+    trial_s = len(problems) * steps * 0.1 / 1000.0
+    return dict(value=trial_s / secs, unit="trial-s of gradient per wall-s", cores=len(problems), kind="port",
+                seconds_per_trial_s=secs / trial_s,
+                sample=f"{label}: {len(problems)} x {steps} steps, recorded forward + backward (oracle "
+                       f"restatement of LIFDiff in double, one problem per host thread, {secs:.1f} s)")
 
 
 def run_ours(args, rank, world):
@@ -254,25 +327,35 @@ def run_ours(args, rank, world):
                       kernel=KERNEL_NAME[sched], algorithmic_bytes_per_launch=per_launch_bytes),
         clocks=clk.summary(),
     )
-    if os.environ.get("FB_BENCH_ADJOINT", "1") == "1":
-        del brain
+    del brain
+    torch.cuda.empty_cache()
+    if os.environ.get("FB_BENCH_ACTIVE", "1") == "1":
+        res["high_activity"] = run_high_activity(g, idx, hz, args)
         torch.cuda.empty_cache()
-        res["adjoint"] = run_adjoint(g, idx, hz)
-        brain = None
+    precisions = [x for x in os.environ.get("FB_ADJ_PRECISIONS", "f32,f64").split(",") if x]
+    if os.environ.get("FB_BENCH_ADJOINT", "1") == "1":
+        res["adjoint"] = by_precision(precisions, lambda pr: run_adjoint(g, idx, hz, prec=pr, cpu=pr == precisions[0]))
+        torch.cuda.empty_cache()
     if os.environ.get("FB_BENCH_ADJOINT_BATCH", "1") == "1":
         plain_per_trial_s = dev_s / sim_s
-        ab = run_adjoint_batched(g, idx, hz, n_trials=int(os.environ.get("FB_ADJ_TRIALS", "64")),
-                                 steps=int(os.environ.get("FB_ADJ_STEPS", "5000")))
-        ab["plain_single_trial_forward_per_trial_s"] = plain_per_trial_s
-        ab["cost_vs_plain_single_trial_forward"] = ab["fwd_bwd_per_trial_s"] / plain_per_trial_s
-        res["adjoint_batched"] = ab
-        torch.cuda.empty_cache()
-        res["adjoint_uneven"] = run_adjoint_uneven(n_inst=int(os.environ.get("FB_ADJ_UNEVEN", "128")))
+
+        def batched_adj(pr):
+            ab = run_adjoint_batched(g, idx, hz, n_trials=int(os.environ.get("FB_ADJ_TRIALS", "64")),
+                                     steps=int(os.environ.get("FB_ADJ_STEPS", "5000")), prec=pr, rank=rank,
+                                     world=world, cpu=pr == precisions[0])
+            ab["plain_single_trial_forward_per_trial_s"] = plain_per_trial_s
+            ab["cost_vs_plain_single_trial_forward"] = ab["fwd_bwd_per_trial_s"] / plain_per_trial_s
+            torch.cuda.empty_cache()
+            return ab
+
+        res["adjoint_batched"] = by_precision(precisions, batched_adj)
+        res["adjoint_uneven"] = by_precision(
+            precisions, lambda pr: run_adjoint_uneven(n_inst=int(os.environ.get("FB_ADJ_UNEVEN", "128")), prec=pr,
+                                                      cpu=pr == precisions[0]))
         torch.cuda.empty_cache()
     if os.environ.get("FB_BENCH_BATCHED", "1") == "1":
-        del brain
         torch.cuda.empty_cache()
-        bt = run_batched(g, args, n_trials=int(os.environ.get("FB_BATCH_TRIALS", "256")))
+        bt = run_batched(g, args, n_trials=int(os.environ.get("FB_BATCH_TRIALS", "256")), rank=rank, world=world)
         bt["cost_vs_plain_per_trial_s"] = (1.0 / bt["trial_s_per_wall_s"]) / (dev_s / sim_s)
         res["batched"] = bt
     if os.environ.get("FB_BENCH_FLYVIS", "1") == "1":
@@ -288,6 +371,78 @@ def run_ours(args, rank, world):
                                    sample=f"{sample} brain steps of the same workload from rest "
                                           f"({secs:.1f} s, oracle port of lif_step, 1 thread)")
         print(json.dumps(res), flush=True)
+
+
+def run_high_activity(g, idx, hz, args, bias_mv=HIGH_ACTIVITY_BIAS_MV, launches=5):
+    """High-activity variant of the full-scale forward: the headline's graph and drive plus a
+    tonic bias of `bias_mv` on every neuron (setBias), which holds the network about 1 mV below
+    threshold, so that almost every spike is a recurrent threshold crossing (about 60 Hz mean rate
+    and 50k synaptic events per step, against about 1.5k in the headline, where nearly every spike
+    is a driven one). Times the delivery and threshold cascade the headline barely exercises:
+    `launches` launches of the bench step's length from rest, L2 flushed between them."""
+    import torch
+    from flybrain import SYNTH_PARAMS, DeviceGraph, LIFCuda
+    from flybrain import _native as nat
+    S = BRAIN_STEPS_PER_BENCH_STEP
+    brain = LIFCuda(DeviceGraph(g), SYNTH_PARAMS, seed=1)
+    brain._batch.set_drive(0, idx, hz)
+    brain.setBias(np.arange(g.N, dtype=np.int32), bias_mv)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    brain.run(S)  # warm-up
+    brain.reset()
+    outdeg = g.outdeg().astype(np.int64)
+    driven = np.zeros(g.N, bool)
+    driven[idx] = True
+    sc_prev = brain.spikeCount.astype(np.int64)
+    ms, events, spikes, dspikes = [], 0.0, 0.0, 0.0
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(launches):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            brain.run(S)
+            ms.append(brain._batch.last_ms())
+            sc = brain.spikeCount.astype(np.int64)
+            d = sc - sc_prev
+            events += float((d * outdeg).sum())
+            spikes += float(d.sum())
+            dspikes += float(d[driven].sum())
+            sc_prev = sc
+    secs = sum(ms) / 1e3
+    sim_s = launches * S * SYNTH_PARAMS["dt"] / 1000.0
+    sched = "lagged" if brain._batch.last_schedule() == nat.FB_SCHEDULE_LAGGED else "grid"
+    peak, kind = peaks()
+    byts = algorithmic_bytes(g.N, S, spikes / launches, events / launches)
+    ach = byts / (np.mean(ms) / 1e3) / 1e9
+    del brain
+    sample = int(os.environ.get("FB_CPU_ACTIVE_SAMPLE_STEPS", "1000"))
+    v, csecs, _ = cpu_baseline(g, idx, hz, SYNTH_PARAMS, sample, bias_mv=bias_mv, warm_steps=300)
+    return dict(bias_mv=bias_mv, launches=launches, brain_steps=launches * S, events_per_s=events / secs,
+                ms_per_1000_steps=1e3 * secs / (launches * S) * 1000, realtime_factor=sim_s / secs,
+                spikes_per_step=spikes / (launches * S), recurrent_fraction=1.0 - dspikes / max(spikes, 1.0),
+                events_per_step=events / (launches * S), schedule=sched, gpu_launches=launches * (2 if sched == "lagged" else 1),
+                roofline=dict(bound="hbm", achieved=ach, peak=peak, unit="GB/s", frac=ach / peak, peak_kind=kind,
+                              traffic=None, kernel=KERNEL_NAME[sched], algorithmic_bytes_per_launch=byts),
+                clocks=clk.summary(),
+                cpu_baseline=dict(value=v, unit="synaptic events/s", cores=1, kind="port",
+                                  sample=f"{sample} brain steps after 300 from rest, same bias ({csecs:.1f} s, "
+                                         "oracle port of lif_step, 1 thread)"),
+                config=f"the headline workload (N={g.N:,}, 2,000 drive neurons at U(100,200) Hz) plus a tonic "
+                       f"{bias_mv} mV bias on every neuron; {launches} launches of {S} steps from rest, L2 flushed "
+                       "between launches")
+
+
+def by_precision(precisions, fn):
+    """A leg's result in its first precision, with each further precision's result beside it
+    under its own key (e.g. "f64")."""
+    out = None
+    for pr in precisions:
+        r = fn(pr)
+        if out is None:
+            out = r
+        else:
+            out[pr] = r
+    return out
 
 
 def run_embodied(g, ms=1000, sensory=3000, seed=3):
@@ -375,83 +530,84 @@ def run_flyvis(n_eyes=64, steps=200, seed=1):
                        "luminance inputs; one launch per step, state [N][eyes] in HBM")
 
 
-def run_batched(g, args, n_trials=256, seed=7):
+def run_batched(g, args, n_trials=256, seed=7, rank=0, world=1):
     """Batched ensemble: n_trials independent brains over the full graph's topology in one
-    persistent launch. Each trial: its own seed, duration U(200, 2000) ms, drive set of
-    U{500..4000} neurons at U(50, 250) Hz, and per-cell-type outgoing gains lognormal(0, 0.2) over
-    64 types compiled into its weights (writeGraph's outScale, on the device)."""
+    persistent launch (flybrain.ensemble). Each trial: its own seed, duration U(200, 2000) ms,
+    drive set of U{500..4000} neurons at U(50, 250) Hz, and per-cell-type outgoing gains
+    lognormal(0, 0.2) over 64 types compiled into its weights (writeGraph's outScale, on the
+    device). Over several ranks, rank r runs trials r, r + world, ... (no exchange); the value is
+    every rank's trial-seconds over the slowest rank's launch time."""
     import torch
-    from flybrain import BrainBatch, DeviceGraph
+    from flybrain.ensemble import build_ensemble, ensemble_spec
+    from flybrain.shard import trials_of_rank
     from flybrain.synth import SYNTH_PARAMS
-    rng = np.random.default_rng(seed)
     p = dict(SYNTH_PARAMS, wSyn=0.275, inhGain=1.0, minSyn=1)
-    topo = DeviceGraph(g)
-    counts = torch.from_numpy(g.counts.astype(np.float32)).cuda()
-    sign = torch.from_numpy(g.sign.astype(np.float32)).cuda()
-    ctype = torch.from_numpy(g.cell_type.astype(np.int64)).cuda()
-    graphs = []
-    for _ in range(n_trials):
-        gains = torch.from_numpy(rng.lognormal(0.0, 0.2, 64).astype(np.float32)).cuda()
-        graphs.append(topo.compile(counts, sign, p, out_scale=gains[ctype].contiguous()))
-    torch.cuda.synchronize()
-    seeds = rng.integers(1, 1 << 30, n_trials)
-    batch = BrainBatch(graphs, p, seeds)
-    steps = np.round(rng.uniform(200.0, 2000.0, n_trials) / p["dt"]).astype(np.int32)
-    for b in range(n_trials):
-        nd = int(rng.integers(500, 4001))
-        idx = np.sort(rng.choice(g.N, nd, replace=False)).astype(np.int32)
-        batch.set_drive(b, idx, rng.uniform(50.0, 250.0, nd))
+    spec = ensemble_spec(g.N, n_trials, seed=seed, dt=p["dt"])
+    mine = trials_of_rank(n_trials, rank, world, "interleaved")
+    batch, graphs, _ = build_ensemble(g, spec, p, mine)
+    steps = spec["steps"][mine]
     batch.step(args.warmup * 10)  # warm-up
     from flybrain.autotune import tune_brains
-    tune = tune_brains(batch, steps=100, key=f"bench-ensemble|B={n_trials}|N={g.N}|E={g.E}")
+    tune = tune_brains(batch, steps=100, key=f"bench-ensemble|B={len(mine)}|N={g.N}|E={g.E}")
     batch.reset(-1)  # back to rest
     outdeg = g.outdeg().astype(np.int64)
     torch.cuda.synchronize()
+    barrier(world)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         batch.step_uneven(steps)
         ms = batch.last_ms()
+    barrier(world)
     events = spikes = 0.0
     readout = []
-    for b in range(n_trials):
+    for b in range(len(mine)):
         sc = batch.read("spikeCount", b).astype(np.int64)
         events += float((sc * outdeg).sum())
         spikes += float(sc.sum())
         readout.append(float(sc[:1000].sum()) / (steps[b] * p["dt"] / 1000.0) / 1000.0)
-    secs = ms / 1e3
-    trial_sim_s = float(steps.sum()) * p["dt"] / 1000.0
+    secs_local = ms / 1e3
+    secs = max_over_ranks(secs_local, world)
+    trial_sim_s = sum_over_ranks(float(steps.sum()) * p["dt"] / 1000.0, world)
+    events_all = sum_over_ranks(events, world)
     byts = algorithmic_bytes(g.N, float(steps.sum()), spikes, events)
     peak, kind = peaks()
-    ach = byts / secs / 1e9
-    return dict(trials=n_trials, neurons=g.N, edges=g.E, trial_steps_total=int(steps.sum()),
-                max_steps=int(steps.max()), trial_sim_s=trial_sim_s, wall_s=secs,
-                trial_s_per_wall_s=trial_sim_s / secs, events_per_s=events / secs, spikes=spikes,
-                mean_readout_rate_hz=float(np.mean(readout)),
-                roofline=dict(bound="hbm", achieved=ach, peak=peak, unit="GB/s", frac=ach / peak,
-                              peak_kind=kind, traffic=None,
-                              algorithmic_bytes=byts),
-                clocks=clk.summary(), gpu_launches=1,
-                tuning=dict(blocks_per_sm=tune["blocks_per_sm"], item_chunks=tune["item_chunks"],
-                            cached=tune["cached"], candidates=len(tune.get("table", []))),
-                config="256 trials x N=165,122, own seeds, durations U(200,2000) ms, drives "
-                       "U{500..4000} neurons at U(50,250) Hz, 64 cell-type gains lognormal(0,0.2); "
-                       "one persistent launch, uneven steps; state in HBM (no L2 flush needed: "
-                       "the batch's state is ~60 GB)")
+    ach = byts / secs_local / 1e9
+    traffic = DRAM_BYTES_PER_TRIAL_STEP_BATCHED * float(steps.sum())
+    res = dict(trials=n_trials, trials_this_rank=int(len(mine)), neurons=g.N, edges=g.E,
+               trial_steps_total=int(steps.sum()), max_steps=int(steps.max()), trial_sim_s=trial_sim_s, wall_s=secs,
+               trial_s_per_wall_s=trial_sim_s / secs, events_per_s=events_all / secs, spikes=spikes,
+               mean_readout_rate_hz=float(np.mean(readout)),
+               roofline=dict(bound="hbm", achieved=ach, peak=peak, unit="GB/s", frac=ach / peak,
+                             peak_kind=kind, traffic=traffic, algorithmic_bytes=byts,
+                             dram_gbs=traffic / secs_local / 1e9, dram_frac=traffic / secs_local / 1e9 / peak,
+                             traffic_note="DRAM bytes scaled from a 32-trial ncu capture of the same kernel by "
+                                          "trial-steps; achieved/frac count lif.c's algorithmic bytes, dram_gbs/"
+                                          "dram_frac what DRAM actually carried"),
+               clocks=clk.summary(), gpu_launches=1,
+               tuning=dict(blocks_per_sm=tune["blocks_per_sm"], item_chunks=tune["item_chunks"],
+                           cached=tune["cached"], candidates=len(tune.get("table", []))),
+               config=f"{n_trials} trials x N=165,122, own seeds, durations U(200,2000) ms, drives "
+                      "U{500..4000} neurons at U(50,250) Hz, 64 cell-type gains lognormal(0,0.2); "
+                      "one persistent launch, uneven steps; state in HBM (no L2 flush needed: "
+                      "the batch's state is ~60 GB)" + (f"; trials split over {world} ranks" if world > 1 else ""))
+    if rank == 0:
+        sample = int(os.environ.get("FB_CPU_BATCH_SAMPLE_STEPS", "200"))
+        res["cpu_baseline"] = cpu_batched(g, spec, p, graphs, mine, sample)
+    return res
 
 
-def run_adjoint(g, idx, hz, steps=5000, seed=3):
+def run_adjoint(g, idx, hz, steps=5000, seed=3, prec="f32", cpu=True):
     """The differentiable workload: surrogate-gradient LIF (fast-sigmoid slope 25/mV, beta 0.04)
     on the full graph, 500 ms at dt 0.1 ms, checkpoint every 100 steps; loss = MSE between 20 ms
     low-pass rates of 1,000 seeded readout neurons and a seeded 0-80 Hz target; gradients for
     every edge gain, every neuron's bias and 64 cell-type gains through the autograd function.
     The adjoint is bounded with the reference's adjClip (100, the value of its loom refit) since
     the steep surrogate's adjoint overflows on this graph otherwise. Arithmetic: float32
-    intermediates (FB_ADJ_PRECISION=f64 for the reference's double). Reports forward+backward
+    intermediates, or prec="f64" for the reference's double). Reports forward+backward
     time against the plain (unrecorded) forward of the same window, and the library's own
     forward/backward times."""
     import torch
     from flybrain.autograd import DiffContext, LIFDiffFunction, lowpass_rates
     from flybrain.diff import DiffNet
-    prec = os.environ.get("FB_ADJ_PRECISION", "f32")
     rng = np.random.default_rng(seed)
     data = dict(N=g.N, indptr=g.indptr, indices=g.indices, weights=g.counts.astype(np.float32), sign=g.sign)
     opts = dict(dt=0.1, vRest=-52.0, vThresh=-45.0, vReset=-52.0, tauM=20.0, tauSyn=5.0, tRef=2.2,
@@ -497,7 +653,7 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3):
     _, bwd_s = clock(loss.backward)
     sim_s = steps * 0.1 / 1000
     ge, gb, gt = eg.grad, bias.grad, tg.grad
-    return dict(neurons=g.N, edges=g.E, steps=steps, checkpoint=100, sim_s=sim_s, precision=prec,
+    out = dict(neurons=g.N, edges=g.E, steps=steps, checkpoint=100, sim_s=sim_s, precision=prec,
                 plain_forward_s=plain, library_forward_recorded_s=lib_fwd, library_backward_s=lib_bwd,
                 autograd_forward_s=fwd_s, autograd_backward_s=bwd_s,
                 fwd_bwd_per_trial_s=(fwd_s + bwd_s) / sim_s, plain_per_trial_s=plain / sim_s,
@@ -508,6 +664,47 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3):
                 config="surrogate-gradient LIF (beta 0.04, adjClip 100), N=165,122, 500 ms at dt 0.1 ms, "
                        "K=100; MSE of 20 ms low-pass rates of 1,000 readouts vs a 0-80 Hz target; "
                        "gradients for every edge gain, bias and 64 type gains (autograd)")
+    del net, dctx
+    if os.environ.get("FB_BENCH_GRAD_CHECK", "1") == "1":
+        out["grad_check"] = grad_check_full(g, idx, hz, data, prec)
+    if cpu:
+        from oracle.lifdiff_oracle import DiffProblem
+        cs = int(os.environ.get("FB_CPU_ADJ_SAMPLE_STEPS", "300"))
+        prob = DiffProblem(g.N, g.indptr, g.indices, g.counts.astype(np.float32), g.sign, params=ADJ_OPTS,
+                           driven=idx, drive_hz=hz, edgeGain=np.ones(g.E, np.float32), outScale=np.ones(g.N, np.float32))
+        out["cpu_baseline"] = cpu_adjoint([prob], cs, [readout.astype(np.int32)], "the same network and readouts")
+        out["cpu_baseline"]["vs_gpu_fwd_bwd"] = out["cpu_baseline"]["seconds_per_trial_s"] / out["fwd_bwd_per_trial_s"]
+    return out
+
+
+def grad_check_full(g, idx, hz, data, prec, steps=500, seed=3):
+    """Gradient accuracy of this leg's arithmetic at full scale: the same network in its smooth
+    form (soft spikes, the same surrogate slope), 500 steps, the same loss through the autograd
+    function; 32 parameters (11 edge gains, 11 biases, 10 type gains, drawn among those with a
+    non-zero gradient) against central finite differences (h = 1e-3) of the forward in double."""
+    import torch
+    from flybrain.autograd import DiffContext, finite_difference_check
+    from flybrain.diff import DiffNet
+    rng = np.random.default_rng(seed)
+    net = DiffNet(data, dict(ADJ_OPTS, soft=True, precision=prec, edgeGain=np.ones(g.E, np.float32),
+                             bias=np.zeros(g.N, np.float32), outScale=np.ones(g.N, np.float32)))
+    for i, h in zip(idx.tolist(), hz.tolist()):
+        net.setDriveOne(i, h)
+    readout = np.sort(rng.choice(g.N, 1000, replace=False))
+    dctx = DiffContext(net, g.cell_type, readout, steps, seed=seed)
+    target = torch.as_tensor(rng.uniform(0, 80, (1, 1000)), dtype=torch.float32, device="cuda")
+    eg = torch.ones(g.E, device="cuda", requires_grad=True)
+    bias = torch.zeros(g.N, device="cuda", requires_grad=True)
+    tg = torch.as_tensor(rng.lognormal(0, 0.2, 64), dtype=torch.float32, device="cuda").requires_grad_()
+    t0 = time.perf_counter()
+    r = finite_difference_check(dctx, target, eg, bias, tg, seed=5, fd_precision="f64")
+    r["seconds"] = time.perf_counter() - t0
+    r["config"] = (f"soft spikes (beta 0.04), N={g.N:,}, {steps} steps, K=100; {r['params']} parameters against "
+                   "FP64 central differences, h=1e-3; tolerance of scripts/grad_check.mjs:98")
+    r["rows"] = [dict(kind=x["kind"], index=x["index"], rel=x["rel"]) for x in r["rows"]]
+    del net, dctx
+    torch.cuda.empty_cache()
+    return r
 
 
 ADJ_OPTS = dict(dt=0.1, vRest=-52.0, vThresh=-45.0, vReset=-52.0, tauM=20.0, tauSyn=5.0, tRef=2.2, delay=1.8,
@@ -544,18 +741,22 @@ def _tune_adjoint(batch, seeds, readouts, rng, key, steps=400):
                 cached=r["cached"], candidates=len(r.get("table", [])), tuning_s=sum(x["s"] for x in r.get("table", [])))
 
 
-def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
+def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5, prec="f32", rank=0, world=1, cpu=True):
     """Batched forward+adjoint: n_trials trials of the differentiable workload (surrogate slope
     25/mV, adjClip 100, 500 ms at dt 0.1 ms, K=100, float32 intermediates) sharing the full graph
     and its edge gains, each with its own seed and target trace, in one batch (fb_diff_batch_*);
     gradients for every edge (summed over trials in trial order), bias and type gain. Cost per
-    trial-second against the plain single-trial forward."""
+    trial-second against the plain single-trial forward. Over several ranks, rank r runs one
+    contiguous block of the trials and the per-edge gradients are summed in global trial order
+    across ranks (flybrain.shard.ordered_sum: the same float64 additions as one process)."""
     import torch
     from flybrain.diff import DiffBatch, DiffNet
-    prec = os.environ.get("FB_ADJ_PRECISION", "f32")
+    from flybrain.shard import ordered_sum, trials_of_rank
     rng = np.random.default_rng(seed)
     data = dict(N=g.N, indptr=g.indptr, indices=g.indices, weights=g.counts.astype(np.float32), sign=g.sign)
     eg = np.ones(g.E, np.float32)
+    mine = trials_of_rank(n_trials, rank, world, "blocks")
+    n_all, n_trials = n_trials, int(len(mine))
     members = []
     for _ in range(n_trials):
         n = DiffNet(data, dict(ADJ_OPTS, edgeGain=eg), _defer=True)
@@ -568,9 +769,9 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
     create_s = time.perf_counter() - t0
     readout = np.sort(rng.choice(g.N, 1000, replace=False)).astype(np.int32)
     readouts = [readout] * n_trials
-    targets = [torch.as_tensor(rng.uniform(0, 80, (1, 1000)), dtype=torch.float32, device="cuda")
-               for _ in range(n_trials)]
-    seeds = list(range(1, n_trials + 1))
+    all_targets = [rng.uniform(0, 80, (1, 1000)) for _ in range(n_all)]
+    targets = [torch.as_tensor(all_targets[b], dtype=torch.float32, device="cuda") for b in mine.tolist()]
+    seeds = [int(b) + 1 for b in mine.tolist()]
 
     def clock(fn):
         torch.cuda.synchronize()
@@ -586,11 +787,23 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
     (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
     gs, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
     ge = torch.zeros(g.E, dtype=torch.float64, device="cuda")
-    _, sum_s = clock(lambda: batch.edge_sum(out=ge))
+    if world == 1:
+        _, sum_s = clock(lambda: batch.edge_sum(out=ge))
+    else:  # this rank's trials in order, continued across ranks in global trial order
+        def cross():
+            per = []
+            for b in range(n_trials):
+                x = torch.zeros(g.E, dtype=torch.float64, device="cuda")
+                batch.edge_sum(insts=[b], out=x)
+                per.append(x)
+            return ordered_sum(per, n_all, rank, world, (g.E,), device="cuda")
+        ge, sum_s = clock(cross)
     trial_s = n_trials * steps * 0.1 / 1000
     total = fwd_s + loss_s + bwd_s + sum_s
+    trial_s = sum_over_ranks(trial_s, world)
+    total = max_over_ranks(total, world)
     spikes = sum(int(batch.tape(b)[0][-1]) for b in range(min(n_trials, 4)))
-    return dict(trials=n_trials, neurons=g.N, edges=g.E, steps=steps, checkpoint=batch.p["checkpoint"],
+    out = dict(trials=n_all, trials_this_rank=n_trials, neurons=g.N, edges=g.E, steps=steps, checkpoint=batch.p["checkpoint"],
                 precision=prec, tuning=tune,
                 create_s=create_s, plain_batch_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s,
                 backward_s=bwd_s, edge_sum_s=sum_s, trial_s=trial_s,
@@ -598,19 +811,31 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5):
                 trial_s_of_gradient_per_wall_s=trial_s / total, loss=loss, spikes_first4=spikes,
                 grads=dict(edge_nonzero=int((ge != 0).sum()), edge_finite=bool(torch.isfinite(ge).all()),
                            bias_nonzero=int(sum(int((x["bias"] != 0).sum()) for x in gs))),
-                config=f"{n_trials} trials sharing the N=165,122 graph and its edge gains, own seeds and "
+                config=f"{n_all} trials sharing the N=165,122 graph and its edge gains, own seeds and "
                        "target traces; surrogate slope 25/mV, adjClip 100, 500 ms at dt 0.1 ms, K and "
-                       "launch shape autotuned")
+                       "launch shape autotuned" + (f"; contiguous trial blocks over {world} ranks, per-edge "
+                                                  "gradients summed in trial order" if world > 1 else ""))
+    del batch, members, gs, dls
+    torch.cuda.empty_cache()
+    if cpu and rank == 0:
+        from oracle import oracle as O
+        from oracle.lifdiff_oracle import DiffProblem
+        O.build(ref=False)
+        nt = max(1, min(int(O.lib("port").ob_threads()), n_trials))
+        cs = int(os.environ.get("FB_CPU_ADJ_BATCH_SAMPLE_STEPS", "200"))
+        probs = [DiffProblem(g.N, g.indptr, g.indices, data["weights"], g.sign, params=ADJ_OPTS, driven=idx,
+                             drive_hz=hz, edgeGain=eg, outScale=np.ones(g.N, np.float32)) for _ in range(nt)]
+        out["cpu_baseline"] = cpu_adjoint(probs, cs, [readout] * nt, f"{nt} of the trials")
+    return out
 
 
-def run_adjoint_uneven(n_inst=128, seed=11):
+def run_adjoint_uneven(n_inst=128, seed=11, prec="f32", cpu=True):
     """Batched uneven adjoint: n_inst instances over separately seeded synthetic subgraphs of
     5,000-60,000 neurons, each 100-400 ms (dt 0.1 ms) with its own drive (1% of neurons at
     150 Hz) and target trace; forward+backward of the whole batch against its plain forward."""
     import torch
     from flybrain.diff import DiffBatch, DiffNet
     from flybrain.synth import synth_graph
-    prec = os.environ.get("FB_ADJ_PRECISION", "f32")
     rng = np.random.default_rng(seed)
     import concurrent.futures as cf
     import multiprocessing as mp
@@ -652,7 +877,7 @@ def run_adjoint_uneven(n_inst=128, seed=11):
     _, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
     trial_s = sum(steps) * 0.1 / 1000
     total = fwd_s + loss_s + bwd_s
-    return dict(instances=n_inst, neurons_total=int(sum(batch.N)), edges_total=int(sum(batch.E)),
+    out = dict(instances=n_inst, neurons_total=int(sum(batch.N)), edges_total=int(sum(batch.E)),
                 steps_min=min(steps), steps_max=max(steps), precision=prec, graph_gen_s=gen_s,
                 checkpoint=batch.p["checkpoint"], tuning=tune,
                 plain_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s, backward_s=bwd_s,
@@ -662,6 +887,20 @@ def run_adjoint_uneven(n_inst=128, seed=11):
                 config=f"{n_inst} instances over synthetic subgraphs of 5,000-60,000 neurons, 100-400 ms at "
                        "dt 0.1 ms, own drive/seed/target; surrogate slope 25/mV, adjClip 100, K and launch "
                        "shape autotuned")
+    if cpu:
+        from oracle import oracle as O
+        from oracle.lifdiff_oracle import DiffProblem
+        O.build(ref=False)
+        nt = max(1, min(int(O.lib("port").ob_threads()), n_inst))
+        cs = int(os.environ.get("FB_CPU_ADJ_BATCH_SAMPLE_STEPS", "200"))
+        probs = []
+        for k in range(nt):
+            m = members[k]
+            hz = m.drive[list(m.drivenSet)]
+            probs.append(DiffProblem(m.N, m.indptr, m.indices, m.counts, m.sign, params=ADJ_OPTS,
+                                     driven=np.asarray(list(m.drivenSet), np.int32), drive_hz=hz))
+        out["cpu_baseline"] = cpu_adjoint(probs, cs, readouts[:nt], f"the first {nt} instances")
+    return out
 
 
 def run_reference(args, rank, world):
@@ -678,7 +917,7 @@ def run_reference(args, rank, world):
     ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, SYNTH_PARAMS, seed=1, backend=backend)
     for i, h in zip(idx.tolist(), hz.tolist()):
         ob.setDriveOne(i, h)
-    S = int(os.environ.get("FB_REF_SAMPLE_STEPS", "500"))
+    S = int(os.environ.get("FB_REF_SAMPLE_STEPS", str(BRAIN_STEPS_PER_BENCH_STEP)))  # the window of our arm
     for _ in range(args.warmup):
         ob.run(S)
     ob.reset()

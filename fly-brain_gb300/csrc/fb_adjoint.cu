@@ -1788,6 +1788,15 @@ extern "C" int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *
       I.tStepsCap = cap;
     }
     if ((rc = set_inputs(b, I, steps[k], in ? in + k : nullptr))) return rc;
+    // soft spikes (src/lifdiff.js:335-340) deliver every neuron above 1e-4 every step, so one step
+    // can deliver a contribution over every edge: the overflow pool then needs E entries (a
+    // neuron arrives at most once per step, so no step delivers more)
+    if (p->soft && (int64_t)D.ovfCap < D.E + 1 && D.E + 1 <= 0x7fffffff) {
+      DOvf *o = nullptr;
+      if ((rc = talloc(b, &o, (size_t)(D.E + 1)))) return rc;
+      D.ovf = o;
+      D.ovfCap = (uint32_t)(D.E + 1);
+    }
   }
   bool edits = false;
   for (int k = 0; k < b->B; k++) edits = edits || b->in[k].D.epOff;

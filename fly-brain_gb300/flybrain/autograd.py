@@ -99,3 +99,60 @@ def lowpass_rates(raster: torch.Tensor, dt_ms: float, tau_ms: float = 20.0) -> t
         out.append(rb)
         r = rb[-1]
     return torch.cat(out).to(raster.dtype)
+
+
+def rate_loss(dctx: DiffContext, target: torch.Tensor, edge_gain, bias, type_gain) -> torch.Tensor:
+    """MSE between the 20 ms low-pass rates of the readout raster and a target trace."""
+    raster = LIFDiffFunction.apply(edge_gain, bias, type_gain, dctx)
+    return ((lowpass_rates(raster, dctx.net.p["dt"]) - target) ** 2).mean()
+
+
+def finite_difference_check(dctx: DiffContext, target, edge_gain, bias, type_gain, n_edge=11, n_bias=11,
+                            n_type=10, h=1e-3, seed=0, fd_precision="f64"):
+    """The adjoint's gradients of rate_loss against central finite differences, the check of
+    scripts/grad_check.mjs:69-109 applied to the three input kinds of LIFDiffFunction.
+
+    Parameters are drawn at random among the edges and biases whose adjoint gradient is non-zero
+    (most of a large network's are exactly zero over a short window) and among the cell types.
+    The adjoint runs in the context's precision; each finite difference takes two forward passes
+    in `fd_precision` ("f64": double-precision finite differences). A row passes grad_check's
+    tolerance |g - fd| <= 1e-3 |fd| + 4e-6 |L| / h (scripts/grad_check.mjs:98). Returns the rows
+    and the maximum and median relative errors |g - fd| / |fd|."""
+    for p in (edge_gain, bias, type_gain):
+        p.grad = None
+    L = rate_loss(dctx, target, edge_gain, bias, type_gain)
+    L.backward()
+    grads = dict(edge=edge_gain.grad.double().cpu().numpy(), bias=bias.grad.double().cpu().numpy(),
+                 type=type_gain.grad.double().cpu().numpy())
+    rng = np.random.default_rng(seed)
+
+    def pick(kind, n):
+        nz = np.nonzero(grads[kind] != 0)[0]
+        return [(kind, int(i)) for i in rng.choice(nz, min(n, nz.shape[0]), replace=False)]
+
+    picks = pick("edge", n_edge) + pick("bias", n_bias) + pick("type", n_type)
+    base = dict(edge=edge_gain.detach().clone(), bias=bias.detach().clone(), type=type_gain.detach().clone())
+    adj_prec = dctx.over.get("precision", dctx.net.p["precision"])
+    saved = dict(dctx.over)
+    dctx.over["precision"] = fd_precision
+    rows = []
+    try:
+        with torch.no_grad():
+            Lfd = float(rate_loss(dctx, target, base["edge"], base["bias"], base["type"]))
+            for kind, idx in picks:
+                vals = []
+                for sgn in (1, -1):
+                    x = {k: v.clone() for k, v in base.items()}
+                    x[kind][idx] += sgn * h
+                    vals.append(float(rate_loss(dctx, target, x["edge"], x["bias"], x["type"])))
+                fd = (vals[0] - vals[1]) / (2 * h)
+                a = float(grads[kind][idx])
+                ok = abs(a - fd) <= 1e-3 * abs(fd) + 4e-6 * abs(Lfd) / h
+                rows.append(dict(kind=kind, index=idx, adjoint=a, fd=fd, rel=abs(a - fd) / max(abs(fd), 1e-300), ok=ok))
+    finally:
+        dctx.over.clear()
+        dctx.over.update(saved)
+    rel = np.array([r["rel"] for r in rows]) if rows else np.zeros(1)
+    return dict(h=h, adjoint_precision=adj_prec, fd_precision=fd_precision, loss=float(L), params=len(rows),
+                passed=int(sum(r["ok"] for r in rows)), max_rel=float(rel.max()), median_rel=float(np.median(rel)),
+                rows=rows)

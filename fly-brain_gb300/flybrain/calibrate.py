@@ -120,7 +120,8 @@ def _mulberry32_lognormal(N: int, sigma: float, seed: int) -> np.ndarray:
     """exp(sigma * z) for N draws of the reference's seeded generator and Box-Muller transform
     (src/brainmodel.js:85-90), in float64."""
     M = 0xFFFFFFFF
-    a = (int(seed) * 2654435761) & M
+    # (seed * 2654435761) | 0: the product in double (rounded above 2^53), then modulo 2^32
+    a = int(math.fmod(math.floor(float(seed) * 2654435761.0), 4294967296.0)) & M
 
     def rnd():
         nonlocal a

@@ -106,9 +106,13 @@ def n_slots(p: dict) -> int:
 
 
 def seed_state(seed: int) -> int:
-    """Initial xorshift32 state, src/lifwasm.js:52: (seed * 2654435761) >>> 0 || 1."""
-    s = (int(seed) * 2654435761) & 0xFFFFFFFF
-    return s or 1
+    """Initial xorshift32 state, src/lifwasm.js:52: (seed * 2654435761) >>> 0 || 1. JavaScript
+    forms the product in double (rounded once when it exceeds 2^53, i.e. for seeds of 2^21 and
+    more) and >>> 0 takes that double modulo 2^32."""
+    x = math.fmod(math.floor(float(seed) * 2654435761.0), 4294967296.0)
+    if x < 0:
+        x += 4294967296.0
+    return int(x) or 1
 
 
 def write_graph_f64(N, indptr, indices, counts, nt_sign, p, in_scale=None, sensory_mask=None,
@@ -320,6 +324,24 @@ class OracleBrain:
     @property
     def nAwake(self):
         return self.N
+
+
+def run_many(brains, steps, nthreads: int = 0) -> int:
+    """Advances independent oracle brains (graphs may be shared) by steps[k] steps each, in
+    parallel over nthreads host threads (<= 0: all): ob_run_many, the CPU counterpart of a batched
+    ensemble. Returns the total fired count."""
+    if not brains:
+        return 0
+    L = brains[0].L
+    for b in brains:
+        if b._dirty:
+            b._syncDriven()
+    hs = (C.c_void_p * len(brains))(*[b._h for b in brains])
+    st = np.ascontiguousarray(steps, dtype=np.int32)
+    n = int(L.ob_run_many(hs, len(brains), st.ctypes.data_as(C.c_void_p), int(nthreads)))
+    for b, k in zip(brains, st.tolist()):
+        b.t += k * b.p["dt"]
+    return n
 
 
 def fv_run(model: dict, v, x, steps: int, backend: str = "port", nthreads: int = 0, kdt=None):

@@ -132,7 +132,7 @@ def test_mulberry32_stream():
     M = 0xFFFFFFFF
 
     def words(seed, n):
-        a = (seed * 2654435761) & M
+        a = int(math.fmod(float(seed) * 2654435761.0, 4294967296.0))  # JS: the product in double
         out = []
         for _ in range(n):
             a = (a + 0x6D2B79F5) & M

@@ -71,5 +71,10 @@ def test_header_constants_and_seed():
     assert c[7] == np.float32(np.exp(-0.1 / 5.0))
     assert O.seed_state(1) == 2654435761
     assert O.seed_state(0) == 1
+    # JavaScript forms seed * 2654435761 in double: above 2^53 the product is rounded (here to a
+    # multiple of 64) before >>> 0; exact integer arithmetic would give 2146089093
+    assert O.seed_state(123456789) == 2146089088
+    assert O.seed_state(1073741823) == 2714273280
+    assert O.seed_state(2097151) == 2548598351  # below 2^21 the product is exact
     assert O.n_slots(dict(delay=1.8, dt=0.1)) == 19
     assert O.n_slots(dict(delay=1.8, dt=0.5)) == 5
