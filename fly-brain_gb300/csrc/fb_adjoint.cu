@@ -320,6 +320,14 @@ __global__ void __launch_bounds__(kDB, 4) k_ckpt(const DiffDev *Ds, int32_t t, i
 // gated edge into the target's bucket. In a replay (row >= 0) the arrival's res is recorded.
 // exact32 (forward): lane 0 forms lif.c's s = f32(signW32 * res) (times the amplitude when it is
 // not 1) and skips a zero s before depressing res (src/lifdiff.js:256-272).
+// Tape entries [a0, a0 + n) of an arrival step, cut at the tape's capacity: a forward that ran out
+// of tape keeps counting offsets past it (and reports FB_EOVERFLOW when it ends), and the steps
+// after the overflow must not read beyond the entries that exist.
+__device__ __forceinline__ int64_t tape_count(const DiffDev &D, int64_t a0, int64_t a1) {
+  if (a1 > D.tapeCap) a1 = D.tapeCap;
+  return a1 > a0 ? a1 - a0 : 0;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
   __shared__ DiffDev D;
@@ -328,7 +336,7 @@ __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, 
   if (t >= D.steps || e < 0) return;
   float *resRow = row >= 0 ? D.resAt + (int64_t)row * D.maxArr : nullptr;
   const bool ex = row < 0 && D.exact32;
-  const int64_t a0 = D.tOff[e], na = D.tOff[e + 1] - a0;
+  const int64_t a0 = D.tOff[e], na = tape_count(D, a0, D.tOff[e + 1]);
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -400,7 +408,7 @@ __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) 
   const int tid = threadIdx.x;
   const int64_t base = D.tOff[t];
   if (replay) {
-    const int32_t nf = D.tForced[t];
+    const int32_t nf = (int32_t)tape_count(D, base, base + D.tForced[t]);
     for (int k = tid; k < nf; k += blockDim.x) {
       const int32_t i = D.tIdx[base + k];
       D.refr[i] = (float)(P.tRef + P.dt);
@@ -917,7 +925,7 @@ __global__ void __launch_bounds__(kDB, 4) k_barrival(const DiffDev *Ds, DP<R> P,
   const int e = t - (D.nslots - 1);
   if (t >= D.steps || e < 0) return;
   const float *resRow = D.resAt + (int64_t)row * D.maxArr;
-  const int64_t a0 = D.tOff[e], na = D.tOff[e + 1] - a0;
+  const int64_t a0 = D.tOff[e], na = tape_count(D, a0, D.tOff[e + 1]);
   const int lane = threadIdx.x & 31;
   const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -1034,7 +1042,7 @@ __global__ void k_raster(const DiffDev *Ds, int32_t steps, float *out) {
   __shared__ DiffDev D;
   load_dev(Ds, D);
   for (int t = blockIdx.x; t < steps; t += gridDim.x) {
-    const int64_t a = D.tOff[t], b = D.tOff[t + 1];
+    const int64_t a = D.tOff[t], b = a + tape_count(D, a, D.tOff[t + 1]);
     for (int64_t k = a + threadIdx.x; k < b; k += blockDim.x) {
       const int c = D.roMap[D.tIdx[k]];
       if (c >= 0) out[(int64_t)t * D.nro + c] = D.tAmp[k];
@@ -1769,6 +1777,7 @@ extern "C" int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *
     if (steps[k] < 0) return dfail(FB_EINVAL, "fb_diff_forward: steps[%d]=%d", k, steps[k]);
     maxSteps = std::max(maxSteps, steps[k]);
   }
+  b->recorded = 0;  // the previous tape is gone once this forward starts writing
   for (int k = 0; k < b->B; k++) {
     Inst &I = b->in[k];
     DiffDev &D = I.D;
@@ -1796,6 +1805,16 @@ extern "C" int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *
       if ((rc = talloc(b, &o, (size_t)(D.E + 1)))) return rc;
       D.ovf = o;
       D.ovfCap = (uint32_t)(D.E + 1);
+    }
+    // and record up to one entry per neuron and step (a neuron spikes at most once a step)
+    if (p->soft && record && D.tapeCap < (int64_t)steps[k] * N) {
+      int32_t *ti = nullptr;
+      float *ta = nullptr;
+      const int64_t cap = (int64_t)steps[k] * N;
+      if ((rc = talloc(b, &ti, (size_t)cap)) || (rc = talloc(b, &ta, (size_t)cap))) return rc;
+      D.tIdx = ti;
+      D.tAmp = ta;
+      D.tapeCap = cap;
     }
   }
   bool edits = false;

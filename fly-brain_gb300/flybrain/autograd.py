@@ -77,11 +77,12 @@ class LIFDiffFunction(torch.autograd.Function):
         return g_edge.float(), g_bias.float(), g_type.float(), None
 
 
-def lowpass_rates(raster: torch.Tensor, dt_ms: float, tau_ms: float = 20.0) -> torch.Tensor:
+def lowpass_rates(raster: torch.Tensor, dt_ms: float, tau_ms: float = 20.0, dtype=None) -> torch.Tensor:
     """Exponentially low-passed firing rates in Hz of a (steps x R) spike raster, exactly:
     r_t = a r_{t-1} + c s_t with a = exp(-dt / tau), c = (1 - a) / dt (dt in s), r_{-1} = 0.
     Evaluated blockwise in float64 as r_t = a^(t+1) r_start + c a^t sum_{k<=t} a^-k s_k, with
-    blocks short enough that a^-k stays below 1e12; differentiable through torch ops."""
+    blocks short enough that a^-k stays below 1e12; differentiable through torch ops. The result
+    has the raster's dtype unless `dtype` is given (torch.float64 keeps the double rates)."""
     a = float(np.exp(-dt_ms / tau_ms))
     c = (1 - a) / (dt_ms / 1000.0)
     T, R = raster.shape
@@ -98,37 +99,48 @@ def lowpass_rates(raster: torch.Tensor, dt_ms: float, tau_ms: float = 20.0) -> t
         rb = (a * down[:n, None]) * r[None, :] + c * down[:n, None] * cs
         out.append(rb)
         r = rb[-1]
-    return torch.cat(out).to(raster.dtype)
+    return torch.cat(out).to(dtype or raster.dtype)
 
 
-def rate_loss(dctx: DiffContext, target: torch.Tensor, edge_gain, bias, type_gain) -> torch.Tensor:
-    """MSE between the 20 ms low-pass rates of the readout raster and a target trace."""
+def rate_loss(dctx: DiffContext, target: torch.Tensor, edge_gain, bias, type_gain, dtype=None) -> torch.Tensor:
+    """MSE between the 20 ms low-pass rates of the readout raster and a target trace (in `dtype`,
+    default the raster's float32)."""
     raster = LIFDiffFunction.apply(edge_gain, bias, type_gain, dctx)
-    return ((lowpass_rates(raster, dctx.net.p["dt"]) - target) ** 2).mean()
+    r = lowpass_rates(raster, dctx.net.p["dt"], dtype=dtype)
+    return ((r - target.to(r.dtype)) ** 2).mean()
 
 
 def finite_difference_check(dctx: DiffContext, target, edge_gain, bias, type_gain, n_edge=11, n_bias=11,
-                            n_type=10, h=1e-3, seed=0, fd_precision="f64"):
-    """The adjoint's gradients of rate_loss against central finite differences, the check of
-    scripts/grad_check.mjs:69-109 applied to the three input kinds of LIFDiffFunction.
+                            n_type=10, h=1e-3, seed=0, fd_precision="f64", pool=4):
+    """The adjoint's gradients of rate_loss (evaluated in float64) against central finite
+    differences, the check of scripts/grad_check.mjs:69-109 applied to the three input kinds of
+    LIFDiffFunction.
 
-    Parameters are drawn at random among the edges and biases whose adjoint gradient is non-zero
-    (most of a large network's are exactly zero over a short window) and among the cell types.
-    The adjoint runs in the context's precision; each finite difference takes two forward passes
-    in `fd_precision` ("f64": double-precision finite differences). A row passes grad_check's
-    tolerance |g - fd| <= 1e-3 |fd| + 4e-6 |L| / h (scripts/grad_check.mjs:98). Returns the rows
-    and the maximum and median relative errors |g - fd| / |fd|."""
+    Parameters of each kind are drawn at random among the pool * n of that kind with the largest
+    adjoint gradients: in a large, sparsely active network most gradients are zero or far below
+    what a central difference can resolve (the difference is then exactly 0 and the check says
+    nothing), so the check is made where the loss actually responds. The adjoint runs in the
+    context's precision; each finite difference takes two forward passes in `fd_precision`
+    ("f64": double-precision finite differences). h is one step for every kind, or a dict
+    {"edge": .., "bias": .., "type": ..}: the network's state is float32 (as the reference's
+    Float32Array state), so a kind whose perturbation moves the loss by less than about 1e-6 of
+    itself is measured by rounding noise rather than slope and needs a larger step
+    (scripts/grad_check.mjs:82-86 picks its steps per parameter for the same reason). A row also
+    records grad_check's tolerance |g - fd| <= 1e-3 |fd| + 4e-6 |L| / h (scripts/grad_check.mjs:98).
+    Returns the rows and the maximum and median relative errors |g - fd| / |fd|."""
+    f64 = torch.float64
     for p in (edge_gain, bias, type_gain):
         p.grad = None
-    L = rate_loss(dctx, target, edge_gain, bias, type_gain)
+    L = rate_loss(dctx, target, edge_gain, bias, type_gain, dtype=f64)
     L.backward()
     grads = dict(edge=edge_gain.grad.double().cpu().numpy(), bias=bias.grad.double().cpu().numpy(),
                  type=type_gain.grad.double().cpu().numpy())
     rng = np.random.default_rng(seed)
 
     def pick(kind, n):
-        nz = np.nonzero(grads[kind] != 0)[0]
-        return [(kind, int(i)) for i in rng.choice(nz, min(n, nz.shape[0]), replace=False)]
+        a = np.abs(grads[kind])
+        top = np.argsort(-a, kind="stable")[: min(pool * n, int((a > 0).sum()))]
+        return [(kind, int(i)) for i in rng.choice(top, min(n, top.shape[0]), replace=False)]
 
     picks = pick("edge", n_edge) + pick("bias", n_bias) + pick("type", n_type)
     base = dict(edge=edge_gain.detach().clone(), bias=bias.detach().clone(), type=type_gain.detach().clone())
@@ -138,21 +150,28 @@ def finite_difference_check(dctx: DiffContext, target, edge_gain, bias, type_gai
     rows = []
     try:
         with torch.no_grad():
-            Lfd = float(rate_loss(dctx, target, base["edge"], base["bias"], base["type"]))
+            Lfd = float(rate_loss(dctx, target, base["edge"], base["bias"], base["type"], dtype=f64))
             for kind, idx in picks:
+                hk = float(h[kind]) if isinstance(h, dict) else float(h)
                 vals = []
                 for sgn in (1, -1):
                     x = {k: v.clone() for k, v in base.items()}
-                    x[kind][idx] += sgn * h
-                    vals.append(float(rate_loss(dctx, target, x["edge"], x["bias"], x["type"])))
-                fd = (vals[0] - vals[1]) / (2 * h)
+                    x[kind][idx] += sgn * hk
+                    vals.append(float(rate_loss(dctx, target, x["edge"], x["bias"], x["type"], dtype=f64)))
+                fd = (vals[0] - vals[1]) / (2 * hk)
                 a = float(grads[kind][idx])
-                ok = abs(a - fd) <= 1e-3 * abs(fd) + 4e-6 * abs(Lfd) / h
-                rows.append(dict(kind=kind, index=idx, adjoint=a, fd=fd, rel=abs(a - fd) / max(abs(fd), 1e-300), ok=ok))
+                ok = abs(a - fd) <= 1e-3 * abs(fd) + 4e-6 * abs(Lfd) / hk
+                rows.append(dict(kind=kind, index=idx, h=hk, adjoint=a, fd=fd, rel=abs(a - fd) / max(abs(fd), 1e-300),
+                                 ok=ok))
     finally:
         dctx.over.clear()
         dctx.over.update(saved)
     rel = np.array([r["rel"] for r in rows]) if rows else np.zeros(1)
-    return dict(h=h, adjoint_precision=adj_prec, fd_precision=fd_precision, loss=float(L), params=len(rows),
-                passed=int(sum(r["ok"] for r in rows)), max_rel=float(rel.max()), median_rel=float(np.median(rel)),
-                rows=rows)
+    per_kind = {}
+    for k in ("edge", "bias", "type"):
+        rk = np.array([r["rel"] for r in rows if r["kind"] == k])
+        if rk.size:
+            per_kind[k] = dict(max_rel=float(rk.max()), median_rel=float(np.median(rk)), n=int(rk.size))
+    return dict(h=h, adjoint_precision=adj_prec, fd_precision=fd_precision, loss=float(L.detach()),
+                params=len(rows), passed=int(sum(r["ok"] for r in rows)), max_rel=float(rel.max()),
+                median_rel=float(np.median(rel)), per_kind=per_kind, rows=rows)

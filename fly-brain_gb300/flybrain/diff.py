@@ -210,6 +210,10 @@ class DiffNet:
         self.h = h
         self._tape_cap = tape_cap
         self._drive_dirty = False
+        # arrays set from device tensors are not in the host record the handle is built from:
+        # a rebuilt handle (after a drive change) gets them again
+        for key, t in getattr(self, "_dev_arrays", {}).items():
+            nat.check(self.L.fb_diff_set(self.h, _FIELDS[key], C.c_void_p(t.data_ptr())))
 
     def __del__(self):
         h = getattr(self, "h", None)
@@ -235,9 +239,16 @@ class DiffNet:
         """Replace logGain / outScale / thrOffset / bias (per neuron) or edgeGain (per edge)."""
         key = {"logGain": "log_gain", "outScale": "out_scale", "thrOffset": "thr_offset",
                "bias": "bias", "edgeGain": "edge_gain"}.get(name, name)
+        if self._drive_dirty and self.h is not None:
+            self._create(self._tape_cap)  # a pending drive change rebuilds the handle: first, not after
+        if not hasattr(self, "_dev_arrays"):
+            self._dev_arrays = {}
         if hasattr(values, "data_ptr"):
-            nat.check(self.L.fb_diff_set(self.h, _FIELDS[key], C.c_void_p(values.data_ptr())))
+            t = values.detach().contiguous().clone()
+            self._dev_arrays[key] = t
+            nat.check(self.L.fb_diff_set(self.h, _FIELDS[key], C.c_void_p(t.data_ptr())))
             return
+        self._dev_arrays.pop(key, None)
         v = np.ascontiguousarray(values, np.float32)
         self.arrays[key] = v
         nat.check(self.L.fb_diff_set(self.h, _FIELDS[key], v.ctypes.data))

@@ -70,3 +70,40 @@ def test_autograd_gradients_match_finite_differences():
                 fails.append((kind, idx, a, fd, rel))
     assert not fails, fails
     assert np.abs(grads["edge"]).sum() > 0 and np.abs(grads["bias"]).sum() > 0 and np.abs(grads["type"]).sum() > 0
+
+
+def test_first_call_after_a_drive_change_uses_its_inputs():
+    """A drive change rebuilds the device network at the next forward; the edge gains, biases and
+    type gains the autograd function sets must survive it (the first call's loss equals the
+    second's), and so must arrays set from device tensors before a later rebuild."""
+    import torch
+    dctx, target, _, rng = _setup()
+    net = dctx.net
+    N, E = net.N, net.E
+    for i in rng.choice(N, 20, replace=False):
+        net.setDriveOne(int(i), 150.0)
+    eg = torch.as_tensor(rng.uniform(0.5, 1.5, E), dtype=torch.float32, device="cuda")
+    bias = torch.as_tensor(rng.uniform(-1, 1, N), dtype=torch.float32, device="cuda")
+    tg = torch.as_tensor(rng.lognormal(0, 0.3, 64), dtype=torch.float32, device="cuda")
+    with torch.no_grad():
+        first = float(_loss(dctx, target, eg, bias, tg))
+        second = float(_loss(dctx, target, eg, bias, tg))
+    assert first == second
+    # arrays set, then a drive change, then a plain forward: the rebuilt handle keeps the arrays
+    sc0 = net.forward(STEPS, seed=dctx.seed, record=False).copy()
+    net.setDriveOne(int(rng.integers(N)), 90.0)
+    net.setDriveOne(int(rng.integers(N)), 0.0)
+    net.forward(STEPS, seed=dctx.seed, record=False)
+    out = tg[dctx.cell_type].contiguous()
+    net.set_array("outScale", out)
+    net.set_array("edgeGain", eg)
+    net.set_array("bias", bias)
+    sc1 = net.forward(STEPS, seed=dctx.seed, record=False)
+    assert np.isfinite(sc0).all() and np.isfinite(sc1).all()
+    with torch.no_grad():
+        third = float(_loss(dctx, target, eg, bias, tg))
+    net.setDriveOne(int(rng.integers(N)), 120.0)
+    with torch.no_grad():
+        fourth = float(_loss(dctx, target, eg, bias, tg))
+        fifth = float(_loss(dctx, target, eg, bias, tg))
+    assert fourth == fifth and np.isfinite(third)
