@@ -665,8 +665,8 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3, prec="f32", cpu=True):
                        "K=100; MSE of 20 ms low-pass rates of 1,000 readouts vs a 0-80 Hz target; "
                        "gradients for every edge gain, bias and 64 type gains (autograd)")
     del net, dctx
-    if os.environ.get("FB_BENCH_GRAD_CHECK", "1") == "1":
-        out["grad_check"] = grad_check_full(g, idx, hz, data, prec)
+    if os.environ.get("FB_BENCH_GRAD_CHECK", "1") == "1" and cpu:
+        out["grad_check"] = grad_check_full(g, idx, hz, data)
     if cpu:
         from oracle.lifdiff_oracle import DiffProblem
         cs = int(os.environ.get("FB_CPU_ADJ_SAMPLE_STEPS", "300"))
@@ -677,32 +677,48 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3, prec="f32", cpu=True):
     return out
 
 
-def grad_check_full(g, idx, hz, data, prec, steps=500, seed=3):
-    """Gradient accuracy of this leg's arithmetic at full scale: the same network in its smooth
-    form (soft spikes, the same surrogate slope), 500 steps, the same loss through the autograd
-    function; 32 parameters (11 edge gains, 11 biases, 10 type gains, drawn among those with a
-    non-zero gradient) against central finite differences (h = 1e-3) of the forward in double."""
+def grad_check_full(g, idx, hz, data, steps=500, seed=3, n=(3, 3, 2)):
+    """Gradient accuracy at full scale: the adjoint leg's network in the smooth form
+    scripts/grad_check.mjs checks (soft spikes, its surrogate width of 1.5 mV, no adjoint clipping:
+    with the leg's steep surrogate the smooth model is silent at rest and no parameter moves the
+    loss), 500 steps, the leg's loss (in float64) through the autograd function; n = (edge gains,
+    biases, type gains) parameters drawn among the 4n of each kind with the largest gradients,
+    against central finite differences of the forward in double (steps 1e-2, 1e-1 mV and 1e-3: a
+    single edge's or neuron's smaller perturbation moves the loss by less than the float32 state
+    resolves). The float64 and the float32 adjoints are compared with the same differences;
+    tests/test_grad_check_scale_gpu.py checks 32 parameters."""
     import torch
     from flybrain.autograd import DiffContext, finite_difference_check
     from flybrain.diff import DiffNet
-    rng = np.random.default_rng(seed)
-    net = DiffNet(data, dict(ADJ_OPTS, soft=True, precision=prec, edgeGain=np.ones(g.E, np.float32),
-                             bias=np.zeros(g.N, np.float32), outScale=np.ones(g.N, np.float32)))
-    for i, h in zip(idx.tolist(), hz.tolist()):
-        net.setDriveOne(i, h)
-    readout = np.sort(rng.choice(g.N, 1000, replace=False))
-    dctx = DiffContext(net, g.cell_type, readout, steps, seed=seed)
-    target = torch.as_tensor(rng.uniform(0, 80, (1, 1000)), dtype=torch.float32, device="cuda")
+
+    def context(prec):
+        rng = np.random.default_rng(seed)
+        net = DiffNet(data, dict(ADJ_OPTS, soft=True, surrogateBeta=1.5, adjClip=0.0, precision=prec,
+                                 edgeGain=np.ones(g.E, np.float32), bias=np.zeros(g.N, np.float32),
+                                 outScale=np.ones(g.N, np.float32)))
+        for i, h in zip(idx.tolist(), hz.tolist()):
+            net.setDriveOne(i, h)
+        readout = np.sort(rng.choice(g.N, 1000, replace=False))
+        target = torch.as_tensor(rng.uniform(0, 80, (1, 1000)), dtype=torch.float32, device="cuda")
+        return DiffContext(net, g.cell_type, readout, steps, seed=seed), target
+
+    d64, target = context("f64")
+    d32, _ = context("f32")
+    rng = np.random.default_rng(seed + 1)
     eg = torch.ones(g.E, device="cuda", requires_grad=True)
     bias = torch.zeros(g.N, device="cuda", requires_grad=True)
     tg = torch.as_tensor(rng.lognormal(0, 0.2, 64), dtype=torch.float32, device="cuda").requires_grad_()
     t0 = time.perf_counter()
-    r = finite_difference_check(dctx, target, eg, bias, tg, seed=5, fd_precision="f64")
+    r = finite_difference_check(d64, target, eg, bias, tg, n_edge=n[0], n_bias=n[1], n_type=n[2],
+                                h=dict(edge=1e-2, bias=1e-1, type=1e-3), seed=5, fd_precision="f64",
+                                others={"f32": d32})
     r["seconds"] = time.perf_counter() - t0
-    r["config"] = (f"soft spikes (beta 0.04), N={g.N:,}, {steps} steps, K=100; {r['params']} parameters against "
-                   "FP64 central differences, h=1e-3; tolerance of scripts/grad_check.mjs:98")
-    r["rows"] = [dict(kind=x["kind"], index=x["index"], rel=x["rel"]) for x in r["rows"]]
-    del net, dctx
+    r["config"] = (f"soft spikes (surrogate width 1.5 mV, scripts/grad_check.mjs's), no adjoint clipping, "
+                   f"N={g.N:,}, {steps} steps, K=100; {r['params']} parameters against FP64 central differences "
+                   "(h: edge 1e-2, bias 1e-1 mV, type 1e-3); max_rel/median_rel: float64 adjoint, others.f32: "
+                   "float32 adjoint")
+    r["rows"] = [dict(kind=x["kind"], index=x["index"], rel=x["rel"], rel_f32=x["rel_f32"]) for x in r["rows"]]
+    del d64, d32
     torch.cuda.empty_cache()
     return r
 

@@ -45,6 +45,21 @@ __device__ __forceinline__ void red_release(uint32_t *p, uint32_t v) {
 
 constexpr int kMaxPer = kLagPer;
 
+// Loads issued a step or two before their values are used (the count and first-entry prefetch).
+// A plain load may be scheduled at any point before its first use, which for a prefetch can be
+// the end of the step, exposing the whole L2 latency at the next step's start; these stay where
+// they are written.
+__device__ __forceinline__ uint32_t ld_early(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint2 ld_early(const uint2 *p) {
+  uint2 v;
+  asm volatile("ld.global.cg.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p) : "memory");
+  return v;
+}
+
 struct LagShared {
   int32_t nLocal;  // neurons owned by this block
   int32_t idLo, idHi;
@@ -664,7 +679,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         nA[r] = nB[r];
-        if (nB[r]) eA[r] = ldcg(a.buf + (int64_t)slot1 * a.E + S.off[kOf(r)]);
+        if (nB[r]) eA[r] = ld_early(a.buf + (int64_t)slot1 * a.E + S.off[kOf(r)]);
       }
     }
     // step s + 2: its counts
@@ -674,7 +689,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         const int k = kOf(r);
-        nB[r] = (r < per && k < nLocal) ? ldcg(a.cnt + (int64_t)slot2 * a.cntStride + cOf(k)) : 0u;
+        nB[r] = (r < per && k < nLocal) ? ld_early(a.cnt + (int64_t)slot2 * a.cntStride + cOf(k)) : 0u;
       }
     }
 

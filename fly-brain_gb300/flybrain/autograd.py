@@ -110,8 +110,20 @@ def rate_loss(dctx: DiffContext, target: torch.Tensor, edge_gain, bias, type_gai
     return ((r - target.to(r.dtype)) ** 2).mean()
 
 
+def adjoint_gradients(dctx: DiffContext, target, edge_gain, bias, type_gain) -> dict:
+    """The adjoint's gradients of rate_loss (in float64) for the three inputs, as float64 numpy
+    arrays, and the loss."""
+    e = edge_gain.detach().clone().requires_grad_()
+    b = bias.detach().clone().requires_grad_()
+    t = type_gain.detach().clone().requires_grad_()
+    L = rate_loss(dctx, target, e, b, t, dtype=torch.float64)
+    L.backward()
+    return dict(edge=e.grad.double().cpu().numpy(), bias=b.grad.double().cpu().numpy(),
+                type=t.grad.double().cpu().numpy(), loss=float(L.detach()))
+
+
 def finite_difference_check(dctx: DiffContext, target, edge_gain, bias, type_gain, n_edge=11, n_bias=11,
-                            n_type=10, h=1e-3, seed=0, fd_precision="f64", pool=4):
+                            n_type=10, h=1e-3, seed=0, fd_precision="f64", pool=4, others=None):
     """The adjoint's gradients of rate_loss (evaluated in float64) against central finite
     differences, the check of scripts/grad_check.mjs:69-109 applied to the three input kinds of
     LIFDiffFunction.
@@ -127,7 +139,9 @@ def finite_difference_check(dctx: DiffContext, target, edge_gain, bias, type_gai
     itself is measured by rounding noise rather than slope and needs a larger step
     (scripts/grad_check.mjs:82-86 picks its steps per parameter for the same reason). A row also
     records grad_check's tolerance |g - fd| <= 1e-3 |fd| + 4e-6 |L| / h (scripts/grad_check.mjs:98).
-    Returns the rows and the maximum and median relative errors |g - fd| / |fd|."""
+    Returns the rows and the maximum and median relative errors |g - fd| / |fd|. others: named
+    further contexts (the same network in another arithmetic, say) whose adjoints are compared
+    with the same finite differences (row fields rel_<name>, summary others[<name>])."""
     f64 = torch.float64
     for p in (edge_gain, bias, type_gain):
         p.grad = None
@@ -166,6 +180,17 @@ def finite_difference_check(dctx: DiffContext, target, edge_gain, bias, type_gai
     finally:
         dctx.over.clear()
         dctx.over.update(saved)
+    extra = {}
+    for name, ctx2 in (others or {}).items():
+        g2 = adjoint_gradients(ctx2, target, base["edge"], base["bias"], base["type"])
+        rel2 = []
+        for r in rows:
+            a2 = float(g2[r["kind"]][r["index"]])
+            r["adjoint_" + name] = a2
+            r["rel_" + name] = abs(a2 - r["fd"]) / max(abs(r["fd"]), 1e-300)
+            rel2.append(r["rel_" + name])
+        rel2 = np.array(rel2) if rel2 else np.zeros(1)
+        extra[name] = dict(max_rel=float(rel2.max()), median_rel=float(np.median(rel2)))
     rel = np.array([r["rel"] for r in rows]) if rows else np.zeros(1)
     per_kind = {}
     for k in ("edge", "bias", "type"):
@@ -174,4 +199,4 @@ def finite_difference_check(dctx: DiffContext, target, edge_gain, bias, type_gai
             per_kind[k] = dict(max_rel=float(rk.max()), median_rel=float(np.median(rk)), n=int(rk.size))
     return dict(h=h, adjoint_precision=adj_prec, fd_precision=fd_precision, loss=float(L.detach()),
                 params=len(rows), passed=int(sum(r["ok"] for r in rows)), max_rel=float(rel.max()),
-                median_rel=float(np.median(rel)), per_kind=per_kind, rows=rows)
+                median_rel=float(np.median(rel)), per_kind=per_kind, others=extra, rows=rows)
