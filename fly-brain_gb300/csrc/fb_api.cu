@@ -1045,9 +1045,10 @@ static int lag_setup(fb_brains *br) {
     CU(cudaStreamSynchronize(br->stream));
     R.nD = nD;
     R.cap = std::max<int>(1, (int)((Nnd + R.nTB - 1) / R.nTB));
-    if (R.cap > kLagPer * kLagThreads || nD > kLagPer * kLagThreads)
-      return fail(FB_EINVAL, "fb_step: %d neurons per block or %d driven neurons exceed the delay-scheduled kernel's %d",
-                  R.cap, nD, kLagPer * kLagThreads);
+    if (R.cap > kLagPer * kLagTileWorkers || nD > kLagPer * kLagThreads || (nD + R.nTB - 1) / R.nTB > kLagHelpMax)
+      return fail(FB_EINVAL, "fb_step: %d neurons per block (at most %d) or %d driven neurons (at most %d) exceed "
+                  "the delay-scheduled kernel", R.cap, kLagPer * kLagTileWorkers, nD,
+                  std::min(kLagPer * kLagThreads, kLagHelpMax * R.nTB));
     const int nDcap = std::max(32, (nD + 31) / 32 * 32);
     R.smem = lagged_smem_bytes(R.cap, nDcap);
     if (lagged_blocks_per_sm(R.smem) < 1)

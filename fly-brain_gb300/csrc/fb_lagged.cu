@@ -45,6 +45,56 @@ __device__ __forceinline__ void red_release(uint32_t *p, uint32_t v) {
 
 constexpr int kMaxPer = kLagPer;
 
+// Tile blocks: warps 0 .. kTW/32 - 1 update neurons; the last two warps serve them. The
+// publisher warp releases the block's completion of each step and checks the lag for the next
+// one; the helper warp loads the next step's share of the driven block's spikes into shared
+// memory. Both do this while the workers run a step, so neither a release's wait for the block's
+// writes nor the list's L2 round trips lies on the workers' path; the workers synchronise among
+// themselves on named barrier 1 and with the service warps once per step (barrier 0).
+constexpr int kTW = kLagTileWorkers;
+constexpr int kTWarps = kTW / 32;
+constexpr int kHelpMax = kLagHelpMax;  // the host keeps ceil(driven / tile blocks) within it
+
+__device__ __forceinline__ void wbar() { asm volatile("bar.sync 1, %0;" ::"n"(kTW) : "memory"); }
+__device__ __forceinline__ bool wbar_or(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "n"(kTW)
+      : "memory");
+  return r != 0;
+}
+// Exclusive prefix over the worker threads of a tile block; *total receives their sum.
+__device__ __forceinline__ uint64_t worker_exclusive_scan(uint64_t x, uint64_t *total, uint64_t *scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  wbar();
+  if (lane == 31) scratch[warp] = inc;
+  wbar();
+  if (warp == 0) {
+    const uint64_t w = lane < kTWarps ? scratch[lane] : 0ull;
+    uint64_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < kTWarps) scratch[lane] = wi - w;
+    if (lane == 31) scratch[32] = wi;
+  }
+  wbar();
+  const uint64_t res = scratch[warp] + inc - x;
+  *total = scratch[32];
+  wbar();
+  return res;
+}
+
 // Loads issued a step or two before their values are used (the count and first-entry prefetch).
 // A plain load may be scheduled at any point before its first use, which for a prefetch can be
 // the end of the step, exposing the whole L2 latency at the next step's start; these stay where
@@ -86,6 +136,11 @@ struct LagShared {
   int32_t nbgP[2];
   float bgAccP[2];
   uint32_t dbCnt2[2];
+  // tile blocks, by step parity: the service warps' verdicts for the step and the helper warp's
+  // share of the driven block's spikes ({row start, row end, rank key, amplitude})
+  int32_t stopQ[2];
+  int32_t helpN[2];
+  uint4 help[2][kHelpMax];
 };
 
 
@@ -386,15 +441,18 @@ __device__ __forceinline__ void emit(const LagArgs &a, const LagState &S, int k,
 }
 
 // Background targets of the step that fall on this block's neurons: a hit count per neuron.
+template <bool kWorkers>
 __device__ void collect_bg(const LagArgs &a, LagShared &sh, const LagState &S, uint32_t *sBg, int s,
                            bool driven) {
   const int nbg = ldcg(a.bgCount + (s & (kLagRing - 1)));
   const uint32_t *list = a.bgList + (int64_t)(s & (kLagRing - 1)) * a.bgCap;
+  const int nT = kWorkers ? kTW : (int)blockDim.x;
   for (int c0 = 0; c0 < nbg; c0 += kBgChunk) {
     const int m = min(kBgChunk, nbg - c0);
-    for (int k = threadIdx.x; k < m; k += blockDim.x) sBg[k] = ldcg(list + c0 + k);
-    __syncthreads();
-    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    for (int k = threadIdx.x; k < m; k += nT) sBg[k] = ldcg(list + c0 + k);
+    if (kWorkers) wbar();
+    else __syncthreads();
+    for (int k = threadIdx.x; k < m; k += nT) {
       const int32_t x = (int32_t)sBg[k];
       if (driven) {  // the target's place in the driven list, if driven
         const int32_t p = __ldg(a.drvPosOf + x);
@@ -410,7 +468,8 @@ __device__ void collect_bg(const LagArgs &a, LagShared &sh, const LagState &S, u
       }
       if (lo < sh.nLocal && S.id[lo] == x) atomicAdd(S.hits + lo, 1u);
     }
-    __syncthreads();
+    if (kWorkers) wbar();
+    else __syncthreads();
   }
 }
 
@@ -585,9 +644,9 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   }
 
   // ---------------- the steps ----------------
-  // this thread's neurons: k = tid + r * kLB (r < per); for the driven block the list in order,
+  // driven block: this thread's entries are k = tid + r * kLB (r < per), the list in order,
   // round by round
-  const int per = drivenBlock ? a.m : (nLocal + kLB - 1) / kLB;
+  const int per = a.m;
   auto kOf = [&](int r) { return tid + r * kLB; };
   // count slot of local neuron k: driven neurons have their own slots after the N neuron ids
   auto cOf = [&](int k) { return drivenBlock ? (uint32_t)(a.N + k) : (uint32_t)S.id[k]; };
@@ -597,12 +656,12 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   uint32_t nA[kMaxPer], nB[kMaxPer];
   uint2 eA[kMaxPer];
   bool haveA = false, haveB = false;
-  uint32_t dbKnown = 0;     // tile blocks: driven-block steps known finished (thread 0)
   uint64_t tp = a.prof != nullptr ? global_ns() : 0;
-  const int pb = drivenBlock ? 0 : 5;  // phase slots of this block
+  const int pb = 0;                    // phase slots of the driven block (tile blocks: 5 ..)
   int sEnd = a.T;                      // the steps run (fewer after a failed wait)
   const int publisher = (int)blockDim.x - 64;
-  for (int s = 0; s < a.T; s++) {
+  if (drivenBlock) {
+   for (int s = 0; s < a.T; s++) {
     const int slot = s % a.S;
     const int ring = s & (kLagRing - 1);
     // lag: every block has finished step s - L (and, for the background, the driven block has
@@ -623,10 +682,6 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
           if (ok) sh.known = need;
         }
       }
-      if (ok && !drivenBlock && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s + 1));
-      // test hook: a wait that nothing satisfies (the driven block's progress word never reaches
-      // 2^32 - 1), so it runs out after timeoutNs and the launch ends with FB_ETIMEOUT
-      if (ok && s == a.tripStep && blockIdx.x == 1) ok = wait_geq(a, a.dbDone, 0xffffffffu);
       sh.stopP[s & 1] = ok ? 0 : 1;
     }
     __syncthreads();
@@ -641,7 +696,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     // one warp that warp set the driven block's pace, 4.65 against 4.26 us per step)
     if ((int)tid == publisher && s > 0) {
       const int sp = s - 1;
-      if (drivenBlock) {
+      {
         const uint32_t n = sh.dbCnt2[sp & 1];
         sh.dbCnt2[sp & 1] = 0;
         a.dbCnt[sp & (kLagRing - 1)] = (int32_t)n;
@@ -651,8 +706,6 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         // these spikes `help` steps later
         if (s % a.dbPub == 0) st_release(a.dbDone, (uint32_t)s);
         atomicAdd(a.done + (sp & (kLagRing - 1)), 1u);  // the driven block pushes nothing itself
-      } else {
-        red_release(a.done + (sp & (kLagRing - 1)), 1u);
       }
       if ((sp & 3) == 3) {  // now and then: a later step known finished everywhere, which keeps
         // the count prefetch two steps ahead going (it needs step s + 2 - L finished)
@@ -693,7 +746,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       }
     }
 
-    if (drivenBlock) {
+    {
       const int par = s & 1, parN = par ^ 1;
       const int m = a.m;
       const uint32_t nbg = (uint32_t)sh.nbgP[par], s0 = sh.rngP[par];
@@ -704,7 +757,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
           a.bgList[(int64_t)ring * a.bgCap + d - 1] = xs_jump_hex(sHex, s0, (uint32_t)d) % (uint32_t)a.N;
         __syncthreads();
         if (tid == 0) st_release(a.bgReady, (uint32_t)(s + 1));
-        collect_bg(a, sh, S, sBg, s, true);
+        collect_bg<false>(a, sh, S, sBg, s, true);
       }
       // each warp's first draw among the step's live entries, from the ballots taken at the end
       // of the last step: (live entries of earlier rounds) + (live entries of earlier warps)
@@ -782,87 +835,193 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       // the next step's live entries (the count is published at the next step's start)
       driven_ballots(a, sh, S, parN);
       lap(a, 4, tp);
-      continue;
-    }
-
-    // ---------------- tile block ----------------
-    if (a.hasBg) collect_bg(a, sh, S, sBg, s, false);
-    uint64_t flags = 0;  // bit 16 r: neuron r of this thread crossed the threshold
-#pragma unroll
-    for (int r = 0; r < kMaxPer; r++) {
-      const int k = kOf(r);
-      if (r < per && k < nLocal) {
-        receive(a, S, k, nCur[r], (uint32_t)S.id[k], slot, haveE, eCur[r]);
-        const bool f = integrate(a, S, k);
-        emit(a, S, k, f);
-        if (f) flags |= (uint64_t)1 << (16 * r);
       }
-    }
-    // compaction in ascending local index: neurons r = 0 (k = tid) first, then r = 1, ...
-    uint32_t fired = 0;
-    if (__syncthreads_or(flags != 0)) {
-      uint64_t tot;
-      const uint64_t pos = block_exclusive_scan(flags, &tot, sh.scan64);
-      int32_t *st = a.tStage + ((int64_t)ring * a.nTB + b) * a.cap;
-      uint32_t before = 0;
-#pragma unroll
-      for (int r = 0; r < kMaxPer; r++) {
-        const uint32_t c = (uint32_t)(tot >> (16 * r)) & 0xffffu;
-        if ((flags >> (16 * r)) & 1u) st[before + ((uint32_t)(pos >> (16 * r)) & 0xffffu)] = kOf(r);
-        before += c;
+  }
+  } else {
+    // ---------------- tile blocks ----------------
+    const int lane = tid & 31, warp = tid >> 5;
+    const int perT = (nLocal + kTW - 1) / kTW;
+    auto kT = [&](int r) { return tid + r * kTW; };
+    auto mineT = [&](int r) { return tid < kTW && r < perT && kT(r) < nLocal; };
+    // the lag check for step s1 (publisher lane): every block has finished step s1 + ahead - L so
+    // the counts prefetched two steps ahead are final (this block's completion is published up
+    // to s1 - 2 when the check runs); the background draws of step s1 are published
+    auto lag_ok = [&](int s1) -> bool {
+      bool ok = true;
+      const int need = s1 + min(2, a.L - 2) - a.L;
+      if (need >= 0 && sh.known < need) {
+        const int far = min(need + 4, s1 - 2);
+        if (far > need && ld_acquire(a.done + (far & (kLagRing - 1))) >= done_target(far, gridDim.x)) {
+          sh.known = far;
+        } else {
+          ok = wait_geq(a, a.done + (need & (kLagRing - 1)), done_target(need, gridDim.x));
+          if (ok) sh.known = need;
+        }
       }
-      fired = before;
-    }
-    lap(a, 6, tp);
-    // own spikes into the slot of step s + D: their 32-edge chunks dealt round-robin over the
-    // block's warps, so a large row is spread over the block
-    const uint32_t warp = tid >> 5, nwarps = blockDim.x >> 5;
-    if (fired) {
-      __syncthreads();
-      const int32_t *st = a.tStage + ((int64_t)ring * a.nTB + b) * a.cap;
-      uint32_t base = 0;
-      for (uint32_t f = 0; f < fired; f++) {
-        const int k = ldcg(st + f);
-        const uint32_t lo = S.row0[k], hi = S.row1[k];
-        push_edges(a, lo, hi, (uint32_t)(a.nD + S.id[k]), S.amp[k], (s + a.D) % a.S,
-                   (warp + nwarps - base % nwarps) % nwarps, nwarps);
-        base += (hi - lo + 31) / 32;
+      if (ok && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s1 + 1));
+      // test hook: a wait that nothing satisfies (the driven block's progress word never reaches
+      // 2^32 - 1), so it runs out after timeoutNs and the launch ends with FB_ETIMEOUT
+      if (ok && s1 == a.tripStep && blockIdx.x == 1) ok = wait_geq(a, a.dbDone, 0xffffffffu);
+      return ok;
+    };
+    // the driven block's spikes of step s1 - help that fall to this block (spike e goes to tile
+    // block (e + 61 sp) mod nTB: the assignment rotates, so no block carries a push every step),
+    // one per lane of the helper warp, into the shared list of step s1's parity
+    uint32_t dbKnown = 0;  // helper warp, lane 0: driven-block steps known released
+    auto help_load = [&](int s1) -> bool {
+      const int par1 = s1 & 1;
+      int n = 0;
+      bool ok = true;
+      if (s1 >= a.help && s1 < a.T) {
+        const int sp = s1 - a.help, rp = sp & (kLagRing - 1);
+        if (lane == 0 && dbKnown < (uint32_t)(sp + 1)) ok = wait_geq(a, a.dbDone, (uint32_t)(sp + 1), &dbKnown);
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (ok) {
+          const int nsp = ldcg(a.dbCnt + rp);
+          int e0 = b - (int)(((int64_t)sp * 61) % a.nTB);
+          if (e0 < 0) e0 += a.nTB;
+          n = nsp > e0 ? (nsp - e0 + a.nTB - 1) / a.nTB : 0;
+          if (n > kHelpMax) {
+            if (lane == 0) atomicCAS(a.err, 0, FB_EOVERFLOW);
+            n = kHelpMax;
+          }
+          if (lane < n) {
+            const int e = e0 + lane * a.nTB;
+            const uint4 x = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2);
+            const uint4 row = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2 + 1);
+            sh.help[par1][lane] = make_uint4(row.x, row.y, x.y, x.z);
+          }
+        }
       }
-    }
-    lap(a, 7, tp);
-    // the driven block's spikes of step s - help, shared out over the tile blocks
-    if (s >= a.help) {
-      const int sp = s - a.help, rp = sp & (kLagRing - 1);
-      if (tid == 0) {
-        bool ok = true;
-        if (dbKnown < (uint32_t)(sp + 1)) ok = wait_geq(a, a.dbDone, (uint32_t)(sp + 1), &dbKnown);
-        sh.stop = ok ? 0 : 1;
+      if (lane == 0) {
+        sh.helpN[par1] = n;
+        sh.stopQ[par1] = ok ? 0 : 1;
       }
-      __syncthreads();
-      if (sh.stop) {
+      return ok;
+    };
+    if (warp == kTWarps && lane == 0) sh.stopP[0] = lag_ok(0) ? 0 : 1;
+    if (warp == kTWarps + 1) help_load(0);
+    uint32_t nA[kMaxPer], nB[kMaxPer];
+    uint2 eA[kMaxPer];
+    bool haveA = false, haveB = false;
+    uint64_t tp = a.prof != nullptr ? global_ns() : 0;
+    for (int s = 0; s < a.T; s++) {
+      const int slot = s % a.S;
+      const int ring = s & (kLagRing - 1);
+      const int par = s & 1;
+      __syncthreads();  // the workers finished step s - 1; the service warps prepared step s
+      if (sh.stopP[par] | sh.stopQ[par]) {
         sEnd = s;
         break;
       }
-      // spike e goes to tile block (e + 61 sp) mod nTB: the assignment rotates from step to
-      // step, so no block carries a push every step; its chunks are dealt over the block's warps
-      const int nsp = ldcg(a.dbCnt + rp);
-      int e0 = b - (int)(((int64_t)sp * 61) % a.nTB);
-      if (e0 < 0) e0 += a.nTB;
-      uint32_t base = 0;
-      for (int e = e0; e < nsp; e += a.nTB) {
-        const uint4 x = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2);
-        const uint4 row = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2 + 1);
-        push_edges(a, row.x, row.y, x.y, __uint_as_float(x.z), (sp + a.D) % a.S,
-                   (warp + nwarps - base % nwarps) % nwarps, nwarps);
-        base += (row.y - row.x + 31) / 32;
+      if (warp == kTWarps) {  // publisher: step s - 1 complete, then the lag for step s + 1
+        if (lane == 0) {
+          if (s > 0) {
+            const int sp = s - 1;
+            red_release(a.done + (sp & (kLagRing - 1)), 1u);
+            if ((sp & 3) == 3) {  // now and then: a later step known finished everywhere
+              const int probe = sp - 5;
+              if (probe > sh.known && ld_acquire(a.done + (probe & (kLagRing - 1))) >= done_target(probe, gridDim.x))
+                sh.known = probe;
+            }
+          }
+          if (s + 1 < a.T) sh.stopP[par ^ 1] = lag_ok(s + 1) ? 0 : 1;
+        }
+        continue;
       }
+      if (warp == kTWarps + 1) {  // helper: the next step's share of the driven spikes
+        help_load(s + 1);
+        continue;
+      }
+      lap(a, 5, tp);
+      // this step's counts and first entries (prefetched when the lag allowed it)
+      uint32_t nCur[kMaxPer];
+      uint2 eCur[kMaxPer];
+      const bool haveE = haveA;
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        nCur[r] = haveA ? nA[r] : (mineT(r) ? ldcg(a.cnt + (int64_t)slot * a.cntStride + S.id[kT(r)]) : 0u);
+        eCur[r] = eA[r];
+      }
+      haveA = haveB && s + 1 < a.T;
+      if (haveA) {
+        const int slot1 = (s + 1) % a.S;
+#pragma unroll
+        for (int r = 0; r < kMaxPer; r++) {
+          nA[r] = nB[r];
+          if (nB[r]) eA[r] = ld_early(a.buf + (int64_t)slot1 * a.E + S.off[kT(r)]);
+        }
+      }
+      haveB = s + 2 < a.T && *(volatile int32_t *)&sh.known >= s + 2 - a.L;
+      if (haveB) {
+        const int slot2 = (s + 2) % a.S;
+#pragma unroll
+        for (int r = 0; r < kMaxPer; r++)
+          nB[r] = mineT(r) ? ld_early(a.cnt + (int64_t)slot2 * a.cntStride + S.id[kT(r)]) : 0u;
+      }
+      if (a.hasBg) collect_bg<true>(a, sh, S, sBg, s, false);
+      uint64_t flags = 0;  // bit 16 r: neuron r of this thread crossed the threshold
+#pragma unroll
+      for (int r = 0; r < kMaxPer; r++) {
+        if (mineT(r)) {
+          const int k = kT(r);
+          receive(a, S, k, nCur[r], (uint32_t)S.id[k], slot, haveE, eCur[r]);
+          const bool f = integrate(a, S, k);
+          emit(a, S, k, f);
+          if (f) flags |= (uint64_t)1 << (16 * r);
+        }
+      }
+      // compaction in ascending local index: neurons r = 0 (k = tid) first, then r = 1, ...
+      uint32_t fired = 0;
+      if (wbar_or(flags != 0)) {
+        uint64_t tot;
+        const uint64_t pos = worker_exclusive_scan(flags, &tot, sh.scan64);
+        int32_t *st = a.tStage + ((int64_t)ring * a.nTB + b) * a.cap;
+        uint32_t before = 0;
+#pragma unroll
+        for (int r = 0; r < kMaxPer; r++) {
+          const uint32_t c = (uint32_t)(tot >> (16 * r)) & 0xffffu;
+          if ((flags >> (16 * r)) & 1u) st[before + ((uint32_t)(pos >> (16 * r)) & 0xffffu)] = kT(r);
+          before += c;
+        }
+        fired = before;
+      }
+      lap(a, 6, tp);
+      // own spikes into the slot of step s + D: their 32-edge chunks dealt round-robin over the
+      // worker warps, so a large row is spread over the block
+      const uint32_t nw = kTWarps;
+      if (fired) {
+        wbar();
+        const int32_t *st = a.tStage + ((int64_t)ring * a.nTB + b) * a.cap;
+        uint32_t base = 0;
+        for (uint32_t f = 0; f < fired; f++) {
+          const int k = ldcg(st + f);
+          const uint32_t lo = S.row0[k], hi = S.row1[k];
+          push_edges(a, lo, hi, (uint32_t)(a.nD + S.id[k]), S.amp[k], (s + a.D) % a.S,
+                     ((uint32_t)warp + nw - base % nw) % nw, nw);
+          base += (hi - lo + 31) / 32;
+        }
+      }
+      lap(a, 7, tp);
+      // the driven block's spikes of step s - help that fall to this block (listed by the helper
+      // warp during the last step)
+      if (s >= a.help) {
+        const int sp = s - a.help;
+        const int n = sh.helpN[par];
+        uint32_t base = 0;
+        for (int j = 0; j < n; j++) {
+          const uint4 h = sh.help[par][j];
+          push_edges(a, h.x, h.y, h.z, __uint_as_float(h.w), (sp + a.D) % a.S,
+                     ((uint32_t)warp + nw - base % nw) % nw, nw);
+          base += (h.y - h.x + 31) / 32;
+        }
+      }
+      if (tid == 0) {
+        a.tCnt[(int64_t)ring * a.nTB + b] = (int32_t)fired;
+        if (a.log && fired) atomicAdd(a.stepTot + s, (int32_t)fired);
+      }
+      lap(a, 8, tp);
     }
-    if (tid == 0) {
-      a.tCnt[(int64_t)ring * a.nTB + b] = (int32_t)fired;
-      if (a.log && fired) atomicAdd(a.stepTot + s, (int32_t)fired);
-    }
-    __syncthreads();
-    lap(a, 8, tp);
   }
 
   // ---------------- epilogue ----------------

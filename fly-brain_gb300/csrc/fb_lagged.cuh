@@ -9,13 +9,16 @@ namespace fb {
 constexpr int kLagRing = 64;  // ring depth of the per-step counters and lists (a power of two)
 constexpr int kLagThreads = 1024;  // threads per block
 constexpr int kLagPer = 2;        // neurons per thread at most (tile and driven blocks)
-// The tile blocks push the driven block's spikes `help` steps late. With a delay of at least
-// kLagPairDelay steps the driven block releases its spike lists every other step (the release
-// holds up its warp about as long as the rest of a step) and help = 3; otherwise every step and
-// help = 2. The lag bound is L = D - help >= 2 (a block's own completion of step s - 1 is
-// published at step s, after its wait).
+constexpr int kLagTileWorkers = kLagThreads - 64;  // tile-block threads that update neurons
+constexpr int kLagHelpMax = 32;   // driven spikes of one step a tile block pushes at most
+// The tile blocks push the driven block's spikes `help` steps late (their helper warp lists a
+// step's share one step before the workers push it). The driven block releases its spike lists
+// every help - 1 steps (the release holds up its warp about as long as the rest of a step): with a
+// delay of at least 8 steps help = 4, from kLagPairDelay steps 3, otherwise 2. The lag bound is
+// L = D - help >= 2 (a block's own completion of step s - 1 is published at step s, before it
+// checks the lag of step s + 1).
 constexpr int kLagPairDelay = 6;
-inline int lag_help(int D) { return D >= kLagPairDelay ? 3 : 2; }
+inline int lag_help(int D) { return D >= 8 ? 4 : D >= kLagPairDelay ? 3 : 2; }
 
 struct LagArgs {
   Trial *G;  // the brain's device header: scalars are written back at the end
