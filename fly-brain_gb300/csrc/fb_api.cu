@@ -405,6 +405,8 @@ struct LagRes {
   int32_t *bgCount = nullptr, *dbCnt = nullptr, *dbNF = nullptr, *tStage = nullptr, *tCnt = nullptr;
   int32_t *ndIds = nullptr, *ndLo = nullptr, *drvPosOf = nullptr;
   int cap = 1, nD = 0;
+  int nDB = 1, nDcap = 32, nDall = 32, dLo[kLagMaxDB + 1] = {0, 0, 0};
+  unsigned long long *liveTag = nullptr;
   size_t smem = 0;
 };
 
@@ -450,6 +452,7 @@ struct fb_brains {
   int32_t subGrab = 4;
   int64_t timeoutNs = 5000000000LL;  // bound of every device-side wait (fb_tuning.timeout_us)
   int32_t tripStep = -1;             // test hook (fb_debug_trip_wait): armed for one launch
+  int32_t lagDB = 0;                 // driven blocks of the delay-scheduled kernel (0: automatic)
   int logging = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float lastMs = 0.f;
@@ -678,6 +681,12 @@ extern "C" int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t) {
     return fail(FB_EINVAL, "fb_brains_set_tuning: blocks_per_sm %d (1..%d), item_chunks %d (1..64), sub_grab %d (-1, 1..256), "
                 "timeout_us %d (>= 1)", t->blocks_per_sm, br->maxBlocksPerSm, t->item_chunks, t->sub_grab, t->timeout_us);
   if (t->timeout_us) br->timeoutNs = (int64_t)t->timeout_us * 1000;
+  if (t->lag_driven_blocks < 0 || t->lag_driven_blocks > kLagMaxDB)
+    return fail(FB_EINVAL, "fb_brains_set_tuning: lag_driven_blocks %d (0 automatic, 1..%d)", t->lag_driven_blocks, kLagMaxDB);
+  if (t->lag_driven_blocks != br->lagDB) {
+    br->lagDB = t->lag_driven_blocks;
+    br->lag.drivenVersion = ~0ull;  // the ownership is recomputed at the next launch
+  }
   if (t->blocks_per_sm) {
     br->blocksPerSm = t->blocks_per_sm;
     br->grid = br->sms * br->blocksPerSm;
@@ -693,6 +702,8 @@ extern "C" int fb_brains_tuning(fb_brains *br, fb_tuning *t) {
   t->item_chunks = br->itemChunks;
   t->sub_grab = br->subGrab ? br->subGrab : -1;
   t->timeout_us = (int32_t)std::min<int64_t>(br->timeoutNs / 1000, 0x7fffffff);
+  t->lag_driven_blocks = br->lagDB;
+  t->pad = 0;
   t->max_blocks_per_sm = br->maxBlocksPerSm;
   t->sms = br->sms;
   return FB_OK;
@@ -990,11 +1001,13 @@ static int lag_setup(fb_brains *br) {
     R.nTB = sms - 1;
     R.D = T.nslots - 1;
     R.S = 2 * R.D;
-    R.capMax = std::max(1, (N + R.nTB - 1) / R.nTB);
-    R.nDmax = 0;
-    for (int nd = 32; nd <= 8192; nd += 32)
-      if (lagged_smem_bytes(R.capMax, nd) <= (size_t)optin) R.nDmax = nd;
-    if (R.nDmax == 0) return fail(FB_EINVAL, "fb_step: the delay-scheduled kernel does not fit in shared memory");
+    // tile blocks hold at most ceil(N / (sms - kLagMaxDB)) neurons (the fewest tile blocks)
+    R.capMax = std::max(1, (N + sms - kLagMaxDB - 1) / (sms - kLagMaxDB));
+    int perDB = 0;  // driven entries one driven block holds at most
+    for (int nd = 32; nd <= kLagPer * kLagThreads; nd += 32)
+      if (lagged_smem_bytes(R.capMax, nd, kLagMaxDB * nd) <= (size_t)optin) perDB = nd;
+    if (perDB == 0) return fail(FB_EINVAL, "fb_step: the delay-scheduled kernel does not fit in shared memory");
+    R.nDmax = kLagMaxDB * perDB;
     // in-degree prefix: each target's bucket entries start at inOff[q]
     std::vector<uint32_t> ix(E), off(N + 1, 0);
     if (E) CU(cudaMemcpy(ix.data(), T.indices, E * 4, cudaMemcpyDeviceToHost));
@@ -1003,10 +1016,12 @@ static int lag_setup(fb_brains *br) {
     if ((rc = lag_alloc(br, &R.inOff, N + 1)) || (rc = lag_alloc(br, &R.cnt, (size_t)R.S * (N + R.nDmax))) ||
         (rc = lag_alloc(br, &R.buf, (size_t)R.S * std::max<int64_t>(E, 1))) || (rc = lag_alloc(br, &R.pend0, N)) ||
         (rc = lag_alloc(br, &R.sync, 256)) || (rc = lag_alloc(br, &R.bgCount, kLagRing)) ||
-        (rc = lag_alloc(br, &R.dbList, (size_t)kLagRing * R.nDmax * 2)) || (rc = lag_alloc(br, &R.dbCnt, kLagRing)) ||
-        (rc = lag_alloc(br, &R.dbNF, kLagRing)) || (rc = lag_alloc(br, &R.tStage, (size_t)kLagRing * R.nTB * R.capMax)) ||
-        (rc = lag_alloc(br, &R.tCnt, (size_t)kLagRing * R.nTB)) || (rc = lag_alloc(br, &R.ndIds, N)) ||
-        (rc = lag_alloc(br, &R.ndLo, R.nTB + 1)) || (rc = lag_alloc(br, &R.drvPosOf, N)) || (rc = lag_alloc(br, &R.edgeRec, std::max<int64_t>(E, 1))))
+        (rc = lag_alloc(br, &R.dbList, (size_t)kLagRing * R.nDmax * 2)) ||
+        (rc = lag_alloc(br, &R.dbCnt, (size_t)kLagRing * kLagMaxDB)) ||
+        (rc = lag_alloc(br, &R.liveTag, (size_t)kLagRing * kLagMaxDB)) ||
+        (rc = lag_alloc(br, &R.dbNF, kLagRing)) || (rc = lag_alloc(br, &R.tStage, (size_t)kLagRing * R.grid * R.capMax)) ||
+        (rc = lag_alloc(br, &R.tCnt, (size_t)kLagRing * R.grid)) || (rc = lag_alloc(br, &R.ndIds, N)) ||
+        (rc = lag_alloc(br, &R.ndLo, R.grid + 1)) || (rc = lag_alloc(br, &R.drvPosOf, N)) || (rc = lag_alloc(br, &R.edgeRec, std::max<int64_t>(E, 1))))
       return rc;
     CU(cudaMemcpy(R.inOff, off.data(), (N + 1) * 4, cudaMemcpyHostToDevice));
     std::vector<uint32_t> tab;
@@ -1034,6 +1049,14 @@ static int lag_setup(fb_brains *br) {
     for (int i = 0; i < N; i++)
       if (!isD[i]) nd.push_back(i);
     const int64_t Nnd = (int64_t)nd.size();
+    // a long driven list is split over two driven blocks in list order (their draws stay in
+    // lif.c's order: each offsets its own by the other's share); the other SMs are tile blocks
+    R.nDB = br->lagDB ? br->lagDB : nD >= kLagSplit ? 2 : 1;
+    if (R.nDB > 1 && nD < R.nDB) R.nDB = 1;  // every driven block owns at least one entry
+    R.nTB = R.grid - R.nDB;
+    for (int d = 0; d <= R.nDB; d++) R.dLo[d] = (int)((int64_t)nD * d / R.nDB);
+    int part = 0;
+    for (int d = 0; d < R.nDB; d++) part = std::max(part, R.dLo[d + 1] - R.dLo[d]);
     std::vector<int32_t> lo(R.nTB + 1);
     for (int t = 0; t <= R.nTB; t++) lo[t] = (int32_t)(Nnd * t / R.nTB);
     std::vector<int32_t> posOf(N, -1);
@@ -1045,12 +1068,14 @@ static int lag_setup(fb_brains *br) {
     CU(cudaStreamSynchronize(br->stream));
     R.nD = nD;
     R.cap = std::max<int>(1, (int)((Nnd + R.nTB - 1) / R.nTB));
-    if (R.cap > kLagPer * kLagTileWorkers || nD > kLagPer * kLagThreads || (nD + R.nTB - 1) / R.nTB > kLagHelpMax)
-      return fail(FB_EINVAL, "fb_step: %d neurons per block (at most %d) or %d driven neurons (at most %d) exceed "
-                  "the delay-scheduled kernel", R.cap, kLagPer * kLagTileWorkers, nD,
-                  std::min(kLagPer * kLagThreads, kLagHelpMax * R.nTB));
-    const int nDcap = std::max(32, (nD + 31) / 32 * 32);
-    R.smem = lagged_smem_bytes(R.cap, nDcap);
+    if (R.cap > std::min(R.capMax, kLagPer * kLagTileWorkers) || part > kLagPer * kLagThreads ||
+        (nD + R.nTB - 1) / R.nTB > kLagHelpMax)
+      return fail(FB_EINVAL, "fb_step: %d neurons per tile block (at most %d) or %d driven neurons per driven block "
+                  "(at most %d) exceed the delay-scheduled kernel", R.cap, std::min(R.capMax, kLagPer * kLagTileWorkers),
+                  part, kLagPer * kLagThreads);
+    R.nDcap = std::max(32, (part + 31) / 32 * 32);
+    R.nDall = std::max(32, (nD + 31) / 32 * 32);
+    R.smem = lagged_smem_bytes(R.cap, R.nDcap, R.nDall);
     if (lagged_blocks_per_sm(R.smem) < 1)
       return fail(FB_EINVAL, "fb_step: the delay-scheduled kernel does not fit on an SM (%zu bytes)", R.smem);
     R.drivenVersion = ds.version;
@@ -1066,6 +1091,7 @@ static int run_lagged(fb_brains *br, int32_t steps) {
   CU(cudaMemsetAsync(R.sync, 0, 256 * 4, br->stream));
   CU(cudaMemsetAsync(R.cnt, 0, (size_t)R.S * (N + R.nDmax) * 4, br->stream));
   CU(cudaMemsetAsync(R.pend0, 0, (size_t)N * 4, br->stream));
+  CU(cudaMemsetAsync(R.liveTag, 0, sizeof(unsigned long long) * kLagRing * kLagMaxDB, br->stream));
   LagArgs a;
   memset(&a, 0, sizeof a);
   a.G = br->trials;
@@ -1080,8 +1106,10 @@ static int run_lagged(fb_brains *br, int32_t steps) {
   a.nTB = R.nTB;
   a.cap = R.cap;
   a.nD = R.nD;
-  a.nDcap = std::max(32, (R.nD + 31) / 32 * 32);
-  a.m = (R.nD + kLagThreads - 1) / kLagThreads;
+  a.nDcap = R.nDcap;
+  a.nDall = R.nDall;
+  a.nDB = R.nDB;
+  for (int d = 0; d <= kLagMaxDB; d++) a.dLo[d] = R.dLo[std::min(d, R.nDB)];
   a.hasBg = T.bgEvents > 0 ? 1 : 0;
   a.bgCap = R.bgCap;
   a.dt = T.dt; a.vRest = T.vRest; a.vThresh = T.vThresh; a.vReset = T.vReset; a.tRef = T.tRef;
@@ -1094,7 +1122,8 @@ static int run_lagged(fb_brains *br, int32_t steps) {
   a.ring = T.ring; a.ringCount = T.ringCount; a.driven = T.driven;
   a.ndIds = R.ndIds; a.ndLo = R.ndLo; a.drvPosOf = R.drvPosOf;
   a.cnt = R.cnt; a.cntStride = N + R.nDmax; a.buf = R.buf; a.pend0 = R.pend0;
-  a.done = R.sync; a.dbDone = R.sync + 64; a.bgReady = R.sync + 65; a.barCount = R.sync + 128;
+  a.done = R.sync; a.dbDone = R.sync + 64; a.bgReady = R.sync + 72; a.barCount = R.sync + 128;
+  a.liveTag = R.liveTag;
   a.stepTot = (int32_t *)(R.sync + 192);
   a.bgList = R.bgList; a.bgCount = R.bgCount; a.dbList = R.dbList; a.dbCnt = R.dbCnt;
   a.tStage = R.tStage; a.tCnt = R.tCnt;

@@ -112,6 +112,8 @@ __device__ __forceinline__ uint2 ld_early(const uint2 *p) {
 
 struct LagShared {
   int32_t nLocal;  // neurons owned by this block
+  int32_t dLo;     // driven block: list position of its first entry
+  int32_t m;       // driven block: entries per thread
   int32_t idLo, idHi;
   int32_t stop;
   int32_t stopP[2];  // the lag check's verdict, by step parity (the driven block's steps have one
@@ -131,7 +133,7 @@ struct LagShared {
   // update), the generator at the step's start, its states at every 32nd driven draw, the
   // background draws, the accumulator after them, and the step's spike count.
   uint32_t wcnt[2][kMaxPer * 32];
-  uint32_t cst[2][kMaxPer * kLagThreads / 32];
+  uint32_t cst[2][kLagMaxDB * kMaxPer * kLagThreads / 32];  // every 32nd draw of the whole list
   uint32_t rngP[2];
   int32_t nbgP[2];
   float bgAccP[2];
@@ -191,6 +193,31 @@ __device__ __forceinline__ bool wait_geq(const LagArgs &a, const uint32_t *p, ui
       if (lag_timeout(a, t0, it)) return false;
   }
   if (seen) *seen = v;
+  return true;
+}
+
+// A driven block's count of live entries at step s (its share of the step's draws), published
+// as one word (s + 1) << 32 | count: the step tag makes the value self-describing, so neither side
+// needs a fence.
+__device__ __forceinline__ void live_put(const LagArgs &a, int s, int d, uint32_t n) {
+  const unsigned long long v = ((unsigned long long)(uint32_t)(s + 1) << 32) | n;
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(a.liveTag + (s & (kLagRing - 1)) * kLagMaxDB + d), "l"(v)
+               : "memory");
+}
+// Driven block d's count for step s; false on a timeout or a recorded error.
+__device__ __forceinline__ bool live_get(const LagArgs &a, int s, int d, uint32_t &n) {
+  const unsigned long long *p = a.liveTag + (s & (kLagRing - 1)) * kLagMaxDB + d;
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  if ((uint32_t)(v >> 32) != (uint32_t)(s + 1)) {
+    const uint64_t t0 = global_ns();
+    uint32_t it = 0;
+    do {
+      if (lag_timeout(a, t0, it)) return false;
+      asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    } while ((uint32_t)(v >> 32) != (uint32_t)(s + 1));
+  }
+  n = (uint32_t)v;
   return true;
 }
 
@@ -454,9 +481,9 @@ __device__ void collect_bg(const LagArgs &a, LagShared &sh, const LagState &S, u
     else __syncthreads();
     for (int k = threadIdx.x; k < m; k += nT) {
       const int32_t x = (int32_t)sBg[k];
-      if (driven) {  // the target's place in the driven list, if driven
-        const int32_t p = __ldg(a.drvPosOf + x);
-        if (p >= 0) atomicAdd(S.hits + p, 1u);
+      if (driven) {  // the target's place in the driven list, if this block owns it
+        const int32_t p = __ldg(a.drvPosOf + x) - sh.dLo;
+        if (p >= 0 && p < sh.nLocal) atomicAdd(S.hits + p, 1u);
         continue;
       }
       if (x < sh.idLo || x > sh.idHi) continue;
@@ -511,9 +538,9 @@ __device__ __forceinline__ void driven_ballots(const LagArgs &a, LagShared &sh, 
 #pragma unroll
   for (int r = 0; r < kMaxPer; r++) {
     const int k = threadIdx.x + r * kLB;
-    const bool live = r < a.m && k < a.nD && !(S.r[k] > 0);
+    const bool live = r < sh.m && k < sh.nLocal && !(S.r[k] > 0);
     const uint32_t wm = __ballot_sync(0xffffffffu, live);
-    if (lane == 0 && r < a.m) sh.wcnt[par][r * 32 + warp] = __popc(wm);
+    if (lane == 0 && r < sh.m) sh.wcnt[par][r * 32 + warp] = __popc(wm);
   }
 }
 
@@ -521,7 +548,9 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ LagShared sh;
   const int tid = threadIdx.x;
-  const bool drivenBlock = blockIdx.x == 0;
+  const int nDB = a.nDB;
+  const bool drivenBlock = (int)blockIdx.x < nDB;
+  const int dIdx = drivenBlock ? (int)blockIdx.x : 0;  // driven block: its part of the list
   const int cap = drivenBlock ? a.nDcap : a.cap;
   LagState S = carve(smraw, cap);
   unsigned char *tail = smraw + (size_t)kStateWords * 4 * cap;
@@ -529,7 +558,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   uint32_t *sHex = sBg + kBgChunk;
   uint32_t *sOff = sHex + kHexWords;
   int32_t *sThr = (int32_t *)(sOff + kOffWords);  // driven block: threshold spikes of a step
-  const int b = blockIdx.x - 1;        // tile index of a tile block
+  const int b = (int)blockIdx.x - nDB;  // tile index of a tile block
 
   // ---------------- prologue: own state into shared memory ----------------
   if (tid == 0) {
@@ -539,8 +568,11 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     sh.dbCount = 0;
     sh.head0 = ldcg(&a.G->head);
     sh.steps0 = ldcg(&a.G->stepsDone);
+    sh.dLo = 0;
     if (drivenBlock) {
-      sh.nLocal = a.nD;
+      sh.dLo = a.dLo[dIdx];
+      sh.nLocal = a.dLo[dIdx + 1] - a.dLo[dIdx];
+      sh.m = (sh.nLocal + kLB - 1) / kLB;
       sh.idLo = 0;
       sh.idHi = -1;
       sh.rng = ldcg(&a.G->rngP[sh.steps0 & 1]);
@@ -557,7 +589,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   const int head0 = sh.head0;
   const int64_t steps0 = sh.steps0;
   for (int k = tid; k < nLocal; k += blockDim.x) {
-    const int32_t i = drivenBlock ? a.driven[k] : a.ndIds[a.ndLo[b] + k];
+    const int32_t i = drivenBlock ? a.driven[sh.dLo + k] : a.ndIds[a.ndLo[b] + k];
     S.id[k] = i;
     S.v[k] = a.v[i];
     S.ge[k] = a.gE[i];
@@ -646,10 +678,10 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   // ---------------- the steps ----------------
   // driven block: this thread's entries are k = tid + r * kLB (r < per), the list in order,
   // round by round
-  const int per = a.m;
+  const int per = sh.m;
   auto kOf = [&](int r) { return tid + r * kLB; };
   // count slot of local neuron k: driven neurons have their own slots after the N neuron ids
-  auto cOf = [&](int k) { return drivenBlock ? (uint32_t)(a.N + k) : (uint32_t)S.id[k]; };
+  auto cOf = [&](int k) { return drivenBlock ? (uint32_t)(a.N + sh.dLo + k) : (uint32_t)S.id[k]; };
   // contribution counts are loaded two steps ahead and, where a neuron has one, its first bucket
   // entry one step ahead (the lag guarantees those buckets are complete): nA / eA hold step s's,
   // nB step s + 1's
@@ -682,6 +714,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
           if (ok) sh.known = need;
         }
       }
+      if (ok && dIdx > 0 && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s + 1));
       sh.stopP[s & 1] = ok ? 0 : 1;
     }
     __syncthreads();
@@ -699,12 +732,12 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       {
         const uint32_t n = sh.dbCnt2[sp & 1];
         sh.dbCnt2[sp & 1] = 0;
-        a.dbCnt[sp & (kLagRing - 1)] = (int32_t)n;
+        a.dbCnt[(sp & (kLagRing - 1)) * nDB + dIdx] = (int32_t)n;
         if (a.log) atomicAdd(a.stepTot + sp, (int32_t)n);
         // the spike lists and counts of the steps before s, released every other step: the
         // release holds up its warp about as long as the rest of a step, and the tile blocks push
         // these spikes `help` steps later
-        if (s % a.dbPub == 0) st_release(a.dbDone, (uint32_t)s);
+        if (s % a.dbPub == 0) st_release(a.dbDone + dIdx, (uint32_t)s);
         atomicAdd(a.done + (sp & (kLagRing - 1)), 1u);  // the driven block pushes nothing itself
       }
       if ((sp & 3) == 3) {  // now and then: a later step known finished everywhere, which keeps
@@ -748,15 +781,18 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
 
     {
       const int par = s & 1, parN = par ^ 1;
-      const int m = a.m;
+      const int m = sh.m, nLoc = sh.nLocal, dLo = sh.dLo;
       const uint32_t nbg = (uint32_t)sh.nbgP[par], s0 = sh.rngP[par];
-      // background draws 1..nbg (lif.c:46-48), published for every block
+      // background draws 1..nbg (lif.c:46-48), published for every block by driven block 0 (the
+      // other driven blocks waited for them in their lag check)
       if (a.hasBg) {
-        if (tid == 0) a.bgCount[ring] = (int32_t)nbg;
-        for (int d = 1 + tid; d <= (int)nbg; d += blockDim.x)
-          a.bgList[(int64_t)ring * a.bgCap + d - 1] = xs_jump_hex(sHex, s0, (uint32_t)d) % (uint32_t)a.N;
-        __syncthreads();
-        if (tid == 0) st_release(a.bgReady, (uint32_t)(s + 1));
+        if (dIdx == 0) {
+          if (tid == 0) a.bgCount[ring] = (int32_t)nbg;
+          for (int d = 1 + tid; d <= (int)nbg; d += blockDim.x)
+            a.bgList[(int64_t)ring * a.bgCap + d - 1] = xs_jump_hex(sHex, s0, (uint32_t)d) % (uint32_t)a.N;
+          __syncthreads();
+          if (tid == 0) st_release(a.bgReady, (uint32_t)(s + 1));
+        }
         collect_bg<false>(a, sh, S, sBg, s, true);
       }
       // each warp's first draw among the step's live entries, from the ballots taken at the end
@@ -772,15 +808,43 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         wfirst[r] = totLive + __reduce_add_sync(0xffffffffu, lane < warp ? v : 0u);
         totLive += __reduce_add_sync(0xffffffffu, v);
       }
+      // with the list split over driven blocks: this block's share of the step's draws goes to
+      // the others, whose shares before it offset its draws (pre), and the step's draws in all
+      // (all) fix the generator state of the next step (lif.c:49-52 draws the list in order)
+      uint32_t pre = 0, all = totLive;
+      if (nDB > 1) {
+        if (tid == 0) live_put(a, s, dIdx, totLive);
+        if (dIdx > 0) {
+          uint32_t x = 0;
+          if (lane == 0)
+            for (int d2 = 0; d2 < dIdx; d2++) {
+              uint32_t n = 0;
+              if (!live_get(a, s, d2, n)) break;
+              x += n;
+            }
+          pre = __shfl_sync(0xffffffffu, x, 0);
+        }
+      }
       // the last warp prepares the next step's generator states: after this step's nbg
-      // background and totLive driven draws
-      if ((int)tid >= (int)blockDim.x - 32)
-        driven_prepare(a, sh, sHex, parN, xs_jump_hex(sHex, s0, nbg + totLive), a.hasBg ? sh.bgAccP[par] : 0.f);
+      // background and all driven draws
+      if ((int)tid >= (int)blockDim.x - 32) {
+        if (nDB > 1) {
+          uint32_t x = 0;
+          if (lane == 0)
+            for (int d2 = dIdx + 1; d2 < nDB; d2++) {
+              uint32_t n = 0;
+              if (!live_get(a, s, d2, n)) break;
+              x += n;
+            }
+          all = pre + totLive + __shfl_sync(0xffffffffu, x, 0);
+        }
+        driven_prepare(a, sh, sHex, parN, xs_jump_hex(sHex, s0, nbg + all), a.hasBg ? sh.bgAccP[par] : 0.f);
+      }
       // entries k = tid + r * kLB (r < m), the driven list in order round by round
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         const int k = tid + r * kLB;
-        if (r < m && k < a.nD) receive(a, S, k, nCur[r], a.N + k, slot, haveE, eCur[r]);
+        if (r < m && k < nLoc) receive(a, S, k, nCur[r], a.N + dLo + k, slot, haveE, eCur[r]);
       }
       lap(a, 1, tp);
       // the draws in list order: one per non-refractory entry (lif.c:49-52). Entry k's draw is
@@ -790,10 +854,10 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       for (int r = 0; r < kMaxPer; r++) {
         if (r >= m) break;
         const int k = tid + r * kLB;
-        const bool live = k < a.nD && !(S.r[k] > 0);
+        const bool live = k < nLoc && !(S.r[k] > 0);
         const uint32_t wmask = __ballot_sync(0xffffffffu, live);
         if (live) {
-          const uint32_t p = wfirst[r] + __popc(wmask & ltMask);
+          const uint32_t p = pre + wfirst[r] + __popc(wmask & ltMask);
           const uint32_t x = xs_apply_lane(sOff, p & 31u, sh.cst[par][p >> 5]);  // lanes hold distinct p mod 32
           const float u = __fmul_rn((float)(x >> 8), 1.0f / 16777216.0f);
           if (u < __fmul_rn(S.drive[k], a.dtS)) {  // lif.c:52
@@ -811,7 +875,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         const int k = tid + r * kLB;
-        if (r < m && k < a.nD) {
+        if (r < m && k < nLoc) {
           const bool f = integrate(a, S, k);
           if (f) thrMask |= 1u << r;
           emit(a, S, k, f || ((firedMask >> r) & 1u));
@@ -819,14 +883,14 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       }
       // the step's spikes in any order, each with its rank key (the list position of a forced
       // spike, nD + id of a threshold spike): sorted by key they are lif.c's fired order
-      uint4 *out = a.dbList + (int64_t)ring * a.nDcap * 2;
+      uint4 *out = a.dbList + ((int64_t)ring * a.nDall + dLo) * 2;
 #pragma unroll
       for (int r = 0; r < kMaxPer; r++) {
         const int k = tid + r * kLB;
         const bool forced = (firedMask >> r) & 1u, thr = (thrMask >> r) & 1u;
         if (forced || thr) {
           const uint32_t e = atomicAdd(&sh.dbCnt2[par], 1u);
-          out[2 * e] = make_uint4((uint32_t)S.id[k], forced ? (uint32_t)k : (uint32_t)(a.nD + S.id[k]),
+          out[2 * e] = make_uint4((uint32_t)S.id[k], forced ? (uint32_t)(dLo + k) : (uint32_t)(a.nD + S.id[k]),
                                   __float_as_uint(S.amp[k]), 0u);
           out[2 * e + 1] = make_uint4(S.row0[k], S.row1[k], 0u, 0u);
         }
@@ -859,25 +923,35 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         }
       }
       if (ok && a.hasBg) ok = wait_geq(a, a.bgReady, (uint32_t)(s1 + 1));
-      // test hook: a wait that nothing satisfies (the driven block's progress word never reaches
+      // test hook: a wait that nothing satisfies (the background progress word never reaches
       // 2^32 - 1), so it runs out after timeoutNs and the launch ends with FB_ETIMEOUT
-      if (ok && s1 == a.tripStep && blockIdx.x == 1) ok = wait_geq(a, a.dbDone, 0xffffffffu);
+      if (ok && s1 == a.tripStep && b == 0) ok = wait_geq(a, a.bgReady, 0xffffffffu);
       return ok;
     };
     // the driven block's spikes of step s1 - help that fall to this block (spike e goes to tile
     // block (e + 61 sp) mod nTB: the assignment rotates, so no block carries a push every step),
     // one per lane of the helper warp, into the shared list of step s1's parity
-    uint32_t dbKnown = 0;  // helper warp, lane 0: driven-block steps known released
+    uint32_t dbKnown = 0;  // helper warp, lane d < nDB: steps driven block d is known to have released
     auto help_load = [&](int s1) -> bool {
       const int par1 = s1 & 1;
       int n = 0;
       bool ok = true;
       if (s1 >= a.help && s1 < a.T) {
         const int sp = s1 - a.help, rp = sp & (kLagRing - 1);
-        if (lane == 0 && dbKnown < (uint32_t)(sp + 1)) ok = wait_geq(a, a.dbDone, (uint32_t)(sp + 1), &dbKnown);
-        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (lane < nDB && dbKnown < (uint32_t)(sp + 1)) ok = wait_geq(a, a.dbDone + lane, (uint32_t)(sp + 1), &dbKnown);
+        ok = __all_sync(0xffffffffu, ok);
         if (ok) {
-          const int nsp = ldcg(a.dbCnt + rp);
+          // the step's spikes are the driven blocks' lists one after the other: spike e of the
+          // concatenation is entry e - first[d] of block d's list
+          const int nd = lane < nDB ? ldcg(a.dbCnt + rp * nDB + lane) : 0;
+          int first = nd;
+#pragma unroll
+          for (int o = 1; o < kLagMaxDB; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, first, o);
+            if (lane >= o) first += y;
+          }
+          const int nsp = __shfl_sync(0xffffffffu, first, nDB - 1);
+          first -= nd;  // exclusive prefix
           int e0 = b - (int)(((int64_t)sp * 61) % a.nTB);
           if (e0 < 0) e0 += a.nTB;
           n = nsp > e0 ? (nsp - e0 + a.nTB - 1) / a.nTB : 0;
@@ -885,10 +959,14 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
             if (lane == 0) atomicCAS(a.err, 0, FB_EOVERFLOW);
             n = kHelpMax;
           }
+          const int e = e0 + lane * a.nTB;
+          int seg = 0;  // the block whose list holds spike e
+          for (int d2 = 1; d2 < nDB; d2++) seg += e >= __shfl_sync(0xffffffffu, first, d2) ? 1 : 0;
+          const int f = __shfl_sync(0xffffffffu, first, seg);
           if (lane < n) {
-            const int e = e0 + lane * a.nTB;
-            const uint4 x = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2);
-            const uint4 row = ldcg(a.dbList + ((int64_t)rp * a.nDcap + e) * 2 + 1);
+            const int64_t at = (int64_t)rp * a.nDall + a.dLo[seg] + (e - f);
+            const uint4 x = ldcg(a.dbList + at * 2);
+            const uint4 row = ldcg(a.dbList + at * 2 + 1);
             sh.help[par1][lane] = make_uint4(row.x, row.y, x.y, x.z);
           }
         }
@@ -1028,7 +1106,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
   __syncthreads();
   if (drivenBlock && (int)tid == publisher && a.T > 0 && sEnd == a.T) {  // the last step's count
     const int sp = a.T - 1;
-    a.dbCnt[sp & (kLagRing - 1)] = (int32_t)sh.dbCnt2[sp & 1];
+    a.dbCnt[(sp & (kLagRing - 1)) * nDB + dIdx] = (int32_t)sh.dbCnt2[sp & 1];
     if (a.log) atomicAdd(a.stepTot + sp, (int32_t)sh.dbCnt2[sp & 1]);
   }
   const bool ok = lag_grid_sync(a);
@@ -1045,7 +1123,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     a.spikeCount[i] = S.sc[k];
   }
   // slots delivered during the launch are empty (lif.c:44) unless refilled below
-  if (drivenBlock)
+  if (blockIdx.x == 0)
     for (int u = tid; u < min(a.T, ns); u += blockDim.x) a.ringCount[(head0 + u) % ns] = 0;
   if (!lag_grid_sync(a)) return;
   if (tid == 0) sh.dbCount = 0;
@@ -1058,14 +1136,22 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     const int rslot = (head0 + s + ns - 1) % ns;
     const bool toRing = s >= a.T - a.D;
     int32_t *out = a.ring + (int64_t)rslot * a.N;
-    const int nDB = ldcg(a.dbCnt + ring);
-    const uint4 *dl = a.dbList + (int64_t)ring * a.nDcap * 2;  // entry e at dl[2 e], any order
-    // the driven block's spikes in key order into sThr (ids): forced (key < nD) in list order,
-    // then threshold spikes by ascending id
-    for (int e = tid; e < nDB; e += blockDim.x) {
-      const uint4 x = ldcg(dl + 2 * e);
+    // the driven blocks' spike lists one after the other (each in any order)
+    int first[kLagMaxDB + 1];
+    first[0] = 0;
+    for (int d2 = 0; d2 < nDB; d2++) first[d2 + 1] = first[d2] + ldcg(a.dbCnt + ring * nDB + d2);
+    const int nSp = first[nDB];
+    auto dbe = [&](int e) -> uint4 {
+      int d2 = 0;
+      while (d2 + 1 < nDB && e >= first[d2 + 1]) d2++;
+      return ldcg(a.dbList + ((int64_t)ring * a.nDall + a.dLo[d2] + (e - first[d2])) * 2);
+    };
+    // the driven spikes in key order into sThr (ids): forced (key < nD) in list order, then
+    // threshold spikes by ascending id
+    for (int e = tid; e < nSp; e += blockDim.x) {
+      const uint4 x = dbe(e);
       uint32_t rank = 0;
-      for (int o = 0; o < nDB; o++) rank += ldcg(dl + 2 * o).y < x.y ? 1u : 0u;
+      for (int o = 0; o < nSp; o++) rank += dbe(o).y < x.y ? 1u : 0u;
       sThr[rank] = (int32_t)x.x;
       if (x.y < (uint32_t)a.nD) atomicAdd(&sh.dbCount, 1u);
     }
@@ -1097,7 +1183,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       if (toRing) out[k] = id;
       if (logR && rbase + k < a.logRasterCap) a.logRaster[rbase + k] = id;
     };
-    const int nDT = nDB - nF;
+    const int nDT = nSp - nF;
     for (int k = tid; k < nF; k += blockDim.x) put(k, sThr[k]);
     // driven threshold spikes (ascending) merged with the tile spikes (ascending)
     for (int j = tid; j < nDT; j += blockDim.x) {
@@ -1135,7 +1221,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
       }
     }
     if (tid == 0) {
-      const int total = nDB + (int)carry;
+      const int total = nSp + (int)carry;
       if (toRing) a.ringCount[rslot] = total;
       if (a.log && a.logCount) {
         const int64_t lb = steps0 + s - ldcg(&a.G->logStart);
@@ -1150,7 +1236,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
     }
     __syncthreads();
   }
-  if (drivenBlock && tid == 0) {
+  if (blockIdx.x == 0 && tid == 0) {  // every driven block holds the same generator state
     const int64_t g = steps0 + a.T;
     a.G->head = (head0 + a.T) % ns;
     a.G->stepsDone = g;
@@ -1231,9 +1317,9 @@ cudaError_t launch_edge_records(const uint32_t *indices, const uint32_t *inOff, 
   return cudaGetLastError();
 }
 
-size_t lagged_smem_bytes(int cap, int nDcap) {
+size_t lagged_smem_bytes(int cap, int nDcap, int nDall) {
   const int c = cap > nDcap ? cap : nDcap;
-  return (size_t)kStateWords * 4 * c + (size_t)(kBgChunk + kHexWords + kOffWords) * 4 + (size_t)4 * nDcap;
+  return (size_t)kStateWords * 4 * c + (size_t)(kBgChunk + kHexWords + kOffWords) * 4 + (size_t)4 * nDall;
 }
 
 int lagged_blocks_per_sm(size_t smem) {

@@ -75,7 +75,8 @@ class FbDiffGrads(C.Structure):
 
 
 class FbTuning(C.Structure):
-    _fields_ = [(k, C.c_int32) for k in ("blocks_per_sm", "item_chunks", "max_blocks_per_sm", "sms", "sub_grab", "timeout_us")]
+    _fields_ = [(k, C.c_int32) for k in ("blocks_per_sm", "item_chunks", "max_blocks_per_sm", "sms", "sub_grab", "timeout_us",
+                                               "lag_driven_blocks", "pad")]
 
 
 class FbDiffTuning(C.Structure):

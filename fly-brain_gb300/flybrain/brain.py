@@ -156,10 +156,12 @@ class BrainBatch:
         return x.value
 
     def set_tuning(self, blocks_per_sm: int = 0, item_chunks: int = 0, sub_grab: int = 0,
-                   timeout_us: int = 0):
-        """Launch shape of the grid schedule and the bound of device-side waits
-        (fb_brains_set_tuning); 0 keeps a knob."""
-        t = nat.FbTuning(int(blocks_per_sm), int(item_chunks), 0, 0, int(sub_grab), int(timeout_us))
+                   timeout_us: int = 0, lag_driven_blocks: int | None = None):
+        """Launch shape of the grid schedule, the bound of device-side waits and the delay-scheduled
+        kernel's driven blocks (fb_brains_set_tuning); 0 keeps a knob (lag_driven_blocks: None
+        keeps it, 0 makes it automatic)."""
+        ldb = self.tuning()["lag_driven_blocks"] if lag_driven_blocks is None else int(lag_driven_blocks)
+        t = nat.FbTuning(int(blocks_per_sm), int(item_chunks), 0, 0, int(sub_grab), int(timeout_us), ldb, 0)
         nat.check(self.L.fb_brains_set_tuning(self.h, C.byref(t)))
 
     def tuning(self) -> dict:

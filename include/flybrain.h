@@ -163,6 +163,9 @@ typedef struct fb_tuning {
   int32_t timeout_us;             /* bound of every device-side wait of both schedules, microseconds
                                      (default 5,000,000); a wait that runs out ends the launch with
                                      FB_ETIMEOUT */
+  int32_t lag_driven_blocks;      /* delay-scheduled kernel: blocks the driven list is split over
+                                     (1 or 2; 0 = automatic: 2 from 512 driven neurons) */
+  int32_t pad;
 } fb_tuning;
 int fb_brains_set_tuning(fb_brains *br, const fb_tuning *t);
 int fb_brains_tuning(fb_brains *br, fb_tuning *t);

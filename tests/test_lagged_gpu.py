@@ -166,3 +166,33 @@ def test_lagged_refuses_presynaptic_inhibition():
     brain._batch.set_schedule(nat.FB_SCHEDULE_AUTO)
     brain.run(100)
     assert brain._batch.last_schedule() == nat.FB_SCHEDULE_GRID
+
+
+@pytest.mark.parametrize("bg", [False, True])
+def test_driven_list_split_over_two_blocks(bg):
+    """A driven list long enough to be split over two driven blocks (each offsets its draws by the
+    other's share of live entries), N=20,000 with 1,500 drivers (and, in one case, background
+    events and depression, whose hits on driven neurons the second block collects too): three
+    1,000-step launches, state, generator, ring and fired lists identical to the oracle."""
+    from oracle import oracle as O
+    from flybrain import SYNTH_PARAMS, DeviceGraph, LIFCuda, drive_set, synth_graph
+    from flybrain import _native as nat
+    g = synth_graph(20000, 5)
+    idx, hz = drive_set(g.N, 1500, 77, 80.0, 220.0)
+    p = dict(SYNTH_PARAMS, bgRate=15.0, bgAmp=1.5, depU=0.1) if bg else dict(SYNTH_PARAMS)
+    ob = O.OracleBrain(g.N, g.indptr, g.indices, g.weights, g.sign, p, seed=9)
+    gb = LIFCuda(DeviceGraph(g), p, seed=9)
+    for i, h in zip(idx.tolist(), hz.tolist()):
+        ob.setDriveOne(i, h)
+        gb.setDriveOne(i, h)
+    gb._batch.set_schedule(nat.FB_SCHEDULE_LAGGED)
+    for k in range(3):
+        ob.run(1000)
+        gb.run(1000)
+        assert gb._batch.last_schedule() == nat.FB_SCHEDULE_LAGGED
+        assert_same_as_oracle(gb, ob, ("split", bg, k))
+    c0, r0 = ob.run(64, raster=True)
+    counts, raster = lagged_chunks(64)(gb, 64)
+    np.testing.assert_array_equal(counts, c0)
+    np.testing.assert_array_equal(raster, r0)
+    assert int(ob.spikeCount.sum()) > 10000
