@@ -730,21 +730,42 @@ ADJ_OPTS = dict(dt=0.1, vRest=-52.0, vThresh=-45.0, vReset=-52.0, tauM=20.0, tau
 
 def _adj_loss_grads(batch, readouts, targets, dt):
     """Rasters of every member, MSE of 20 ms low-pass rates against the member's target trace,
-    and its gradient with respect to each raster (torch autograd over the filter)."""
+    and its gradient with respect to each raster (torch autograd over the filter). All members
+    at once: the rasters in one library call into a [members, steps, readouts] buffer padded to
+    the longest member (members of equal readout counts), one filter over all columns, each
+    member's loss over its own steps."""
     import torch
     from flybrain.autograd import lowpass_rates
-    dls, loss = [], 0.0
-    for b in range(batch.B):
-        r = torch.zeros((batch._steps[b], readouts[b].shape[0]), dtype=torch.float32, device="cuda")
+    B = batch.B
+    R = {int(r.shape[0]) for r in readouts}
+    if len(R) != 1:  # readout sets of different sizes: member by member
+        dls, loss = [], 0.0
+        for b in range(B):
+            r = torch.zeros((batch._steps[b], readouts[b].shape[0]), dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            batch.raster(b, readouts[b], out=r)
+            r.requires_grad_()
+            L = ((lowpass_rates(r, dt) - targets[b]) ** 2).mean()
+            L.backward()
+            dls.append(r.grad.detach().contiguous())
+            loss += float(L.detach())
         torch.cuda.synchronize()
-        batch.raster(b, readouts[b], out=r)
-        r.requires_grad_()
-        L = ((lowpass_rates(r, dt) - targets[b]) ** 2).mean()
-        L.backward()
-        dls.append(r.grad.detach().contiguous())
-        loss += float(L.detach())
+        return dls, loss / B
+    R = R.pop()
+    steps = [int(x) for x in batch._steps]
+    T = max(steps)
+    P = torch.zeros((B, T, R), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
-    return dls, loss / batch.B
+    batch.rasters(readouts, [P[b, : steps[b]] for b in range(B)])
+    P.requires_grad_()
+    rates = lowpass_rates(P.permute(1, 0, 2).reshape(T, B * R), dt).reshape(T, B, R)
+    tgt = torch.stack([t.reshape(-1) for t in targets]).to(rates.dtype)  # [B, R]
+    valid = (torch.arange(T, device="cuda")[:, None] < torch.as_tensor(steps, device="cuda")[None, :]).to(rates.dtype)
+    per = (((rates - tgt[None]) ** 2).sum(2) * valid).sum(0) / (torch.as_tensor(steps, device="cuda").to(rates.dtype) * R)
+    per.sum().backward()
+    dls = [P.grad[b, : steps[b]] for b in range(B)]
+    torch.cuda.synchronize()
+    return dls, float(per.mean().detach())
 
 
 def _tune_adjoint(batch, seeds, readouts, rng, key, steps=400):
@@ -800,6 +821,7 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5, prec="f32",
     tune = _tune_adjoint(batch, seeds, readouts, rng, f"bench-adjoint|B={n_trials}|N={g.N}|E={g.E}")
     _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
     _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
+    _adj_loss_grads(batch, readouts, targets, 0.1)  # warm-up of the filter at these shapes
     (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
     gs, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
     ge = torch.zeros(g.E, dtype=torch.float64, device="cuda")
@@ -889,6 +911,7 @@ def run_adjoint_uneven(n_inst=128, seed=11, prec="f32", cpu=True):
     tune = _tune_adjoint(batch, seeds, readouts, rng, f"bench-uneven|B={n_inst}|N={sum(batch.N)}")
     _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
     _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
+    _adj_loss_grads(batch, readouts, targets, 0.1)  # warm-up of the filter at these shapes
     (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
     _, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
     trial_s = sum(steps) * 0.1 / 1000

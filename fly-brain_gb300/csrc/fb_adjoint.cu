@@ -1890,6 +1890,32 @@ extern "C" int fb_diff_batch_raster(fb_diff_batch *b, int32_t inst, int32_t nro,
   return FB_OK;
 }
 
+extern "C" int fb_diff_batch_rasters(fb_diff_batch *b, const int32_t *nro, const int32_t *const *readout,
+                                     float *const *out) {
+  if (!b || !nro || !readout || !out) return dfail(FB_EINVAL, "fb_diff_rasters: null argument");
+  if (!b->recorded) return dfail(FB_ESTATE, "fb_diff_rasters: no recorded forward pass");
+  int rc;
+  for (int k = 0; k < b->B; k++) {
+    if (nro[k] <= 0 || !readout[k] || !out[k]) return dfail(FB_EINVAL, "fb_diff_rasters: bad readout %d", k);
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, out[k]) != cudaSuccess || at.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      return dfail(FB_EINVAL, "fb_diff_rasters: out[%d] is not device memory", k);
+    }
+    if ((rc = set_readout(b, b->in[k], nro[k], readout[k]))) return rc;
+  }
+  if ((rc = push_devs(b))) return rc;  // one upload of the member records for every raster
+  for (int k = 0; k < b->B; k++) {
+    const int32_t steps = b->in[k].recordedSteps;
+    if (steps == 0) continue;
+    DCU(cudaMemsetAsync(out[k], 0, (size_t)steps * nro[k] * 4, b->st));
+    k_raster<<<std::min(steps, 4096), 256, 0, b->st>>>(b->dDevs + k, steps, out[k]);
+  }
+  DCU(cudaGetLastError());
+  DCU(cudaStreamSynchronize(b->st));
+  return FB_OK;
+}
+
 extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, const int32_t *nro,
                                       const int32_t *const *readout, int32_t truncate, int32_t loss_from,
                                       fb_diff_grads *g) {

@@ -145,6 +145,7 @@ SIGNATURES = {
     "fb_diff_batch_forward_ex": (C.c_int, [P, C.POINTER(FbDiffParams), P, P, I32, P, P]),
     "fb_diff_batch_tape": (C.c_int, [P, I32, P, P, P, I64, PI64]),
     "fb_diff_batch_raster": (C.c_int, [P, I32, I32, P, P]),
+    "fb_diff_batch_rasters": (C.c_int, [P, P, P, P]),
     "fb_diff_batch_backward": (C.c_int, [P, P, P, P, I32, I32, C.POINTER(FbDiffGrads)]),
     "fb_diff_batch_edge_sum": (C.c_int, [P, I32, P, P]),
     "fb_flyvis_create": (C.c_int, [I32, I64, P, P, P, P, P, I32, C.POINTER(P)]),

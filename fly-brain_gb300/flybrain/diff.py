@@ -394,6 +394,16 @@ class DiffBatch:
                                               C.c_void_p(out.data_ptr())))
         return out
 
+    def rasters(self, readouts, outs):
+        """Every member's readout raster at once: member k's (steps_k x len(readouts[k]))
+        amplitudes into the torch CUDA tensor outs[k] (fb_diff_batch_rasters)."""
+        ros = [np.ascontiguousarray(r, np.int32) for r in readouts]
+        nro = np.array([r.shape[0] for r in ros], np.int32)
+        rp = (C.c_void_p * self.B)(*[r.ctypes.data for r in ros])
+        op = (C.c_void_p * self.B)(*[o.data_ptr() for o in outs])
+        nat.check(self.L.fb_diff_batch_rasters(self.h, nat.ptr(nro), rp, op))
+        return outs
+
     def backward(self, dLs, readouts=None, truncate: int = 0, lossFrom: int = 0, edge: bool = True, device=None):
         """Per member: dLs[b] as DiffNet.backward's dLdSpike (readouts[b] its readout set or None).
         Returns one gradient dict per member."""

@@ -409,6 +409,10 @@ int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *p, const in
 int fb_diff_batch_tape(fb_diff_batch *b, int32_t inst, int64_t *offsets, int32_t *idx, float *amp,
                        int64_t cap, int64_t *len);
 int fb_diff_batch_raster(fb_diff_batch *b, int32_t inst, int32_t nro, const int32_t *readout, float *out);
+/* Every member's readout raster of the recorded forward in one call: member k's steps x nro[k]
+ * amplitudes into out[k] (device memory), with one upload of the member records and one
+ * synchronisation for the whole batch (fb_diff_batch_raster per member costs both per call). */
+int fb_diff_batch_rasters(fb_diff_batch *b, const int32_t *nro, const int32_t *const *readout, float *const *out);
 
 /* Backward of every instance over its recorded forward: dL[b], nro[b] (null: all 0) and
  * readout[b] as in fb_diff_backward; g[b] receives instance b's gradients (host or device

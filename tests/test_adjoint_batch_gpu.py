@@ -117,3 +117,21 @@ def test_batch_rejects_bad_members():
                 HARD, _defer=True)
     with pytest.raises(FlyBrainError):
         DiffBatch([n], HARD)
+
+
+def test_batched_rasters_equal_member_rasters():
+    """fb_diff_batch_rasters (every member's readout raster in one call, into device buffers)
+    gives each member's fb_diff_batch_raster, bit for bit, readouts of different sizes included."""
+    import torch
+    from flybrain.diff import DiffBatch
+    pairs = _members(dict(HARD))
+    batch = DiffBatch([p[0] for p in pairs], dict(HARD))
+    steps = [90, 130, 70]
+    batch.forward(steps, [3, 4, 5])
+    rng = np.random.default_rng(2)
+    readouts = [np.sort(rng.choice(p[1].N, n, replace=False)).astype(np.int32) for p, n in zip(pairs, (40, 25, 60))]
+    outs = [torch.full((steps[b], readouts[b].shape[0]), -1.0, device="cuda") for b in range(3)]
+    batch.rasters(readouts, outs)
+    for b in range(3):
+        _same(outs[b].cpu().numpy(), batch.raster(b, readouts[b]))
+    assert sum(float(o.sum()) for o in outs) > 0
