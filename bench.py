@@ -48,7 +48,7 @@ L2_FLUSH_BYTES = 512 << 20
 # capture of a 100-step launch of each kernel (profiles/); traffic grows in proportion to steps.
 DRAM_BYTES_PER_STEP_SINGLE = {
     "grid": 16.826112e6 / 100,    # fb::step_kernel
-    "lagged": (53.468928e6 + 0.851456e6) / 100,   # fb::lagged_kernel
+    "lagged": (52.875264e6 + 0.801792e6) / 100,   # fb::lagged_kernel
 }
 # DRAM bytes (read + write) per trial-step of the batched grid kernel, from one ncu capture of a
 # 100-step launch over 32 full-scale trials (profiles/step_kernel_batched_32_trials.txt:
