@@ -525,14 +525,17 @@ __device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, fl
   const uint2 *bk = D.bucket + (int64_t)i * kDBucket;
   const uint32_t nb = n < (uint32_t)kDBucket ? n : (uint32_t)kDBucket;
   bool any = false;
-  uint32_t last = 0;
+  uint2 last = make_uint2(0u, 0u);
+  // order: arrival rank, then edge id (a row naming the target more than once adds its edges
+  // in row order, src/lifdiff.js as lif.c:40-42)
+  auto before = [](uint2 p, uint2 q) { return p.x < q.x || (p.x == q.x && p.y < q.y); };
   for (uint32_t done = 0; done < n;) {
     uint32_t m = 0;
-    auto offer = [&](uint2 x) {  // keep the kDSortMax smallest ranks above `last`, sorted
-      if (any && x.x <= last) return;
-      if (m == (uint32_t)kDSortMax && x.x >= e[m - 1].x) return;
+    auto offer = [&](uint2 x) {  // keep the kDSortMax smallest (rank, edge) pairs above `last`, sorted
+      if (any && !before(last, x)) return;
+      if (m == (uint32_t)kDSortMax && !before(x, e[m - 1])) return;
       uint32_t w = m < (uint32_t)kDSortMax ? m++ : m - 1;
-      while (w > 0 && e[w - 1].x > x.x) {
+      while (w > 0 && before(x, e[w - 1])) {
         e[w] = e[w - 1];
         w--;
       }
@@ -550,7 +553,7 @@ __device__ void d_apply(const DiffDev &D, const DP<R> &Pp, int i, uint32_t n, fl
       break;
     }
     for (uint32_t u = 0; u < m; u++) d_add<R>(D, Pp, e[u], geF, giF, ex);
-    last = e[m - 1].x;
+    last = e[m - 1];
     any = true;
     done += m;
   }

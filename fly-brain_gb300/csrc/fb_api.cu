@@ -162,6 +162,9 @@ struct Topology {
   int32_t N = 0;
   int64_t E = 0;
   uint32_t *indptr = nullptr, *indices = nullptr;
+  // per edge, how many earlier edges of its row have the same target (0 .. kMaxRepeat); null
+  // when no row repeats a target
+  uint8_t *dup = nullptr;
   int refs = 0;
 };
 
@@ -174,6 +177,7 @@ static void topo_release(Topology *t) {
   if (t && --t->refs == 0) {
     cudaFree(t->indptr);
     cudaFree(t->indices);
+    cudaFree(t->dup);
     delete t;
   }
 }
@@ -193,14 +197,30 @@ extern "C" int fb_graph_create(int32_t N, int64_t E, const uint32_t *indptr, con
   CU(cudaMemcpy(ip.data(), indptr, (size_t)(N + 1) * 4, cudaMemcpyDefault));
   if (E) CU(cudaMemcpy(ix.data(), indices, (size_t)E * 4, cudaMemcpyDefault));
   if (ip[0] != 0 || ip[N] != (uint64_t)E) return fail(FB_EINVAL, "fb_graph_create: indptr[0]=%u indptr[N]=%u, E=%lld", ip[0], ip[N], (long long)E);
+  if (N >= (1 << 29) - kLagPer * kLagThreads * kLagMaxDB)
+    return fail(FB_EINVAL, "fb_graph_create: N=%d exceeds the delivery keys' %d", N, (1 << 29) - kLagPer * kLagThreads * kLagMaxDB);
+  // a row may name a target more than once (lif.c:40-42 adds each edge in row order): each edge
+  // gets its repeat index, which orders a presynaptic neuron's contributions to one target
   std::vector<int32_t> stamp(N, -1);
+  std::vector<uint8_t> rep, seen(N, 0);
+  bool anyRep = false;
   for (int32_t r = 0; r < N; r++) {
     if (ip[r + 1] < ip[r]) return fail(FB_EINVAL, "fb_graph_create: indptr decreases at row %d", r);
     for (uint32_t j = ip[r]; j < ip[r + 1]; j++) {
       const uint32_t q = ix[j];
       if (q >= (uint32_t)N) return fail(FB_EINVAL, "fb_graph_create: indices[%u]=%u out of range", j, q);
-      if (stamp[q] == r) return fail(FB_EINVAL, "fb_graph_create: row %d repeats target %u", r, q);
-      stamp[q] = r;
+      if (stamp[q] == r) {
+        if (seen[q] >= kMaxRepeat)
+          return fail(FB_EINVAL, "fb_graph_create: row %d names target %u more than %d times", r, q, kMaxRepeat + 1);
+        if (!anyRep) {
+          rep.assign((size_t)E, 0);
+          anyRep = true;
+        }
+        rep[j] = ++seen[q];
+      } else {
+        stamp[q] = r;
+        seen[q] = 0;
+      }
     }
   }
   Topology *t = new (std::nothrow) Topology;
@@ -222,6 +242,11 @@ extern "C" int fb_graph_create(int32_t N, int64_t E, const uint32_t *indptr, con
       cudaMemcpy(g->sign, sign, (size_t)N * 4, cudaMemcpyDefault) != cudaSuccess) {
     cleanup();
     return fail(FB_ECUDA, "fb_graph_create: upload failed");
+  }
+  if (anyRep && (cudaMalloc(&t->dup, (size_t)E) != cudaSuccess ||
+                 cudaMemcpy(t->dup, rep.data(), (size_t)E, cudaMemcpyHostToDevice) != cudaSuccess)) {
+    cleanup();
+    return fail(FB_ECUDA, "fb_graph_create: upload of the repeat indices failed");
   }
   *out = g;
   return FB_OK;
@@ -545,6 +570,7 @@ extern "C" int fb_brains_create(const fb_graph *const *graphs, int32_t B, const 
     T.chunkCap = (E + kChunk - 1) / kChunk + 1;
     T.indptr = g->topo->indptr;
     T.indices = g->topo->indices;
+    T.dup = g->topo->dup;
     T.W = g->W;
     T.sign = g->sign;
     T.rngP[0] = seed_state(seeds[b]);
@@ -1064,7 +1090,7 @@ static int lag_setup(fb_brains *br) {
     if (Nnd) CU(cudaMemcpyAsync(R.ndIds, nd.data(), Nnd * 4, cudaMemcpyHostToDevice, br->stream));
     CU(cudaMemcpyAsync(R.ndLo, lo.data(), (R.nTB + 1) * 4, cudaMemcpyHostToDevice, br->stream));
     CU(cudaMemcpyAsync(R.drvPosOf, posOf.data(), (size_t)N * 4, cudaMemcpyHostToDevice, br->stream));
-    CU(launch_edge_records(T.indices, R.inOff, R.drvPosOf, N, E, R.edgeRec, br->stream));
+    CU(launch_edge_records(T.indices, T.dup, R.inOff, R.drvPosOf, N, E, R.edgeRec, br->stream));
     CU(cudaStreamSynchronize(br->stream));
     R.nD = nD;
     R.cap = std::max<int>(1, (int)((Nnd + R.nTB - 1) / R.nTB));

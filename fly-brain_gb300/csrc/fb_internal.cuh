@@ -18,6 +18,9 @@ constexpr int kChunk = 32;           // edges per delivery work item (one per la
 constexpr int kBucket = 8;           // in-place contribution slots per target and step
 constexpr int kSortMax = 64;         // contributions per target sorted in local memory
 constexpr uint32_t kNil = 0xffffffffu;
+// A row may name one target up to kMaxRepeat + 1 times; a contribution's key is
+// (arrival rank << 3) | (repeat index << 1) | inhibitory, so repeats sort in row order.
+constexpr int kMaxRepeat = 3;
 
 // Per-brain flags (Trial::flags).
 constexpr int32_t kHasBg = 1;        // background events enabled (bgEvents > 0)
@@ -47,6 +50,7 @@ struct Trial {
   // graph (shared, read-only during a step)
   const uint32_t *indptr, *indices;
   const float *W, *sign;
+  const uint8_t *dup;  // per edge: its repeat index in its row (null: no row repeats a target)
   // state, SoA, N each
   float *v, *gE, *gI, *refr, *trace, *adapt, *res, *bias, *thr, *drive;
   uint32_t *spikeCount;

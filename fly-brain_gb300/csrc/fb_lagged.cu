@@ -270,7 +270,8 @@ __device__ __forceinline__ float predict_amp(const LagArgs &a, float sign, float
 }
 
 // One warp pushes the contributions W[j]*amp (lif.c:41-42) of edges [lo, hi) of one presynaptic
-// neuron into the buckets of arrival slot `slot`, keyed by (rank << 1) | inhibitory; of the row's
+// neuron into the buckets of arrival slot `slot`, keyed by (rank << 3) | (repeat << 1) | inhibitory
+// (the edge record's repeat index orders a row's edges to one target); of the row's
 // 32-edge chunks it takes c0, c0 + cs, ... (several warps can share a row). Each edge's record
 // holds its target's count slot, its first bucket entry and their end. Up to kPushChunks edges per
 // lane are in flight at once: their loads, then their slot claims, then their stores.
@@ -279,7 +280,7 @@ __device__ __forceinline__ void push_edges(const LagArgs &a, uint32_t lo, uint32
                                            int slot, uint32_t c0 = 0, uint32_t cs = 1) {
   if (amp == 0.f) return;  // lif.c:37: nothing delivered, no depression
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t key = (rank << 1) | (amp > 0 ? 0u : 1u);
+  const uint32_t key0 = (rank << 3) | (amp > 0 ? 0u : 1u);
   uint32_t *cnt = a.cnt + (int64_t)slot * a.cntStride;
   uint2 *buf = a.buf + (int64_t)slot * a.E;
   for (uint32_t j0 = lo + 32u * kPushChunks * c0; j0 < hi; j0 += 32u * kPushChunks * cs) {
@@ -300,7 +301,8 @@ __device__ __forceinline__ void push_edges(const LagArgs &a, uint32_t lo, uint32
 #pragma unroll
     for (int c = 0; c < kPushChunks; c++) {
       if (j0 + lane + 32 * c < hi) {
-        if (er[c].y + pos[c] < er[c].z) buf[er[c].y + pos[c]] = make_uint2(key, __float_as_uint(__fmul_rn(w[c], amp)));
+        if (er[c].y + pos[c] < er[c].z)
+          buf[er[c].y + pos[c]] = make_uint2(key0 | (er[c].w << 1), __float_as_uint(__fmul_rn(w[c], amp)));
         else atomicCAS(a.err, 0, FB_EOVERFLOW);
       }
     }
@@ -1302,18 +1304,18 @@ void lagged_jump_tables(std::vector<uint32_t> &tab) {
   }
 }
 
-__global__ void edge_records_kernel(const uint32_t *indices, const uint32_t *inOff, const int32_t *posOf,
-                                    int32_t N, int64_t E, uint4 *out) {
+__global__ void edge_records_kernel(const uint32_t *indices, const uint8_t *dup, const uint32_t *inOff,
+                                    const int32_t *posOf, int32_t N, int64_t E, uint4 *out) {
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < E; j += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t q = indices[j];
     const int32_t p = posOf[q];
-    out[j] = make_uint4(p >= 0 ? (uint32_t)(N + p) : q, inOff[q], inOff[q + 1], 0u);
+    out[j] = make_uint4(p >= 0 ? (uint32_t)(N + p) : q, inOff[q], inOff[q + 1], dup ? (uint32_t)dup[j] : 0u);
   }
 }
 
-cudaError_t launch_edge_records(const uint32_t *indices, const uint32_t *inOff, const int32_t *posOf, int32_t N,
-                                int64_t E, uint4 *out, cudaStream_t st) {
-  if (E > 0) edge_records_kernel<<<1024, 256, 0, st>>>(indices, inOff, posOf, N, E, out);
+cudaError_t launch_edge_records(const uint32_t *indices, const uint8_t *dup, const uint32_t *inOff,
+                                const int32_t *posOf, int32_t N, int64_t E, uint4 *out, cudaStream_t st) {
+  if (E > 0) edge_records_kernel<<<1024, 256, 0, st>>>(indices, dup, inOff, posOf, N, E, out);
   return cudaGetLastError();
 }
 

@@ -94,8 +94,8 @@ struct LagArgs {
 
 // Jump tables of the driven block: M^(v 16^i) (i < 3, v = 1..15), M^4096, and M^l (l < 32, by lane).
 void lagged_jump_tables(std::vector<uint32_t> &tab);
-cudaError_t launch_edge_records(const uint32_t *indices, const uint32_t *inOff, const int32_t *posOf, int32_t N,
-                                int64_t E, uint4 *out, cudaStream_t st);
+cudaError_t launch_edge_records(const uint32_t *indices, const uint8_t *dup, const uint32_t *inOff,
+                                const int32_t *posOf, int32_t N, int64_t E, uint4 *out, cudaStream_t st);
 size_t lagged_smem_bytes(int cap, int nDcap, int nDall);
 int lagged_blocks_per_sm(size_t smem);
 cudaError_t launch_lagged(const LagArgs &a, int grid, size_t smem, cudaStream_t st);

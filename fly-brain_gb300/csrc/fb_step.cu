@@ -305,7 +305,7 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T,
     atomicAdd(inh ? T.gI + q : T.gE + q, w);
     return;
   }
-  const uint32_t key = (k << 1) | (inh ? 1u : 0u);
+  const uint32_t key = (k << 3) | ((T.dup ? (uint32_t)__ldg(T.dup + j) : 0u) << 1) | (inh ? 1u : 0u);
   FB_GUARD(a, q < (uint32_t)N, 4, q, j, return);
   const uint32_t pos = atomicAdd(T.cnt + q, 1u);
   if (pos < (uint32_t)kBucket) {

@@ -83,7 +83,8 @@ int fb_device_info(int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor);
 
 /* Uploads a compiled CSR connectome: the arrays writeGraph lays out (src/lifwasm.js:14-34):
  * indptr u32[N+1], indices u32[E], weights f32[E], sign f32[N] (sign already carries wSyn).
- * Rows must not repeat a target (the reference's graph files merge (pre, post) pairs). */
+ * A row may name a target up to four times (lif.c:40-42 adds every edge in row order, and so do
+ * the kernels); more is refused with FB_EINVAL, as is N >= 2^29 - 4096 (the delivery keys). */
 int fb_graph_create(int32_t N, int64_t E, const uint32_t *indptr, const uint32_t *indices,
                     const float *weights, const float *sign, fb_graph **out);
 
@@ -488,7 +489,8 @@ typedef struct fb_brain_view {
  * rejected with FB_EINVAL (use fb_brains_create). Results are those of fb_step, bit for bit.
  * Before anything is written the call checks, on the device, every index the step will follow
  * (indptr from 0 to E and non-decreasing, targets, the driven list, the ring lists and counts);
- * a violation returns FB_EINVAL with the brain untouched. On success the view's head, rng, bgAcc,
+ * a violation returns FB_EINVAL with the brain untouched. A row that names one target more than
+ * once has those contributions added in an unspecified order (fb_graph_create keeps row order). On success the view's head, rng, bgAcc,
  * nFired and lastSlot hold the state after the last step, and ring[lastSlot * N ...] its fired
  * list. On FB_ETIMEOUT or FB_EOVERFLOW the device arrays may be partly advanced while the view's
  * scalars are those from before the call: the brain is no longer consistent and must be rebuilt.
