@@ -12,18 +12,21 @@ that setting cannot be checked this way.
 
 32 parameters (11 edges, 11 biases, 10 types, drawn among the 44, 44 and 40 with the largest
 gradients) are checked against central finite differences of the forward in double (FP64 finite
-differences). Steps: 1e-3 for the type gains; 1e-2 for an edge gain and 1e-1 mV for a bias, whose
-single-parameter perturbations otherwise move the loss by less than the float32 state resolves
-(scripts/grad_check.mjs:82-86 sizes its steps for the same reason). Both the double-precision and
-the float32 adjoint must agree with every difference within 1%, the type gains within 0.3%; the
-measured errors are printed."""
+differences). Steps: 4e-3 for a type gain, 4e-2 for an edge gain, 0.4 mV for a bias. The
+network state is float32 (as the reference's Float32Array state) and spikes below 1e-4 stay off the
+tape, so a difference carries noise of a fixed size in the loss, and its relative error falls as
+the step grows: over these 32 parameters the largest error is 6.1e-3 at a quarter of these steps,
+4.7e-3 at half, 1.4e-3 at these, and twice these steps give errors of the same size (the
+curvature of the loss does not show yet; scripts/grad_check.mjs:82-86 sizes its steps per
+parameter for the same reason). Both the double-precision and the float32 adjoint must agree with every difference within
+0.3% and with the median within 0.1%; the measured errors are printed."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 STEPS = 500
-H = dict(edge=1e-2, bias=1e-1, type=1e-3)
+H = dict(edge=4e-2, bias=0.4, type=4e-3)
 
 
 def _context(prec, problem=None):
@@ -62,5 +65,5 @@ def test_full_scale_soft_gradients_match_fp64_finite_differences():
     assert r["params"] == 32
     assert all(x["fd"] != 0 for x in r["rows"]), "a finite difference is 0: the check has no signal"
     for row in r["rows"]:
-        bound = 3e-3 if row["kind"] == "type" else 1e-2
-        assert row["rel"] <= bound and row["rel_f32"] <= bound, row
+        assert row["rel"] <= 3e-3 and row["rel_f32"] <= 3e-3, row
+    assert r["median_rel"] <= 1e-3 and r["others"]["f32"]["median_rel"] <= 1e-3, r
