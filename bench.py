@@ -631,8 +631,9 @@ def run_adjoint(g, idx, hz, steps=5000, seed=3, prec="f32", cpu=True):
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
-    net.forward(steps, record=False)  # warm-up (allocations)
+    net.forward(steps, record=False)  # warm-up (allocations, the pass's CUDA graph)
     _, plain = clock(lambda: net.forward(steps, record=False))
+    net.forward(steps, record=True)  # warm-up (the recorded pass's graph)
     _, lib_fwd = clock(lambda: net.forward(steps, record=True))
     dro = np.zeros((steps, readout.shape[0]), np.float32)
     net.backward(dro, readout=readout)  # warm-up (arena allocation)
@@ -819,10 +820,17 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5, prec="f32",
 
     batch.forward(200, seeds, counts=False)  # warm-up
     tune = _tune_adjoint(batch, seeds, readouts, rng, f"bench-adjoint|B={n_trials}|N={g.N}|E={g.E}")
+    # each pass runs once untimed first: its first run captures the pass as a CUDA graph (timed
+    # apart, `first_calls`), the timed run replays it
+    _, plain0 = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
     _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
+    _, fwd0 = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
     _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
     _adj_loss_grads(batch, readouts, targets, 0.1)  # warm-up of the filter at these shapes
     (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
+    _, bwd0 = clock(lambda: batch.backward(dls, readouts, device="cuda", edge=False))
+    first = dict(plain_forward_s=plain0, forward_recorded_s=fwd0, backward_s=bwd0,
+                 note="first run of each pass at these shapes, capturing it as a CUDA graph")
     gs, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
     ge = torch.zeros(g.E, dtype=torch.float64, device="cuda")
     if world == 1:
@@ -842,7 +850,7 @@ def run_adjoint_batched(g, idx, hz, n_trials=64, steps=5000, seed=5, prec="f32",
     total = max_over_ranks(total, world)
     spikes = sum(int(batch.tape(b)[0][-1]) for b in range(min(n_trials, 4)))
     out = dict(trials=n_all, trials_this_rank=n_trials, neurons=g.N, edges=g.E, steps=steps, checkpoint=batch.p["checkpoint"],
-                precision=prec, tuning=tune,
+                precision=prec, tuning=tune, first_calls=first,
                 create_s=create_s, plain_batch_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s,
                 backward_s=bwd_s, edge_sum_s=sum_s, trial_s=trial_s,
                 fwd_bwd_per_trial_s=total / trial_s, plain_batch_forward_per_trial_s=plain_s / trial_s,
@@ -909,16 +917,23 @@ def run_adjoint_uneven(n_inst=128, seed=11, prec="f32", cpu=True):
 
     batch.forward([200] * n_inst, seeds, counts=False)  # warm-up
     tune = _tune_adjoint(batch, seeds, readouts, rng, f"bench-uneven|B={n_inst}|N={sum(batch.N)}")
+    # each pass runs once untimed first: its first run captures the pass as a CUDA graph (timed
+    # apart, `first_calls`), the timed run replays it
+    _, plain0 = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
     _, plain_s = clock(lambda: batch.forward(steps, seeds, record=False, counts=False))
+    _, fwd0 = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
     _, fwd_s = clock(lambda: batch.forward(steps, seeds, record=True, counts=False))
     _adj_loss_grads(batch, readouts, targets, 0.1)  # warm-up of the filter at these shapes
     (dls, loss), loss_s = clock(lambda: _adj_loss_grads(batch, readouts, targets, 0.1))
+    _, bwd0 = clock(lambda: batch.backward(dls, readouts, device="cuda", edge=False))
+    first = dict(plain_forward_s=plain0, forward_recorded_s=fwd0, backward_s=bwd0,
+                 note="first run of each pass at these shapes, capturing it as a CUDA graph")
     _, bwd_s = clock(lambda: batch.backward(dls, readouts, device="cuda"))
     trial_s = sum(steps) * 0.1 / 1000
     total = fwd_s + loss_s + bwd_s
     out = dict(instances=n_inst, neurons_total=int(sum(batch.N)), edges_total=int(sum(batch.E)),
                 steps_min=min(steps), steps_max=max(steps), precision=prec, graph_gen_s=gen_s,
-                checkpoint=batch.p["checkpoint"], tuning=tune,
+                checkpoint=batch.p["checkpoint"], tuning=tune, first_calls=first,
                 plain_forward_s=plain_s, forward_recorded_s=fwd_s, loss_s=loss_s, backward_s=bwd_s,
                 trial_s=trial_s, trial_s_of_gradient_per_wall_s=trial_s / total,
                 trial_s_of_plain_forward_per_wall_s=trial_s / plain_s, cost_vs_plain_forward=total / plain_s,

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <climits>
+#include <cstddef>
 
 #include <algorithm>
 #include <cmath>
@@ -1124,6 +1125,15 @@ struct Inst {
 
 }  // namespace
 
+// One pass's launch sequence (a forward from reset, or a backward's replays and reverse steps)
+// captured as a CUDA graph, and the key it was captured under.
+struct PassGraph {
+  std::vector<uint8_t> key;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t used = 0;
+};
+constexpr size_t kPassGraphs = 4;  // graphs kept per batch
+
 struct fb_diff_batch {
   int32_t B = 0;
   std::vector<Inst> in;
@@ -1137,6 +1147,9 @@ struct fb_diff_batch {
   fb_diff_params lastP;
   int32_t f32 = 0, recordedK = 0, recorded = 0, maxSteps = 0, maxTiles = 1, maxN = 1;
   int32_t tuneNeuron = 0, tuneArrival = 0;  // launch shape overrides (0: default)
+  int32_t stepLaunches = 0;                   // 1: launch every step's kernels from the host
+  std::vector<PassGraph> graphs;              // captured passes, least recently used evicted
+  uint64_t graphTick = 0;
   DP<double> P64;
   DP<float> P32;
   int32_t *err = nullptr, *nonfinite = nullptr;
@@ -1506,6 +1519,78 @@ void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int
   if (!replay) k_emit<<<dim3(1, b->B), 512, 0, b->st>>>(b->dDevs, t);
 }
 
+// Key of a captured pass: the pass kind and its integers, the launch shapes and the scalar
+// parameters the kernels take by value. Every other input is in device memory, read when the
+// graph runs.
+struct PassKey {
+  std::vector<uint8_t> v;
+  template <typename T>
+  PassKey &add(const T &x) {
+    const uint8_t *q = (const uint8_t *)&x;
+    v.insert(v.end(), q, q + sizeof(T));
+    return *this;
+  }
+};
+PassKey pass_key(const fb_diff_batch *b, char kind) {
+  PassKey k;
+  const dim3 ng = neuron_grid(b), ag = arrival_grid(b);
+  k.add(kind).add(b->f32).add(ng.x).add(ng.y).add(ag.x).add(ag.y);
+  // the typed parameters without the struct's trailing padding
+  if (b->f32) {
+    const uint8_t *q = (const uint8_t *)&b->P32;
+    k.v.insert(k.v.end(), q, q + offsetof(DP<float>, xcI) + sizeof(float));
+  } else {
+    const uint8_t *q = (const uint8_t *)&b->P64;
+    k.v.insert(k.v.end(), q, q + offsetof(DP<double>, xcI) + sizeof(float));
+  }
+  return k;
+}
+
+// Issues one pass's launch sequence on the batch's stream. By default the sequence is captured
+// once into a CUDA graph under its key and every later pass with the same key replays it: one
+// graph launch instead of several kernel launches per step. The graph holds kernel launches only
+// (no copies, no host work), so a replay reads the members' current inputs. With step launches
+// tuned on, the kernels are launched from the host step by step.
+template <typename F>
+int run_pass(fb_diff_batch *b, const PassKey &key, F issue, const char *fn) {
+  if (b->stepLaunches) {
+    issue();
+    DCU(cudaGetLastError());
+    return FB_OK;
+  }
+  for (PassGraph &g : b->graphs) {
+    if (g.key == key.v) {
+      g.used = ++b->graphTick;
+      DCU(cudaGraphLaunch(g.exec, b->st));
+      return FB_OK;
+    }
+  }
+  cudaGraph_t graph = nullptr;
+  DCU(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  issue();
+  const cudaError_t le = cudaGetLastError();
+  const cudaError_t ce = cudaStreamEndCapture(b->st, &graph);
+  if (le != cudaSuccess || ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return dfail(FB_ECUDA, "%s: capturing the pass failed: %s", fn, cudaGetErrorString(le != cudaSuccess ? le : ce));
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess)
+    return dfail(ie == cudaErrorMemoryAllocation ? FB_ENOMEM : FB_ECUDA, "%s: instantiating the pass's graph failed: %s",
+                 fn, cudaGetErrorString(ie));
+  if (b->graphs.size() >= kPassGraphs) {
+    auto lru = std::min_element(b->graphs.begin(), b->graphs.end(),
+                                [](const PassGraph &x, const PassGraph &y) { return x.used < y.used; });
+    cudaGraphExecDestroy(lru->exec);
+    b->graphs.erase(lru);
+  }
+  b->graphs.push_back(PassGraph{key.v, exec, ++b->graphTick});
+  DCU(cudaGraphLaunch(exec, b->st));
+  return FB_OK;
+}
+
 void run_step(fb_diff_batch *b, int32_t t, int32_t replay, int32_t row) {
   if (b->f32) run_step_t<float>(b, b->P32, t, replay, row);
   else run_step_t<double>(b, b->P64, t, replay, row);
@@ -1699,6 +1784,7 @@ extern "C" void fb_diff_default_params(fb_diff_params *p) {
 extern "C" int fb_diff_batch_destroy(fb_diff_batch *b) {
   if (!b) return FB_OK;
   if (b->st) cudaStreamSynchronize(b->st);
+  for (PassGraph &g : b->graphs) cudaGraphExecDestroy(g.exec);
   for (void *p : b->allocs) cudaFree(p);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
@@ -1737,10 +1823,12 @@ extern "C" int fb_diff_batch_create(const fb_diff_net *nets, int32_t B, int64_t 
 }
 
 extern "C" int fb_diff_batch_set_tuning(fb_diff_batch *b, const fb_diff_tuning *t) {
-  if (!b || !t || t->neuron_blocks < 0 || t->arrival_blocks < 0 || t->arrival_blocks > 65535)
+  if (!b || !t || t->neuron_blocks < 0 || t->arrival_blocks < 0 || t->arrival_blocks > 65535 ||
+      (t->step_launches != 0 && t->step_launches != 1))
     return dfail(FB_EINVAL, "fb_diff_batch_set_tuning: bad arguments");
   b->tuneNeuron = t->neuron_blocks;
   b->tuneArrival = t->arrival_blocks;
+  b->stepLaunches = t->step_launches;
   return FB_OK;
 }
 
@@ -1827,14 +1915,20 @@ extern "C" int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *
     k_prepare_w32<<<dim3(256, b->B), kDB, 0, b->st>>>(b->dDevs, p->wSyn, p->inhGain);
     DCU(cudaGetLastError());
   }
-  k_reset<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, (float)p->vRest);
   const int32_t ep = std::max(1, p->drive_epoch);
-  for (int32_t t = 0; t < maxSteps; t++) {
-    if (record && t % p->checkpoint == 0) k_ckpt<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, t, 1);
-    if (edits && t % ep == 0) k_epoch<<<dim3(1, b->B), 1024, 0, b->st>>>(b->dDevs, t);
-    run_step(b, t, 0, -1);
-  }
-  DCU(cudaGetLastError());
+  const float vRest = (float)p->vRest;
+  const int32_t ck = p->checkpoint;
+  PassKey key = pass_key(b, 'F');
+  key.add(maxSteps).add(record).add(ck).add(edits).add(ep).add(vRest);
+  rc = run_pass(b, key, [&] {
+    k_reset<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, vRest);
+    for (int32_t t = 0; t < maxSteps; t++) {
+      if (record && t % ck == 0) k_ckpt<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, t, 1);
+      if (edits && t % ep == 0) k_epoch<<<dim3(1, b->B), 1024, 0, b->st>>>(b->dDevs, t);
+      run_step(b, t, 0, -1);
+    }
+  }, "fb_diff_forward");
+  if (rc) return rc;
   if ((rc = check_err(b, "fb_diff_forward"))) return rc;
   if (spike_counts) {
     int64_t o = 0;
@@ -1990,18 +2084,22 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
   if ((rc = prepare(b, &b->lastP))) return rc;
   const int32_t steps = b->maxSteps;
   const int nseg = (steps + K - 1) / K;
-  for (int sg = nseg - 1; sg >= 0; sg--) {
-    const int32_t from = sg * K, to = std::min(steps, from + K);
-    // replay the segment from its checkpoint (src/lifdiff.js:390-464)
-    k_ckpt<<<ng, kDB, 0, b->st>>>(b->dDevs, from, 0);
-    for (int32_t t = from; t < to; t++) run_step(b, t, 1, t - from);
-    // reverse sweep of the segment (src/lifdiff.js:540-667)
-    for (int32_t t = to - 1; t >= from; t--) {
-      if (truncate > 0) k_truncate<<<ng, kDB, 0, b->st>>>(b->dDevs, t, truncate);
-      reverse_step(b, t, t - from, t >= loss_from ? 1 : 0);
+  PassKey key = pass_key(b, 'B');
+  key.add(steps).add(K).add(truncate).add(loss_from);
+  rc = run_pass(b, key, [&] {
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+      const int32_t from = sg * K, to = std::min(steps, from + K);
+      // replay the segment from its checkpoint (src/lifdiff.js:390-464)
+      k_ckpt<<<ng, kDB, 0, b->st>>>(b->dDevs, from, 0);
+      for (int32_t t = from; t < to; t++) run_step(b, t, 1, t - from);
+      // reverse sweep of the segment (src/lifdiff.js:540-667)
+      for (int32_t t = to - 1; t >= from; t--) {
+        if (truncate > 0) k_truncate<<<ng, kDB, 0, b->st>>>(b->dDevs, t, truncate);
+        reverse_step(b, t, t - from, t >= loss_from ? 1 : 0);
+      }
     }
-  }
-  DCU(cudaGetLastError());
+  }, "fb_diff_backward");
+  if (rc) return rc;
   if ((rc = check_err(b, "fb_diff_backward"))) return rc;
   // fixed-order reductions of the scalar terms
   const fb_diff_params &P = b->lastP;

@@ -80,7 +80,7 @@ class FbTuning(C.Structure):
 
 
 class FbDiffTuning(C.Structure):
-    _fields_ = [("neuron_blocks", C.c_int32), ("arrival_blocks", C.c_int32)]
+    _fields_ = [("neuron_blocks", C.c_int32), ("arrival_blocks", C.c_int32), ("step_launches", C.c_int32)]
 
 
 class FbDiffInputs(C.Structure):

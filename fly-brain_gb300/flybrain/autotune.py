@@ -103,7 +103,9 @@ def tune_diff(batch, steps, seeds, dLs, readouts=None, Ks=(25, 50, 100, 200), ne
               arrival_blocks=None, key: str | None = None, use_cache: bool = True) -> dict:
     """Search K and the per-step kernels' launch shape for `batch` (a DiffBatch) and apply the
     fastest: batch.p["checkpoint"] = K and the batch's tuning. steps/seeds as
-    DiffBatch.forward takes them; dLs/readouts as DiffBatch.backward takes them.
+    DiffBatch.forward takes them; dLs/readouts as DiffBatch.backward takes them. Candidates are
+    timed with step launches (a captured pass's first run would include its capture); the batch's
+    launch mode is restored afterwards.
     Returns {"checkpoint", "neuron_blocks", "arrival_blocks", "s", "table", "cached"}."""
     key = "diff|" + (key or f"B={batch.B}|N={sum(batch.N)}") + "|" + _device()
     if use_cache:
@@ -113,9 +115,10 @@ def tune_diff(batch, steps, seeds, dLs, readouts=None, Ks=(25, 50, 100, 200), ne
             batch.set_tuning(hit["neuron_blocks"], hit["arrival_blocks"])
             return dict(hit, cached=True)
     table = []
+    mode = dict(getattr(batch, "tuning", None) or {}).get("step_launches", False)
 
     def run(K, nb, ab):
-        batch.set_tuning(nb, ab)
+        batch.set_tuning(nb, ab, step_launches=True)
         _sync()
         t0 = time.perf_counter()
         batch.forward(steps, seeds, record=True, counts=False, checkpoint=K)
@@ -145,7 +148,7 @@ def tune_diff(batch, steps, seeds, dLs, readouts=None, Ks=(25, 50, 100, 200), ne
         if s < best["s"]:
             best = dict(best, arrival_blocks=ab, s=s)
     batch.p["checkpoint"] = best["checkpoint"]
-    batch.set_tuning(best["neuron_blocks"], best["arrival_blocks"])
+    batch.set_tuning(best["neuron_blocks"], best["arrival_blocks"], step_launches=mode)
     out = dict(best, table=table)
     if use_cache:
         _store(key, out)

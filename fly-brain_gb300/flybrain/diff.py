@@ -329,6 +329,7 @@ class DiffBatch:
         self.h = h
         self._steps = [0] * self.B
         self._p = self.p
+        self.tuning = dict(neuron_blocks=0, arrival_blocks=0, step_launches=False)
 
     def __del__(self):
         h = getattr(self, "h", None)
@@ -336,11 +337,14 @@ class DiffBatch:
             self.L.fb_diff_batch_destroy(h)
             self.h = None
 
-    def set_tuning(self, neuron_blocks: int = 0, arrival_blocks: int = 0):
-        """Launch shape of the per-step kernels (fb_diff_batch_set_tuning); 0 = default."""
-        t = nat.FbDiffTuning(int(neuron_blocks), int(arrival_blocks))
+    def set_tuning(self, neuron_blocks: int = 0, arrival_blocks: int = 0, step_launches: bool | None = None):
+        """Launch shape of the per-step kernels (fb_diff_batch_set_tuning); 0 = default.
+        step_launches: True launches every step's kernels from the host, False replays each pass
+        as a captured CUDA graph (the default); None keeps the current choice."""
+        sl = self.tuning.get("step_launches", False) if step_launches is None else bool(step_launches)
+        t = nat.FbDiffTuning(int(neuron_blocks), int(arrival_blocks), int(sl))
         nat.check(self.L.fb_diff_batch_set_tuning(self.h, C.byref(t)))
-        self.tuning = dict(neuron_blocks=int(neuron_blocks), arrival_blocks=int(arrival_blocks))
+        self.tuning = dict(neuron_blocks=int(neuron_blocks), arrival_blocks=int(arrival_blocks), step_launches=sl)
 
     def set_array(self, inst: int, name: str, values):
         key = {"logGain": "log_gain", "outScale": "out_scale", "thrOffset": "thr_offset",

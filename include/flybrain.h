@@ -395,9 +395,13 @@ int fb_diff_batch_set(fb_diff_batch *b, int32_t inst, int32_t field, const float
 /* Launch shape of the per-step kernels (the autotuner's knobs): blocks per member of the
  * thread-per-neuron kernels (256 threads; at most the member's tile count is used) and of the
  * warp-per-arrival kernels. 0 restores the default (one tile per block for one member, about
- * four waves over the batch otherwise; 304 blocks over the batch). Results do not depend on it. */
+ * four waves over the batch otherwise; 304 blocks over the batch). Results do not depend on it.
+ * step_launches: 0 (default) runs a forward, and a backward's replays and reverse steps, as one
+ * CUDA graph launch each, captured at the first pass with the same step counts, checkpoint
+ * interval, launch shape and scalar parameters and kept (up to four per batch); 1 launches every
+ * step's kernels from the host instead. Results do not depend on it either. */
 typedef struct fb_diff_tuning {
-  int32_t neuron_blocks, arrival_blocks;
+  int32_t neuron_blocks, arrival_blocks, step_launches;
 } fb_diff_tuning;
 int fb_diff_batch_set_tuning(fb_diff_batch *b, const fb_diff_tuning *t);
 

@@ -135,3 +135,46 @@ def test_batched_rasters_equal_member_rasters():
     for b in range(3):
         _same(outs[b].cpu().numpy(), batch.raster(b, readouts[b]))
     assert sum(float(o.sum()) for o in outs) > 0
+
+
+def test_captured_passes_equal_step_launches():
+    """A forward and a backward replayed from captured CUDA graphs give what the same passes
+    launched step by step give, bit for bit: at the capture, at a replay of the same key, after
+    an input changed between replays (the graph reads it from device memory), and after more
+    keys than the batch keeps (the first is evicted and captured again)."""
+    from flybrain.diff import DiffBatch
+    pairs = _members(dict(HARD))
+    batch = DiffBatch([p[0] for p in pairs], dict(HARD))
+    rng = np.random.default_rng(4)
+    readouts = [np.sort(rng.choice(p[1].N, 40, replace=False)).astype(np.int32) for p in pairs]
+
+    def run(steps, launches):
+        batch.set_tuning(step_launches=launches)
+        sc = batch.forward(steps, [3, 4, 5])
+        tapes = [batch.tape(b) for b in range(3)]
+        dls = [np.random.default_rng(steps[b]).normal(0, 1, (steps[b], 40)).astype(np.float32) for b in range(3)]
+        gs = batch.backward(dls, readouts, truncate=40, lossFrom=5)
+        return sc, tapes, gs
+
+    def same_run(x, y):
+        for b in range(3):
+            _same(x[0][b], y[0][b])
+            for u, v in zip(x[1][b], y[1][b]):
+                _same(u, v)
+            assert x[2][b]["params"] == y[2][b]["params"]
+            for k in ("logGain", "edge", "bias", "outScale"):
+                _same(x[2][b][k], y[2][b][k])
+
+    steps = [90, 130, 70]
+    ref = run(steps, True)
+    same_run(run(steps, False), ref)  # captured
+    same_run(run(steps, False), ref)  # replayed
+    assert sum(float(np.abs(g["edge"]).sum()) for g in ref[2]) > 0
+    batch.set_array(0, "outScale", np.full(pairs[0][1].N, 1.6, np.float32))
+    ref2 = run(steps, True)
+    same_run(run(steps, False), ref2)
+    assert any(a.sum() != b.sum() for a, b in zip(ref2[0], ref[0]))
+    for k in range(5):  # five more keys
+        other = [s + 7 * (k + 1) for s in steps]
+        same_run(run(other, False), run(other, True))
+    same_run(run(steps, False), ref2)

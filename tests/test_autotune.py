@@ -52,14 +52,15 @@ class FakeDiff:
         self.clock = clock
         self.K = 100
 
-    def set_tuning(self, nb=0, ab=0):
+    def set_tuning(self, nb=0, ab=0, step_launches=None):
         self.tune = (nb, ab)
-        self.tuning = dict(neuron_blocks=nb, arrival_blocks=ab)
+        self.tuning = dict(neuron_blocks=nb, arrival_blocks=ab, step_launches=step_launches)
 
     def forward(self, steps, seeds, record=True, counts=False, checkpoint=100):
         self.K = checkpoint
 
     def backward(self, dLs, readouts=None, edge=True):
+        assert self.tuning["step_launches"] is True  # candidates are timed with step launches
         nb, ab = self.tune
         self.clock[0] += 1.0 + abs(self.K - 50) / 100 + (0.2 if nb != 1 else 0) + (0.1 if ab != 8 else 0)
 
@@ -76,6 +77,7 @@ def test_tune_diff_coordinate_descent(tmp_path, monkeypatch):
                            arrival_blocks=(2, 8))
     assert (r["checkpoint"], r["neuron_blocks"], r["arrival_blocks"]) == (50, 1, 8)
     assert fd.p["checkpoint"] == 50 and fd.tune == (1, 8)
+    assert fd.tuning["step_launches"] is False  # the launch mode is restored
     assert autotune.tune_diff(FakeDiff(clock), [10, 10], [1, 2], [None, None])["cached"]
 
 
