@@ -329,6 +329,9 @@ __device__ __forceinline__ int64_t tape_count(const DiffDev &D, int64_t a0, int6
   return a1 > a0 ? a1 - a0 : 0;
 }
 
+// Edges of a row each lane of a warp-per-arrival kernel keeps in flight at once.
+constexpr int kEdgeILP = 4;
+
 template <typename R>
 __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
   __shared__ DiffDev D;
@@ -369,24 +372,40 @@ __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, 
     }
     if (!__shfl_sync(0xffffffffu, go, 0)) continue;
     const uint32_t lo = D.indptr[pre], hi = D.indptr[pre + 1];
-    for (uint32_t j = lo + lane; j < hi; j += 32) {
-      if (!D.gate[j]) continue;
-      const uint32_t q = D.indices[j];
-      const uint32_t pos = atomicAdd(D.cnt + q, 1u);
-      if (pos < (uint32_t)kDBucket) {
-        D.bucket[(int64_t)q * kDBucket + pos] = make_uint2((uint32_t)k, j);
-      } else {
-        const uint32_t r = atomicAdd(D.ovfTop, 1u);
-        if (r >= D.ovfCap) {
-          atomicCAS(D.err, 0, FB_EOVERFLOW);
-          continue;
+    // kEdgeILP edges per lane in flight (their loads, then their slot claims, then their
+    // stores); the order of the pushes into a bucket does not matter, k_update orders a target's
+    // contributions by (arrival, edge)
+    for (uint32_t j0 = lo + lane; j0 < hi; j0 += 32 * kEdgeILP) {
+      bool on[kEdgeILP];
+      uint32_t q[kEdgeILP], pos[kEdgeILP];
+#pragma unroll
+      for (int u = 0; u < kEdgeILP; u++) {
+        const uint32_t j = j0 + 32u * u;
+        on[u] = j < hi && D.gate[j];
+        if (on[u]) q[u] = D.indices[j];
+      }
+#pragma unroll
+      for (int u = 0; u < kEdgeILP; u++)
+        if (on[u]) pos[u] = atomicAdd(D.cnt + q[u], 1u);
+#pragma unroll
+      for (int u = 0; u < kEdgeILP; u++) {
+        if (!on[u]) continue;
+        const uint32_t j = j0 + 32u * u;
+        if (pos[u] < (uint32_t)kDBucket) {
+          D.bucket[(int64_t)q[u] * kDBucket + pos[u]] = make_uint2((uint32_t)k, j);
+        } else {
+          const uint32_t r = atomicAdd(D.ovfTop, 1u);
+          if (r >= D.ovfCap) {
+            atomicCAS(D.err, 0, FB_EOVERFLOW);
+            continue;
+          }
+          DOvf o;
+          o.k = (uint32_t)k;
+          o.j = j;
+          o.pad = q[u];
+          o.next = atomicExch(D.ovfHead + q[u], r);
+          D.ovf[r] = o;
         }
-        DOvf o;
-        o.k = (uint32_t)k;
-        o.j = j;
-        o.pad = q;
-        o.next = atomicExch(D.ovfHead + q, r);
-        D.ovf[r] = o;
       }
     }
   }
@@ -396,8 +415,7 @@ __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, 
 // driveSoft, one draw per non-refractory member of the live drivenSet in insertion order, compared
 // (in R; exact32: in f32 as lif.c) against drive * dt/1000; then the spike train's neurons of step
 // t that are not refractory, first listing only. Each spike goes to the head of step t's tape list.
-// Replay: the tape's forced list. Runs after the step's delivery, so it also rewinds the overflow
-// pool for the next step.
+// Replay: the tape's forced list. Shares no data with the step's delivery, beside which it runs.
 template <typename R>
 __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) {
   __shared__ DiffDev D;
@@ -416,7 +434,6 @@ __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) 
       D.adapt[i] = (float)((R)D.adapt[i] + P.adaptInc);
       D.isForced[i] = 1;
     }
-    if (tid == 0) *D.ovfTop = 0;
     return;
   }
   const bool ex = D.exact32 != 0;
@@ -493,10 +510,7 @@ __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) 
       for (int64_t q = q0 + tid; q < q1; q += blockDim.x) D.claim[D.trainIdx[q]] = kClaimFree;
     }
   }
-  if (tid == 0) {
-    D.tForced[t] = (int32_t)nf;
-    *D.ovfTop = 0;
-  }
+  if (tid == 0) D.tForced[t] = (int32_t)nf;
 }
 
 // Adds target i's bucket in arrival-rank order: gE (or gI) = f32(g + P[j] (*inhGain) * eff) in R.
@@ -682,6 +696,9 @@ __global__ void __launch_bounds__(kDB, 4) k_update(const DiffDev *Ds, DP<R> P, i
   __shared__ DiffDev D;
   load_dev(Ds, D);
   if (t >= D.steps) return;
+  // the step's delivery is complete and the next one starts after this kernel: the overflow pool
+  // is rewound here (its entries stay readable until the next delivery)
+  if (blockIdx.x == 0 && threadIdx.x == 0) *D.ovfTop = 0;
   const bool ex = row < 0 && D.exact32;
   const uint32_t lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
   const int nWT = (D.N + kWT - 1) / kWT;
@@ -923,7 +940,7 @@ __global__ void __launch_bounds__(kDB, 3) k_bneuron(const DiffDev *Ds, DP<R> P, 
 // fan-out's adjoint into lRaw (a fixed-order warp sum) and add each gated edge's
 // dLoss/dW_j = lg[q] * eff to its accumulator; lane 0 updates the presynaptic neuron's terms.
 template <typename R>
-__global__ void __launch_bounds__(kDB, 4) k_barrival(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
+__global__ void __launch_bounds__(kDB, 2) k_barrival(const DiffDev *Ds, DP<R> P, int32_t t, int32_t row) {
   __shared__ DiffDev D;
   load_dev(Ds, D);
   const int e = t - (D.nslots - 1);
@@ -945,14 +962,42 @@ __global__ void __launch_bounds__(kDB, 4) k_barrival(const DiffDev *Ds, DP<R> P,
     const R eff = base * amp;
     const bool exc = eff > 0;
     const uint32_t lo = D.indptr[pre], hi = D.indptr[pre + 1];
+    // kEdgeILP edges per lane in flight: every load of a group is issued before any value is
+    // used, so a long row costs one dependent round trip per group rather than per edge; each
+    // lane still adds its edges in ascending order
     R lraw = 0;
-    for (uint32_t j = lo + lane; j < hi; j += 32) {
-      if (!D.gate[j]) continue;
-      const uint32_t q = D.indices[j];
-      const R lg = exc ? (R)D.lgE[q] : (R)D.lgI[q];
-      const R cw = (R)D.counts[j] * (D.edgeGain ? (R)D.edgeGain[j] : R(1));
-      lraw += exc ? lg * cw * (R)D.inScale[q] : lg * cw * (R)D.inScale[q] * P.inhGain;
-      D.gEdge[j] += (double)(lg * eff);
+    for (uint32_t j0 = lo + lane; j0 < hi; j0 += 32 * kEdgeILP) {
+      bool on[kEdgeILP];
+      uint32_t q[kEdgeILP];
+      float cnt[kEdgeILP], eg[kEdgeILP], lgv[kEdgeILP], ins[kEdgeILP];
+      double old[kEdgeILP];
+#pragma unroll
+      for (int u = 0; u < kEdgeILP; u++) {
+        const uint32_t j = j0 + 32u * u;
+        on[u] = j < hi && D.gate[j];
+        if (on[u]) {
+          q[u] = D.indices[j];
+          cnt[u] = D.counts[j];
+          eg[u] = D.edgeGain ? D.edgeGain[j] : 1.f;
+          old[u] = D.gEdge[j];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kEdgeILP; u++) {
+        if (on[u]) {
+          lgv[u] = exc ? D.lgE[q[u]] : D.lgI[q[u]];
+          ins[u] = D.inScale[q[u]];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kEdgeILP; u++) {
+        if (on[u]) {
+          const R lg = lgv[u];
+          const R cw = (R)cnt[u] * (R)eg[u];
+          lraw += exc ? lg * cw * (R)ins[u] : lg * cw * (R)ins[u] * P.inhGain;
+          D.gEdge[j0 + 32u * u] = old[u] + (double)(lg * eff);
+        }
+      }
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) lraw += __shfl_xor_sync(0xffffffffu, lraw, o);
@@ -1143,6 +1188,13 @@ struct fb_diff_batch {
   std::map<int64_t, float *> zeros;  // read-only zero arrays by length
   DiffDev *dDevs = nullptr;
   cudaStream_t st = nullptr;
+  // the side branch of a step (the forced spikes and the tape), forked from and joined into `st`
+  cudaStream_t side = nullptr;
+  cudaEvent_t evFork = nullptr, evForced = nullptr, evUpdated = nullptr, evEmitted = nullptr;
+  // a backward's reverse sweeps, beside the replay of the segment before (two arena halves)
+  cudaStream_t rev = nullptr;
+  cudaEvent_t evRep[2] = {nullptr, nullptr}, evRev[2] = {nullptr, nullptr}, evRevJoin = nullptr;
+  int32_t arenaBufs = 1;
   std::vector<void *> allocs;
   fb_diff_params lastP;
   int32_t f32 = 0, recordedK = 0, recorded = 0, maxSteps = 0, maxTiles = 1, maxN = 1;
@@ -1176,6 +1228,20 @@ int talloc(fb_diff_batch *b, T **p, size_t n) {
   int rc = balloc(b, &q, n * sizeof(T));
   *p = (T *)q;
   return rc;
+}
+
+// An allocation that may fail: out of memory is cleared and reported as false.
+template <typename T>
+bool try_talloc(fb_diff_batch *b, T **p, size_t n) {
+  void *q = nullptr;
+  *p = nullptr;
+  if (cudaMalloc(&q, std::max<size_t>(n * sizeof(T), 16)) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  b->allocs.push_back(q);
+  *p = (T *)q;
+  return true;
 }
 
 // Upload n elements of src (host or device), or reuse the copy made for the same pointer and field.
@@ -1511,12 +1577,38 @@ dim3 arrival_grid(const fb_diff_batch *b) {
   return dim3(std::max(2, 304 / b->B), b->B);
 }
 
+// One step on two streams. The side stream takes the step's forced spikes (after an epoch's drive
+// edits) while the main stream delivers the step's arrivals: neither touches what the other
+// reads or writes (the delivery reads the tape of step t - D and the presynaptic res and fills
+// the buckets; the forced spikes write the refractory state, adaptation, spike counts and the
+// head of step t's tape). The update waits for both. In a forward the side stream then writes
+// the step's tape (k_emit) while the main stream goes on to the next step's delivery, which reads
+// only older steps of the tape -- unless the delay is one step (two ring slots), when that
+// delivery waits for the tape. The forced spikes of the next step wait for the tape (its offset).
 template <typename R>
-void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int32_t row) {
+void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int32_t row, bool epoch) {
+  cudaEventRecord(b->evFork, b->st);
+  cudaStreamWaitEvent(b->side, b->evFork, 0);
+  if (epoch) k_epoch<<<dim3(1, b->B), 1024, 0, b->side>>>(b->dDevs, t);
+  k_forced<R><<<dim3(1, b->B), 512, 0, b->side>>>(b->dDevs, P, t, replay);
+  cudaEventRecord(b->evForced, b->side);
+  if (!replay && t > 0 && b->in[0].D.nslots < 3) cudaStreamWaitEvent(b->st, b->evEmitted, 0);
   k_deliver<R><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, P, t, row);
-  k_forced<R><<<dim3(1, b->B), 512, 0, b->st>>>(b->dDevs, P, t, replay);
+  cudaStreamWaitEvent(b->st, b->evForced, 0);
   k_update<R><<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, P, t, row);
-  if (!replay) k_emit<<<dim3(1, b->B), 512, 0, b->st>>>(b->dDevs, t);
+  if (!replay) {
+    cudaEventRecord(b->evUpdated, b->st);
+    cudaStreamWaitEvent(b->side, b->evUpdated, 0);
+    k_emit<<<dim3(1, b->B), 512, 0, b->side>>>(b->dDevs, t);
+    cudaEventRecord(b->evEmitted, b->side);
+  }
+}
+
+// The side stream's work joins the main stream (the end of a pass that ran a step: the side
+// stream takes part in a capture only once it has waited for the main stream).
+void join_side(fb_diff_batch *b) {
+  cudaEventRecord(b->evEmitted, b->side);
+  cudaStreamWaitEvent(b->st, b->evEmitted, 0);
 }
 
 // Key of a captured pass: the pass kind and its integers, the launch shapes and the scalar
@@ -1591,18 +1683,18 @@ int run_pass(fb_diff_batch *b, const PassKey &key, F issue, const char *fn) {
   return FB_OK;
 }
 
-void run_step(fb_diff_batch *b, int32_t t, int32_t replay, int32_t row) {
-  if (b->f32) run_step_t<float>(b, b->P32, t, replay, row);
-  else run_step_t<double>(b, b->P64, t, replay, row);
+void run_step(fb_diff_batch *b, int32_t t, int32_t replay, int32_t row, bool epoch = false) {
+  if (b->f32) run_step_t<float>(b, b->P32, t, replay, row, epoch);
+  else run_step_t<double>(b, b->P64, t, replay, row, epoch);
 }
 
-void reverse_step(fb_diff_batch *b, int32_t t, int32_t row, int32_t scored) {
+void reverse_step(fb_diff_batch *b, cudaStream_t st, int32_t t, int32_t row, int32_t scored) {
   if (b->f32) {
-    k_bneuron<float><<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P32, t, row, scored);
-    k_barrival<float><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P32, t, row);
+    k_bneuron<float><<<neuron_grid(b), kDB, 0, st>>>(b->dDevs, b->P32, t, row, scored);
+    k_barrival<float><<<arrival_grid(b), kDB, 0, st>>>(b->dDevs, b->P32, t, row);
   } else {
-    k_bneuron<double><<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P64, t, row, scored);
-    k_barrival<double><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, b->P64, t, row);
+    k_bneuron<double><<<neuron_grid(b), kDB, 0, st>>>(b->dDevs, b->P64, t, row, scored);
+    k_barrival<double><<<arrival_grid(b), kDB, 0, st>>>(b->dDevs, b->P64, t, row);
   }
 }
 
@@ -1786,6 +1878,13 @@ extern "C" int fb_diff_batch_destroy(fb_diff_batch *b) {
   if (b->st) cudaStreamSynchronize(b->st);
   for (PassGraph &g : b->graphs) cudaGraphExecDestroy(g.exec);
   for (void *p : b->allocs) cudaFree(p);
+  if (b->side) cudaStreamSynchronize(b->side);
+  if (b->rev) cudaStreamSynchronize(b->rev);
+  for (cudaEvent_t e : {b->evFork, b->evForced, b->evUpdated, b->evEmitted, b->evRep[0], b->evRep[1], b->evRev[0],
+                        b->evRev[1], b->evRevJoin})
+    if (e) cudaEventDestroy(e);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->rev) cudaStreamDestroy(b->rev);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return FB_OK;
@@ -1816,8 +1915,14 @@ extern "C" int fb_diff_batch_create(const fb_diff_net *nets, int32_t B, int64_t 
     b->maxN = std::max(b->maxN, b->in[k].D.N);
   }
   if ((rc = build_groups(b))) return bail(rc);
-  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->rev, cudaStreamNonBlocking) != cudaSuccess)
     return bail(dfail(FB_ECUDA, "fb_diff_batch_create: stream creation failed"));
+  for (cudaEvent_t *e : {&b->evFork, &b->evForced, &b->evUpdated, &b->evEmitted, &b->evRep[0], &b->evRep[1],
+                         &b->evRev[0], &b->evRev[1], &b->evRevJoin})
+    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess)
+      return bail(dfail(FB_ECUDA, "fb_diff_batch_create: event creation failed"));
   *out = b;
   return FB_OK;
 }
@@ -1924,9 +2029,9 @@ extern "C" int fb_diff_batch_forward_ex(fb_diff_batch *b, const fb_diff_params *
     k_reset<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, vRest);
     for (int32_t t = 0; t < maxSteps; t++) {
       if (record && t % ck == 0) k_ckpt<<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, t, 1);
-      if (edits && t % ep == 0) k_epoch<<<dim3(1, b->B), 1024, 0, b->st>>>(b->dDevs, t);
-      run_step(b, t, 0, -1);
+      run_step(b, t, 0, -1, edits && t % ep == 0);
     }
+    if (maxSteps > 0) join_side(b);
   }, "fb_diff_forward");
   if (rc) return rc;
   if ((rc = check_err(b, "fb_diff_forward"))) return rc;
@@ -2021,6 +2126,7 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
   const int32_t K = b->recordedK;
   int rc = fill_params(b, &b->lastP);
   if (rc) return rc;
+  int32_t bufs = 2;  // arena halves every member has
   for (int k = 0; k < b->B; k++) {
     Inst &I = b->in[k];
     DiffDev &D = I.D;
@@ -2049,22 +2155,40 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
       const int64_t e = t - (D.nslots - 1);
       if (e >= 0) maxArr = std::max<int64_t>(maxArr, off[e + 1] - off[e]);
     }
-    if (K > I.arenaRows) {
-      float *a;
-      uint8_t *md;
-      if ((rc = talloc(b, &a, (size_t)5 * K * N)) || (rc = talloc(b, &md, (size_t)K * N))) return rc;
-      D.aV = a;
-      D.aGE = a + (size_t)K * N;
-      D.aGI = a + (size_t)2 * K * N;
-      D.aAd = a + (size_t)3 * K * N;
-      D.aSp = a + (size_t)4 * K * N;
-      D.aMode = md;
-      I.arenaRows = K;
+    // rows for two segments when they fit (a segment's replay then runs beside the reverse
+    // sweep of the segment after it, each in its own half), for one otherwise
+    if (I.arenaRows < 2 * (int64_t)K) {
+      int64_t rows = 2 * (int64_t)K;
+      uint8_t *raw = nullptr;
+      if (!try_talloc(b, &raw, (size_t)21 * rows * N)) {
+        rows = K;
+        if (I.arenaRows < rows && (rc = talloc(b, &raw, (size_t)21 * rows * N))) return rc;
+      }
+      if (raw) {  // 5 float planes (v, gE, gI, adapt, spike) and the byte plane of modes
+        const size_t plane = (size_t)rows * N;
+        float *a = (float *)raw;
+        D.aV = a;
+        D.aGE = a + plane;
+        D.aGI = a + 2 * plane;
+        D.aAd = a + 3 * plane;
+        D.aSp = a + 4 * plane;
+        D.aMode = raw + 20 * plane;
+        I.arenaRows = rows;
+      }
     }
-    if (maxArr * K > I.resAtCap) {
-      if ((rc = talloc(b, &D.resAt, maxArr * K))) return rc;
-      I.resAtCap = maxArr * K;
+    int64_t rows = I.arenaRows >= 2 * (int64_t)K ? 2 * (int64_t)K : K;
+    if (maxArr * rows > I.resAtCap) {
+      float *r = nullptr;
+      if (!try_talloc(b, &r, (size_t)(maxArr * rows))) {
+        rows = K;
+        if (maxArr * rows > I.resAtCap && (rc = talloc(b, &r, (size_t)(maxArr * rows)))) return rc;
+      }
+      if (r) {
+        D.resAt = r;
+        I.resAtCap = maxArr * rows;
+      }
     }
+    bufs = std::min<int32_t>(bufs, rows >= 2 * (int64_t)K ? 2 : 1);
     D.maxArr = maxArr;
     D.gDrive = nullptr;
     if (D.driveAt) {
@@ -2084,18 +2208,42 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
   if ((rc = prepare(b, &b->lastP))) return rc;
   const int32_t steps = b->maxSteps;
   const int nseg = (steps + K - 1) / K;
+  b->arenaBufs = bufs;
   PassKey key = pass_key(b, 'B');
-  key.add(steps).add(K).add(truncate).add(loss_from);
+  key.add(steps).add(K).add(truncate).add(loss_from).add(bufs);
+  // Segments are replayed on the main stream (one after another: they share the forward state)
+  // and swept in reverse on the reverse stream (one after another: they share the adjoint
+  // state). With two arena halves, segment sg's replay writes half sg & 1 and may run while the
+  // segment after it (sg + 1, the other half) is swept; it waits for the sweep of sg + 2, the
+  // last reader of its half. A sweep reads only its half, the tape and the adjoint state, and
+  // a replay touches none of these, so the two overlap. With one half, everything runs in order
+  // on the main stream.
   rc = run_pass(b, key, [&] {
     for (int sg = nseg - 1; sg >= 0; sg--) {
       const int32_t from = sg * K, to = std::min(steps, from + K);
+      const int32_t half = bufs == 2 ? (sg & 1) * K : 0;
       // replay the segment from its checkpoint (src/lifdiff.js:390-464)
+      if (bufs == 2 && sg + 2 < nseg) cudaStreamWaitEvent(b->st, b->evRev[sg & 1], 0);
       k_ckpt<<<ng, kDB, 0, b->st>>>(b->dDevs, from, 0);
-      for (int32_t t = from; t < to; t++) run_step(b, t, 1, t - from);
+      for (int32_t t = from; t < to; t++) run_step(b, t, 1, half + t - from);
+      cudaStream_t rs = b->st;
+      if (bufs == 2) {
+        cudaEventRecord(b->evRep[sg & 1], b->st);
+        cudaStreamWaitEvent(b->rev, b->evRep[sg & 1], 0);
+        rs = b->rev;
+      }
       // reverse sweep of the segment (src/lifdiff.js:540-667)
       for (int32_t t = to - 1; t >= from; t--) {
-        if (truncate > 0) k_truncate<<<ng, kDB, 0, b->st>>>(b->dDevs, t, truncate);
-        reverse_step(b, t, t - from, t >= loss_from ? 1 : 0);
+        if (truncate > 0) k_truncate<<<ng, kDB, 0, rs>>>(b->dDevs, t, truncate);
+        reverse_step(b, rs, t, half + t - from, t >= loss_from ? 1 : 0);
+      }
+      if (bufs == 2) cudaEventRecord(b->evRev[sg & 1], b->rev);
+    }
+    if (steps > 0) {
+      join_side(b);
+      if (bufs == 2) {
+        cudaEventRecord(b->evRevJoin, b->rev);
+        cudaStreamWaitEvent(b->st, b->evRevJoin, 0);
       }
     }
   }, "fb_diff_backward");

@@ -119,6 +119,26 @@ def test_hard_gradients_match_oracle():
     _compare_grads(g0, g1)
 
 
+@pytest.mark.parametrize("delay", [0.1, 0.2, 0.3])
+def test_short_delays_match_oracle(delay):
+    """Delays of one to three steps: with one step (two ring slots) a delivery reads the tape the
+    step before wrote, so the forward keeps the tape write ahead of the next delivery; with more
+    the two overlap. Tape, spike counts and gradients against the oracle, hard spikes."""
+    ins, target, driven, hz, params = _hard_inputs()
+    params = dict(params, delay=delay)
+    prob, net = _pair(ins, params, driven, hz)
+    dL = np.zeros(ins["N"], np.float32)
+    dL[target] = 1
+    sc0, tape = prob.forward(120, seed=3)
+    sc1 = net.forward(120, seed=3)
+    assert sc0.tobytes() == sc1.tobytes()
+    off, idx, amp = net.tape()
+    np.testing.assert_array_equal(off, tape["off"])
+    np.testing.assert_array_equal(idx, tape["idx"])
+    assert idx.shape[0] > 300
+    _compare_grads(prob.backward(tape, dL), net.backward(dL))
+
+
 def test_steep_surrogate_nonfinite_values_agree():
     """With the steep surrogate the adjoint overflows; both sides zero and count the same
     non-finite gradients (src/lifdiff.js:681-684)."""
