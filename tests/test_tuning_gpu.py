@@ -201,5 +201,6 @@ def test_tune_diff_applies_a_valid_shape(tmp_path, monkeypatch):
     batch, dLs = _diff_batch()
     r = tune_diff(batch, [100] * 3, [1, 2, 3], dLs, Ks=(16, 50), neuron_blocks=(1, 2), arrival_blocks=(2, 8))
     assert r["checkpoint"] in (16, 50, batch.members[0].p["checkpoint"]) and batch.p["checkpoint"] == r["checkpoint"]
-    assert batch.tuning == dict(neuron_blocks=r["neuron_blocks"], arrival_blocks=r["arrival_blocks"])
+    assert batch.tuning == dict(neuron_blocks=r["neuron_blocks"], arrival_blocks=r["arrival_blocks"],
+                                step_launches=False)  # timed with step launches, then restored
     assert len(r["table"]) == 1 + 1 + 1 + 2 + 2  # warm-up, K0 = 16, K = 50, two of each grid knob
