@@ -242,9 +242,10 @@ __device__ __forceinline__ uint32_t xs_apply_lane(const uint32_t *off, uint32_t 
   return y;
 }
 
-// Phase timer: thread 0 of blocks 0 and 1 adds the time since its last lap to slot k.
+// Phase timer: thread 0 of the first driven block and of the first tile block adds the time
+// since its last lap to slot k.
 __device__ __forceinline__ void lap(const LagArgs &a, int k, uint64_t &tp) {
-  if (a.prof != nullptr && blockIdx.x < 2 && threadIdx.x == 0) {
+  if (a.prof != nullptr && (blockIdx.x == 0 || blockIdx.x == (unsigned)a.nDB) && threadIdx.x == 0) {
     const uint64_t now = global_ns();
     atomicAdd(a.prof + k, (unsigned long long)(now - tp));
     tp = now;
@@ -994,6 +995,9 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
         sEnd = s;
         break;
       }
+      // the service warps' own time per step (phase timer, first tile block)
+      const bool svcTimed = a.prof != nullptr && b == 0 && lane == 0 && warp >= kTWarps;
+      const uint64_t svc0 = svcTimed ? global_ns() : 0;
       if (warp == kTWarps) {  // publisher: step s - 1 complete, then the lag for step s + 1
         if (lane == 0) {
           if (s > 0) {
@@ -1006,11 +1010,13 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
             }
           }
           if (s + 1 < a.T) sh.stopP[par ^ 1] = lag_ok(s + 1) ? 0 : 1;
+          if (svcTimed) atomicAdd(a.prof + 10, (unsigned long long)(global_ns() - svc0));
         }
         continue;
       }
       if (warp == kTWarps + 1) {  // helper: the next step's share of the driven spikes
         help_load(s + 1);
+        if (svcTimed) atomicAdd(a.prof + 11, (unsigned long long)(global_ns() - svc0));
         continue;
       }
       lap(a, 5, tp);
@@ -1051,6 +1057,7 @@ __global__ void __launch_bounds__(kLB, 1) lagged_kernel(LagArgs a) {
           if (f) flags |= (uint64_t)1 << (16 * r);
         }
       }
+      lap(a, 9, tp);
       // compaction in ascending local index: neurons r = 0 (k = tid) first, then r = 1, ...
       uint32_t fired = 0;
       if (wbar_or(flags != 0)) {

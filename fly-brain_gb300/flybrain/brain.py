@@ -194,11 +194,12 @@ class BrainBatch:
         nat.check(self.L.fb_profile(self.h, 1 if on else 0))
 
     def phase_times(self) -> dict:
-        """Accumulated per-phase milliseconds (grid block 0's view) since profile(True)."""
-        ms = (C.c_double * 10)()
-        nat.check(self.L.fb_phase_times(self.h, ms, 10))
+        """Accumulated per-phase milliseconds since profile(True): the grid kernel's phases (grid
+        block 0's view) or, for the delay-scheduled kernel, the slots fb_phase_times documents."""
+        ms = (C.c_double * 12)()
+        nat.check(self.L.fb_phase_times(self.h, ms, 12))
         return dict(zip(("serial", "deliver", "barrier1", "update", "barrier2", "ctl_head",
-                         "ctl_loads", "ctl_draw", "ctl_emit", "ctl_tail"), list(ms)))
+                         "ctl_loads", "ctl_draw", "ctl_emit", "ctl_tail", "lag_publisher", "lag_helper"), list(ms)))
 
     def record(self, cap_steps: int, cap_spikes: int = 0):
         nat.check(self.L.fb_record(self.h, int(cap_steps), int(cap_spikes)))

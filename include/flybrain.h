@@ -255,11 +255,14 @@ int fb_last_step_ms(fb_brains *br, float *ms);
  * serves: [5] the header and background draws, [6] the driven-list gathers, [7] the draws,
  * [8] the forced spikes' emission, [9] the RNG advance. fb_phase_times copies up to n
  * accumulated totals in ms. With the schedule forced to FB_SCHEDULE_LAGGED the delay-scheduled
- * kernel runs instead (AUTO takes the grid kernel while profiling) and the slots hold: the driven
- * block's [0] lag wait, [1] background and delivery, [2] draws, [3] update and spike list,
- * [4] completion signal; tile block 1's [5] lag wait, [6] delivery, update and compaction, [7] own
- * spikes' pushes, [8] the driven spikes' pushes (with their wait), [9] completion signal. */
-#define FB_NPHASES 10
+ * kernel runs instead (AUTO takes the grid kernel while profiling) and the slots hold: the first
+ * driven block's [0] lag wait and completion signal, [1] background and delivery, [2] draws,
+ * [3] update and spike list, [4] the next step's live entries; the first tile block's [5] wait at
+ * the step barrier for its service warps, [6] compaction, [7] own spikes' pushes, [8] the driven
+ * spikes' pushes, [9] delivery and update, [10] its publisher warp's work per step (completion
+ * signal, the next step's lag check), [11] its helper warp's work per step (the next step's
+ * driven spikes). */
+#define FB_NPHASES 12
 int fb_profile(fb_brains *br, int32_t on);
 int fb_phase_times(fb_brains *br, double *ms, int32_t n);
 
