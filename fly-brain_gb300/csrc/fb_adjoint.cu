@@ -416,6 +416,7 @@ __global__ void __launch_bounds__(kDB, 4) k_deliver(const DiffDev *Ds, DP<R> P, 
 // (in R; exact32: in f32 as lif.c) against drive * dt/1000; then the spike train's neurons of step
 // t that are not refractory, first listing only. Each spike goes to the head of step t's tape list.
 // Replay: the tape's forced list. Shares no data with the step's delivery, beside which it runs.
+constexpr int kForcedPer = 4;  // driven-list entries per thread and round in k_forced
 template <typename R>
 __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) {
   __shared__ DiffDev D;
@@ -459,27 +460,52 @@ __global__ void k_forced(const DiffDev *Ds, DP<R> P, int32_t t, int32_t replay) 
     const uint32_t s0 = sh_s0;
     const int32_t nLive = *D.nLive;
     uint32_t draws = 0;
-    for (int32_t r0 = 0; r0 < nLive; r0 += blockDim.x) {
-      const int32_t k = r0 + tid;
-      int32_t i = 0;
-      uint32_t live = 0;
-      float dr = 0.f;
-      if (k < nLive) {
-        i = D.drivenLive[k];
-        live = D.refr[i] > 0 ? 0u : 1u;
-        dr = d_drive(D, i, t);
+    // rounds of kForcedPer entries per thread, each thread's a contiguous run of the list: one
+    // block scan gives a thread's first draw (a jump); its later live entries take the next draws
+    // (one generator step each)
+    const int32_t span = (int32_t)blockDim.x * kForcedPer;
+    for (int32_t r0 = 0; r0 < nLive; r0 += span) {
+      int32_t ii[kForcedPer];
+      float dr[kForcedPer];
+      uint32_t liveMask = 0, nl = 0;
+#pragma unroll
+      for (int u = 0; u < kForcedPer; u++) {
+        const int32_t k = r0 + tid * kForcedPer + u;
+        ii[u] = 0;
+        dr[u] = 0.f;
+        if (k < nLive) {
+          ii[u] = D.drivenLive[k];
+          dr[u] = d_drive(D, ii[u], t);
+          if (!(D.refr[ii[u]] > 0)) {
+            liveMask |= 1u << u;
+            nl++;
+          }
+        }
       }
       uint32_t nlive;
-      const uint32_t dpos = block_exclusive_scan(live, &nlive, scan);
-      uint32_t fire = 0;
-      if (live) {
-        const uint32_t x = xs_jump(sJump, s0, draws + dpos + 1);
-        const R u = (R)(x >> 8) * (R)(1.0 / 16777216.0);  // exact in f32 and f64
-        fire = (ex ? u < (R)(dr * P.xdtS) : u < (R)dr * P.dtS) ? 1u : 0u;
+      const uint32_t dpos = block_exclusive_scan(nl, &nlive, scan);
+      uint32_t fireMask = 0, nfr = 0;
+      if (nl) {
+        uint32_t x = xs_jump(sJump, s0, draws + dpos + 1);
+        bool first = true;
+#pragma unroll
+        for (int u = 0; u < kForcedPer; u++) {
+          if (!((liveMask >> u) & 1u)) continue;
+          if (!first) x = xs_next(x);
+          first = false;
+          const R uu = (R)(x >> 8) * (R)(1.0 / 16777216.0);  // exact in f32 and f64
+          if (ex ? uu < (R)(dr[u] * P.xdtS) : uu < (R)dr[u] * P.dtS) {
+            fireMask |= 1u << u;
+            nfr++;
+          }
+        }
       }
       uint32_t nfire;
-      const uint32_t fpos = block_exclusive_scan(fire, &nfire, scan);
-      if (fire) fire_one(i, base + nf + fpos);
+      const uint32_t fpos = block_exclusive_scan(nfr, &nfire, scan);
+      uint32_t o = 0;
+#pragma unroll
+      for (int u = 0; u < kForcedPer; u++)
+        if ((fireMask >> u) & 1u) fire_one(ii[u], base + nf + fpos + o++);
       draws += nlive;
       nf += nfire;
     }
@@ -736,16 +762,20 @@ __global__ void k_emit(const DiffDev *Ds, int32_t t) {
   load_dev(Ds, D);
   if (t >= D.steps) return;
   const int tid = threadIdx.x;
-  int64_t carry = D.tOff[t] + D.tForced[t];
+  const int64_t carry = D.tOff[t] + D.tForced[t];
+  // thread tid takes a contiguous run of tiles, so one block scan places every tile
   const int nWT = (D.N + kWT - 1) / kWT;
-  for (int t0 = 0; t0 < nWT; t0 += blockDim.x) {
-    const int tl = t0 + tid;
-    const uint32_t c = tl < nWT ? (uint32_t)D.tileCnt[tl] : 0u;
-    uint32_t tot;
-    const uint32_t pre = block_exclusive_scan(c, &tot, scan);
-    if (c) {
-      const int64_t o = carry + pre;
-      for (uint32_t p = 0; p < c; p++) {
+  const int per = (nWT + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int t0 = min(nWT, tid * per), t1 = min(nWT, t0 + per);
+  uint32_t c = 0;
+  for (int tl = t0; tl < t1; tl++) c += (uint32_t)D.tileCnt[tl];
+  uint32_t tot;
+  const uint32_t pre = block_exclusive_scan(c, &tot, scan);
+  if (c) {
+    int64_t o = carry + pre;
+    for (int tl = t0; tl < t1; tl++) {
+      const uint32_t n = (uint32_t)D.tileCnt[tl];
+      for (uint32_t p = 0; p < n; p++) {
         if (o + p < D.tapeCap) {
           D.tIdx[o + p] = D.stage[(int64_t)tl * kWT + p];
           D.tAmp[o + p] = D.stageAmp[(int64_t)tl * kWT + p];
@@ -753,10 +783,10 @@ __global__ void k_emit(const DiffDev *Ds, int32_t t) {
           atomicCAS(D.err, 0, FB_EOVERFLOW);
         }
       }
+      o += n;
     }
-    carry += tot;
   }
-  if (tid == 0) D.tOff[t + 1] = carry;
+  if (tid == 0) D.tOff[t + 1] = carry + tot;
 }
 
 // Zeroes the adjoint state and accumulators of every instance (before a backward pass).
@@ -1590,7 +1620,7 @@ void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int
   cudaEventRecord(b->evFork, b->st);
   cudaStreamWaitEvent(b->side, b->evFork, 0);
   if (epoch) k_epoch<<<dim3(1, b->B), 1024, 0, b->side>>>(b->dDevs, t);
-  k_forced<R><<<dim3(1, b->B), 512, 0, b->side>>>(b->dDevs, P, t, replay);
+  k_forced<R><<<dim3(1, b->B), 1024, 0, b->side>>>(b->dDevs, P, t, replay);
   cudaEventRecord(b->evForced, b->side);
   if (!replay && t > 0 && b->in[0].D.nslots < 3) cudaStreamWaitEvent(b->st, b->evEmitted, 0);
   k_deliver<R><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, P, t, row);
@@ -1599,7 +1629,7 @@ void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int
   if (!replay) {
     cudaEventRecord(b->evUpdated, b->st);
     cudaStreamWaitEvent(b->side, b->evUpdated, 0);
-    k_emit<<<dim3(1, b->B), 512, 0, b->side>>>(b->dDevs, t);
+    k_emit<<<dim3(1, b->B), 1024, 0, b->side>>>(b->dDevs, t);
     cudaEventRecord(b->evEmitted, b->side);
   }
 }
