@@ -1225,6 +1225,7 @@ struct fb_diff_batch {
   cudaStream_t rev = nullptr;
   cudaEvent_t evRep[2] = {nullptr, nullptr}, evRev[2] = {nullptr, nullptr}, evRevJoin = nullptr;
   int32_t arenaBufs = 1;
+  cudaError_t orderErr = cudaSuccess;  // first failed event record or wait of the pass being issued
   std::vector<void *> allocs;
   fb_diff_params lastP;
   int32_t f32 = 0, recordedK = 0, recorded = 0, maxSteps = 0, maxTiles = 1, maxN = 1;
@@ -1607,6 +1608,14 @@ dim3 arrival_grid(const fb_diff_batch *b) {
   return dim3(std::max(2, 304 / b->B), b->B);
 }
 
+// Stream ordering inside a pass: the first failure of an event record or wait is kept and
+// reported by run_pass (the launches' own errors are read there too).
+void order_note(fb_diff_batch *b, cudaError_t e) {
+  if (e != cudaSuccess && b->orderErr == cudaSuccess) b->orderErr = e;
+}
+void ev_record(fb_diff_batch *b, cudaEvent_t ev, cudaStream_t st) { order_note(b, cudaEventRecord(ev, st)); }
+void ev_wait(fb_diff_batch *b, cudaStream_t st, cudaEvent_t ev) { order_note(b, cudaStreamWaitEvent(st, ev, 0)); }
+
 // One step on two streams. The side stream takes the step's forced spikes (after an epoch's drive
 // edits) while the main stream delivers the step's arrivals: neither touches what the other
 // reads or writes (the delivery reads the tape of step t - D and the presynaptic res and fills
@@ -1617,28 +1626,28 @@ dim3 arrival_grid(const fb_diff_batch *b) {
 // delivery waits for the tape. The forced spikes of the next step wait for the tape (its offset).
 template <typename R>
 void run_step_t(fb_diff_batch *b, const DP<R> &P, int32_t t, int32_t replay, int32_t row, bool epoch) {
-  cudaEventRecord(b->evFork, b->st);
-  cudaStreamWaitEvent(b->side, b->evFork, 0);
+  ev_record(b, b->evFork, b->st);
+  ev_wait(b, b->side, b->evFork);
   if (epoch) k_epoch<<<dim3(1, b->B), 1024, 0, b->side>>>(b->dDevs, t);
   k_forced<R><<<dim3(1, b->B), 1024, 0, b->side>>>(b->dDevs, P, t, replay);
-  cudaEventRecord(b->evForced, b->side);
-  if (!replay && t > 0 && b->in[0].D.nslots < 3) cudaStreamWaitEvent(b->st, b->evEmitted, 0);
+  ev_record(b, b->evForced, b->side);
+  if (!replay && t > 0 && b->in[0].D.nslots < 3) ev_wait(b, b->st, b->evEmitted);
   k_deliver<R><<<arrival_grid(b), kDB, 0, b->st>>>(b->dDevs, P, t, row);
-  cudaStreamWaitEvent(b->st, b->evForced, 0);
+  ev_wait(b, b->st, b->evForced);
   k_update<R><<<neuron_grid(b), kDB, 0, b->st>>>(b->dDevs, P, t, row);
   if (!replay) {
-    cudaEventRecord(b->evUpdated, b->st);
-    cudaStreamWaitEvent(b->side, b->evUpdated, 0);
+    ev_record(b, b->evUpdated, b->st);
+    ev_wait(b, b->side, b->evUpdated);
     k_emit<<<dim3(1, b->B), 1024, 0, b->side>>>(b->dDevs, t);
-    cudaEventRecord(b->evEmitted, b->side);
+    ev_record(b, b->evEmitted, b->side);
   }
 }
 
 // The side stream's work joins the main stream (the end of a pass that ran a step: the side
 // stream takes part in a capture only once it has waited for the main stream).
 void join_side(fb_diff_batch *b) {
-  cudaEventRecord(b->evEmitted, b->side);
-  cudaStreamWaitEvent(b->st, b->evEmitted, 0);
+  ev_record(b, b->evEmitted, b->side);
+  ev_wait(b, b->st, b->evEmitted);
 }
 
 // Key of a captured pass: the pass kind and its integers, the launch shapes and the scalar
@@ -1675,9 +1684,11 @@ PassKey pass_key(const fb_diff_batch *b, char kind) {
 // tuned on, the kernels are launched from the host step by step.
 template <typename F>
 int run_pass(fb_diff_batch *b, const PassKey &key, F issue, const char *fn) {
+  b->orderErr = cudaSuccess;
   if (b->stepLaunches) {
     issue();
     DCU(cudaGetLastError());
+    DCU(b->orderErr);
     return FB_OK;
   }
   for (PassGraph &g : b->graphs) {
@@ -1690,7 +1701,8 @@ int run_pass(fb_diff_batch *b, const PassKey &key, F issue, const char *fn) {
   cudaGraph_t graph = nullptr;
   DCU(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
   issue();
-  const cudaError_t le = cudaGetLastError();
+  cudaError_t le = cudaGetLastError();
+  if (le == cudaSuccess) le = b->orderErr;
   const cudaError_t ce = cudaStreamEndCapture(b->st, &graph);
   if (le != cudaSuccess || ce != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
@@ -2253,13 +2265,13 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
       const int32_t from = sg * K, to = std::min(steps, from + K);
       const int32_t half = bufs == 2 ? (sg & 1) * K : 0;
       // replay the segment from its checkpoint (src/lifdiff.js:390-464)
-      if (bufs == 2 && sg + 2 < nseg) cudaStreamWaitEvent(b->st, b->evRev[sg & 1], 0);
+      if (bufs == 2 && sg + 2 < nseg) ev_wait(b, b->st, b->evRev[sg & 1]);
       k_ckpt<<<ng, kDB, 0, b->st>>>(b->dDevs, from, 0);
       for (int32_t t = from; t < to; t++) run_step(b, t, 1, half + t - from);
       cudaStream_t rs = b->st;
       if (bufs == 2) {
-        cudaEventRecord(b->evRep[sg & 1], b->st);
-        cudaStreamWaitEvent(b->rev, b->evRep[sg & 1], 0);
+        ev_record(b, b->evRep[sg & 1], b->st);
+        ev_wait(b, b->rev, b->evRep[sg & 1]);
         rs = b->rev;
       }
       // reverse sweep of the segment (src/lifdiff.js:540-667)
@@ -2267,13 +2279,13 @@ extern "C" int fb_diff_batch_backward(fb_diff_batch *b, const float *const *dL, 
         if (truncate > 0) k_truncate<<<ng, kDB, 0, rs>>>(b->dDevs, t, truncate);
         reverse_step(b, rs, t, half + t - from, t >= loss_from ? 1 : 0);
       }
-      if (bufs == 2) cudaEventRecord(b->evRev[sg & 1], b->rev);
+      if (bufs == 2) ev_record(b, b->evRev[sg & 1], b->rev);
     }
     if (steps > 0) {
       join_side(b);
       if (bufs == 2) {
-        cudaEventRecord(b->evRevJoin, b->rev);
-        cudaStreamWaitEvent(b->st, b->evRevJoin, 0);
+        ev_record(b, b->evRevJoin, b->rev);
+        ev_wait(b, b->st, b->evRevJoin);
       }
     }
   }, "fb_diff_backward");
