@@ -1650,9 +1650,9 @@ void join_side(fb_diff_batch *b) {
   ev_wait(b, b->st, b->evEmitted);
 }
 
-// Key of a captured pass: the pass kind and its integers, the launch shapes and the scalar
-// parameters the kernels take by value. Every other input is in device memory, read when the
-// graph runs.
+// Key of a captured pass: the pass kind and its integers, the launch shapes, the ring depth and
+// the scalar parameters the kernels take by value. Every other input is in device memory, read
+// when the graph runs.
 struct PassKey {
   std::vector<uint8_t> v;
   template <typename T>
@@ -1665,7 +1665,9 @@ struct PassKey {
 PassKey pass_key(const fb_diff_batch *b, char kind) {
   PassKey k;
   const dim3 ng = neuron_grid(b), ag = arrival_grid(b);
-  k.add(kind).add(b->f32).add(ng.x).add(ng.y).add(ag.x).add(ag.y);
+  // the ring depth shapes a forward's stream order (a one-step delay orders the tape before the
+  // next delivery) and is not among the scalars below (it follows from delay / dt)
+  k.add(kind).add(b->f32).add(ng.x).add(ng.y).add(ag.x).add(ag.y).add(b->in[0].D.nslots);
   // the typed parameters without the struct's trailing padding
   if (b->f32) {
     const uint8_t *q = (const uint8_t *)&b->P32;

@@ -139,6 +139,23 @@ def test_short_delays_match_oracle(delay):
     _compare_grads(prob.backward(tape, dL), net.backward(dL))
 
 
+def test_captured_passes_follow_a_delay_change():
+    """Forward passes of one network with the delay alternating between one and three steps:
+    each pass's graph is keyed on the ring depth (the stream order differs), so every pass matches
+    the oracle at its own delay, the cached ones included."""
+    from oracle.lifdiff_oracle import DiffProblem
+    ins, target, driven, hz, params = _hard_inputs()
+    _, net = _pair(ins, params, driven, hz)
+    probs = {d: DiffProblem(**ins, params=dict(params, delay=d), driven=driven, drive_hz=hz) for d in (0.1, 0.3)}
+    for delay in (0.1, 0.3, 0.1, 0.3):
+        sc0, tape = probs[delay].forward(100, seed=3)
+        sc1 = net.forward(100, seed=3, delay=delay)
+        assert sc0.tobytes() == sc1.tobytes(), delay
+        off, idx, _ = net.tape()
+        np.testing.assert_array_equal(off, tape["off"])
+        np.testing.assert_array_equal(idx, tape["idx"])
+
+
 def test_steep_surrogate_nonfinite_values_agree():
     """With the steep surrogate the adjoint overflows; both sides zero and count the same
     non-finite gradients (src/lifdiff.js:681-684)."""
