@@ -11,8 +11,10 @@ steps) from rest. One bench step = 1,000 brain steps (100 ms simulated) in one p
           pinned buffers; the events are counted from those after the timed region)
   cpu_baseline : the oracle port of lif_step (1 core: the reference kernel is serial) on a
           bounded sample of the same workload
-  extra legs (each switchable by FB_BENCH_<LEG>=0), each with its own cpu_baseline:
+  extra legs (each switchable by FB_BENCH_<LEG>=0), each with its own cpu_baseline except the
+  scatter leg (a phase of a kernel, timed alone):
           high_activity (the headline plus a 6 mV tonic bias: ~97% of spikes recurrent),
+          scatter (the grid kernel's delivery phase timed alone, 256 trials under that bias),
           adjoint, adjoint_batched, adjoint_uneven (float32 and, beside it, float64 -- the
           reference's arithmetic), batched (256 trials; split over ranks when N > 1), flyvis
           (64 eyes), embodied (the per-millisecond call pattern of the simulated fly)
@@ -363,6 +365,9 @@ def run_ours(args, rank, world):
         bt = run_batched(g, args, n_trials=int(os.environ.get("FB_BATCH_TRIALS", "256")), rank=rank, world=world)
         bt["cost_vs_plain_per_trial_s"] = (1.0 / bt["trial_s_per_wall_s"]) / (dev_s / sim_s)
         res["batched"] = bt
+    if os.environ.get("FB_BENCH_SCATTER", "1") == "1":
+        torch.cuda.empty_cache()
+        res["scatter"] = run_scatter(g, idx, hz)
     if os.environ.get("FB_BENCH_FLYVIS", "1") == "1":
         torch.cuda.empty_cache()
         res["flyvis"] = run_flyvis(n_eyes=int(os.environ.get("FB_FLYVIS_EYES", "64")))
@@ -447,6 +452,56 @@ def by_precision(precisions, fn):
             out = r
         else:
             out[pr] = r
+    return out
+
+
+def run_scatter(g, idx, hz, n_trials=256, bias_mv=6.0, warm=300, steps=100):
+    """The scatter on its own: the grid kernel's delivery phase (each arriving spike's edges into
+    the per-target buckets: edge record, W*s, an atomic slot claim and the bucket store) under
+    load -- n_trials trials of the full graph with the headline drive and a tonic bias_mv bias on
+    every neuron, timed by the kernel's phase timer over `steps` steps after `warm` steps from rest.
+    Bandwidth in the phase's algorithmic bytes (16 B per synaptic event + 20 B per arrival) over the
+    delivery phase's time, against the measured HBM peak; the update phase beside it in its 64 B
+    per neuron. The phase timer's own cost is inside the phase times; the same steps without it are
+    reported as plain_ms_per_step."""
+    from flybrain import SYNTH_PARAMS, BrainBatch, DeviceGraph
+    dg = DeviceGraph(g)
+    outdeg = g.outdeg().astype(np.int64)
+    bb = BrainBatch([dg] * n_trials, SYNTH_PARAMS, list(range(1, n_trials + 1)))
+    bv = np.full(g.N, bias_mv, np.float32)
+    for b in range(n_trials):
+        bb.set_drive(b, idx, hz)
+        bb.write("bias", b, bv)
+    bb.step(warm)
+
+    def counts():
+        return np.stack([bb.read("spikeCount", b).astype(np.int64) for b in range(n_trials)])
+
+    sc0 = counts()
+    bb.step(steps)
+    plain_ms = bb.last_ms()
+    sc1 = counts()
+    bb.profile(True)
+    bb.step(steps)
+    ph = bb.phase_times()
+    bb.profile(False)
+    sc2 = counts()
+    d = sc2 - sc1
+    events, arrivals = float((d * outdeg).sum()), float(d.sum())
+    peak, kind = peaks()
+    dbytes = 16.0 * events + 20.0 * arrivals
+    ubytes = 64.0 * g.N * n_trials * steps
+    deliver_s, update_s = ph["deliver"] / 1e3, ph["update"] / 1e3
+    out = dict(trials=n_trials, bias_mv=bias_mv, steps=steps, events_per_trial_step=events / steps / n_trials,
+               plain_ms_per_step=plain_ms / steps, plain_events_per_trial_step=float(((sc1 - sc0) * outdeg).sum()) / steps / n_trials,
+               phase_ms_per_step={k: v / steps for k, v in ph.items() if k in ("serial", "deliver", "barrier1", "update", "barrier2")},
+               roofline=dict(bound="hbm", achieved=dbytes / deliver_s / 1e9, peak=peak, unit="GB/s",
+                             frac=dbytes / deliver_s / 1e9 / peak, peak_kind=kind, traffic=None,
+                             kernel="fb::step_kernel, delivery phase", algorithmic_bytes=dbytes),
+               update_gbs=ubytes / update_s / 1e9, update_frac=ubytes / update_s / 1e9 / peak,
+               config=f"{n_trials} trials x N={g.N:,}, 2,000 drive neurons at U(100,200) Hz and a tonic {bias_mv} mV bias on "
+                      f"every neuron; {steps} steps after {warm} from rest, phase-timed")
+    del bb
     return out
 
 
