@@ -275,41 +275,59 @@ __device__ void materialize_brain(const StepArgs &a, const Trial &T, Trial *G, i
 
 // One delivery work item: 32 consecutive edges of the concatenated rows of the arrivals in
 // `slot`, starting at edge c * 32. Lane l takes edge c*32+l. The item's record names its first
-// arrival; lanes past that arrival's edges find theirs through the offsets.
-__device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T, Trial *G, int slot, uint32_t F,
-                                              uint32_t c, uint32_t gparity) {
+// arrival; lanes past that arrival's edges find theirs through the offsets. The delivery is split
+// in two so a warp can keep two items' loads in flight: load_edge gathers the edge, its target,
+// key and contribution W*s; claim_edge takes the target's bucket slot and stores the entry (the
+// order of the claims does not matter: the update adds a target's entries in key order).
+struct DEdge {
+  uint32_t q, key;
+  float w;
+  bool valid;
+};
+
+__device__ __forceinline__ DEdge load_edge(const StepArgs &a, const Trial &T, int slot, uint32_t F, uint32_t c) {
+  DEdge d;
+  d.valid = false;
   const int lane = threadIdx.x & 31;
   const uint32_t e = c * kChunk + lane;
-  if (e >= F) return;
+  if (e >= F) return d;
   const int N = T.N;
-  FB_GUARD(a, (int64_t)c < T.chunkCap, 1, c, slot, return);
+  FB_GUARD(a, (int64_t)c < T.chunkCap, 1, c, slot, return d);
   const uint4 ck = ldcg(T.chunkK + (int64_t)slot * T.chunkCap + c);
   uint32_t k = ck.x, pre = ck.y, j = ck.w + e;
   if (e >= ck.z) {  // a later arrival of this item
     const uint32_t *off = T.ringOff + (int64_t)slot * (N + 1);
     k++;
     while (k < (uint32_t)N && ldcg(off + k + 1) <= e) k++;
-    FB_GUARD(a, k < (uint32_t)N, 2, k, e, return);
+    FB_GUARD(a, k < (uint32_t)N, 2, k, e, return d);
     pre = (uint32_t)ldcg(T.ring + (int64_t)slot * N + k);
     j = ldcg(T.ringRow + (int64_t)slot * N + k) + (e - ldcg(off + k));
   }
-  FB_GUARD(a, pre < (uint32_t)N && (int64_t)j < T.E, 3, pre, j, return);
+  FB_GUARD(a, pre < (uint32_t)N && (int64_t)j < T.E, 3, pre, j, return d);
   // the edge's loads are issued with the presynaptic ones, before the zero-amplitude test
   const uint32_t q = __ldg(T.indices + j);
   const float wj = __ldg(T.W + j);
   const float amp = __fmul_rn(__ldg(T.sign + pre), (T.flags & kResRest) ? 1.f : ldcg(T.res + pre));  // lif.c:37
-  if (amp == 0.f) return;
-  const float w = __fmul_rn(wj, amp);  // lif.c:41-42, one rounding
+  if (amp == 0.f) return d;
+  FB_GUARD(a, q < (uint32_t)N, 4, q, j, return d);
+  d.q = q;
+  d.w = __fmul_rn(wj, amp);  // lif.c:41-42, one rounding
   const bool inh = !(amp > 0);
+  d.key = (k << 3) | ((T.dup ? (uint32_t)__ldg(T.dup + j) : 0u) << 1) | (inh ? 1u : 0u);
+  d.valid = true;
+  return d;
+}
+
+__device__ __forceinline__ void claim_edge(const StepArgs &a, const Trial &T, const DEdge &d, uint32_t gparity) {
+  if (!d.valid) return;
+  const uint32_t q = d.q;
   if (T.mode == FB_DELIVER_FAST) {
-    atomicAdd(inh ? T.gI + q : T.gE + q, w);
+    atomicAdd((d.key & 1u) ? T.gI + q : T.gE + q, d.w);
     return;
   }
-  const uint32_t key = (k << 3) | ((T.dup ? (uint32_t)__ldg(T.dup + j) : 0u) << 1) | (inh ? 1u : 0u);
-  FB_GUARD(a, q < (uint32_t)N, 4, q, j, return);
   const uint32_t pos = atomicAdd(T.cnt + q, 1u);
   if (pos < (uint32_t)kBucket) {
-    T.bucket[(int64_t)q * kBucket + pos] = make_uint2(key, __float_as_uint(w));
+    T.bucket[(int64_t)q * kBucket + pos] = make_uint2(d.key, __float_as_uint(d.w));
   } else {
     const uint32_t r = atomicAdd(a.ovfTop + gparity, 1u);
     if (r >= a.ovfCap) {
@@ -317,8 +335,8 @@ __device__ __forceinline__ void deliver_chunk(const StepArgs &a, const Trial &T,
       return;
     }
     OvfRec rec;
-    rec.key = key;
-    rec.bits = __float_as_uint(w);
+    rec.key = d.key;
+    rec.bits = __float_as_uint(d.w);
     rec.pad = q;
     rec.next = atomicExch(T.ovfHead + q, r);
     a.ovf[gparity][r] = rec;
@@ -531,7 +549,7 @@ __device__ void update_tile(const StepArgs &a, const Trial &T, Trial *G, int t, 
 // global memory would be refetched from L2 at every step.
 constexpr int kTrialCache = 4;
 
-__global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
+__global__ void __launch_bounds__(kBlock, 2) step_kernel(StepArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   // per-brain launch constants (layout mirrors step_smem_bytes): step count and log start at
   // launch, start head, ring depth, steps of this launch, first tile; then the prefix of this
@@ -648,20 +666,38 @@ __global__ void __launch_bounds__(kBlock) step_kernel(StepArgs a) {
       if (tid == 0) sPre[a.B] = carry;
       __syncthreads();
     }
-    // work items go to warps from the far end of the grid, whose blocks have the fewest items
+    // work items go to warps from the far end of the grid, whose blocks have the fewest items;
+    // a warp takes two at a time (w and w + nwarps): both items' loads, then both items' claims
     const uint32_t total = sPre[a.B];
-    for (uint32_t w = nwarps - 1 - gwarp; w < total; w += nwarps) {
-      int lo = 0, hi = a.B;  // brain b with sPre[b] <= w < sPre[b+1]
+    auto brain_of = [&](uint32_t w) {  // brain b with sPre[b] <= w < sPre[b+1]
+      int lo = 0, hi = a.B;
       while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (sPre[mid] <= w) lo = mid;
         else hi = mid;
       }
-      const Trial &T = hdr(lo);
-      const int head = (sHead0[lo] + s) % sNs[lo];
-      const uint32_t F = ldcg(T.slotEdges + head), c0 = (w - sPre[lo]) * (uint32_t)a.itemChunks;
-      for (int u = 0; u < a.itemChunks && (c0 + u) * (uint32_t)kChunk < F; u++)
-        deliver_chunk(a, T, a.trials + lo, head, F, c0 + u, (uint32_t)(s & 1));
+      return lo;
+    };
+    for (uint32_t w = nwarps - 1 - gwarp; w < total; w += 2 * nwarps) {
+      const uint32_t w2 = w + nwarps;
+      const bool two = w2 < total;
+      const int b1 = brain_of(w), b2 = two ? brain_of(w2) : b1;
+      const Trial &T1 = hdr(b1);
+      const Trial &T2 = hdr(b2);
+      const int h1 = (sHead0[b1] + s) % sNs[b1], h2 = (sHead0[b2] + s) % sNs[b2];
+      const uint32_t F1 = ldcg(T1.slotEdges + h1), F2 = two ? ldcg(T2.slotEdges + h2) : 0u;
+      const uint32_t c1 = (w - sPre[b1]) * (uint32_t)a.itemChunks;
+      const uint32_t c2 = two ? (w2 - sPre[b2]) * (uint32_t)a.itemChunks : 0u;
+      for (int u = 0; u < a.itemChunks; u++) {
+        const bool on1 = (c1 + u) * (uint32_t)kChunk < F1, on2 = two && (c2 + u) * (uint32_t)kChunk < F2;
+        if (!on1 && !on2) break;
+        DEdge d1, d2;
+        d1.valid = d2.valid = false;
+        if (on1) d1 = load_edge(a, T1, h1, F1, c1 + u);
+        if (on2) d2 = load_edge(a, T2, h2, F2, c2 + u);
+        claim_edge(a, T1, d1, (uint32_t)(s & 1));
+        claim_edge(a, T2, d2, (uint32_t)(s & 1));
+      }
     }
     lap(1);
     if (!grid_sync(a)) return;
