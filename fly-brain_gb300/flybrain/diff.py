@@ -308,7 +308,8 @@ class DiffNet:
 
 
 class DiffBatch:
-    """B independent differentiable brains advanced together by one set of launches
+    """B independent differentiable brains advanced together, every launch covering all members
+    and each forward or backward pass replayed as one captured CUDA graph
     (fb_diff_batch_*): each member is a DiffNet built with DiffNet(..., _defer=True) (its graph,
     per-neuron arrays and driven set); the model parameters are the batch's. Arrays that are the
     same object in several members are uploaded once and shared."""

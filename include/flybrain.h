@@ -384,7 +384,8 @@ int fb_diff_backward(fb_diff *d, const float *dL, int32_t nro, const int32_t *re
 /* ---- batches of differentiable brains ------------------------------------------------------
  * No counterpart in the reference, which trains one LIFDiff at a time: B independent instances
  * (each its own network, drive, seed and length; one parameter set) advanced together, every
- * kernel launch covering the whole batch. Arrays passed by the same pointer for the same field
+ * kernel launch covering the whole batch; a forward pass and a backward pass each run as one
+ * captured CUDA graph (fb_diff_tuning). Arrays passed by the same pointer for the same field
  * of several instances are uploaded once and shared (fb_diff_batch_set on one of them sets it for
  * all). Each instance's results are those of fb_diff_* on that instance alone. */
 typedef struct fb_diff_batch fb_diff_batch; /* opaque */
