@@ -16,8 +16,10 @@
  * setDriveOne, setDrive, setBias, setThr, addG, pulse, setBackground, reset and wake act as
  * LIFWasm's do; the state arrays v, gE, gI, refr, trace, adapt, res, bias, thr, drive (Float32Array)
  * and spikeCount (Uint32Array) read as copies of the device state; N, nAwake and t (simulated ms
- * since reset) are numbers. Beyond LIFWasm: run(n) takes n steps in one launch and returns the
- * last step's fired count; dispose() frees the device state before the object is collected.
+ * since reset) are numbers. LIFGpu's extras (src/lifgpu.js:349-351): setParams(q) merges q into
+ * the parameters (the ring depth round(delay / dt) + 1 must stay), flush() has nothing to submit,
+ * destroy() frees the device state. Beyond both: run(n) takes n steps in one launch and returns
+ * the last step's fired count; dispose() is destroy() under another name.
  * A failing call throws an Error with the library's message (attachBrain falls back on any
  * exception, src/brainsetup.js:66-75).
  *
@@ -34,6 +36,7 @@
 typedef struct {
   fb_graph *graph;
   fb_brains *brains;
+  fb_params p; /* the parameters in force */
   int32_t N;
   double dt; /* ms per step */
   double t;  /* simulated ms since reset */
@@ -159,6 +162,8 @@ static napi_value new_typed(napi_env env, napi_typedarray_type t, size_t n, size
   return out;
 }
 
+static bool merge_params(napi_env env, napi_value obj, fb_params *p);
+
 /* ---- methods ----------------------------------------------------------------------------- */
 
 static napi_value m_step(napi_env env, napi_callback_info info) {
@@ -271,6 +276,22 @@ static napi_value m_set_background(napi_env env, napi_callback_info info) {
   if (!get_f64(env, argv[0], &rate) || !get_f64(env, argv[1], &amp))
     return throw_msg(env, "LIFNative.setBackground(rateHz, ampMv): numbers expected");
   if (fb_set_background(b->brains, 0, rate, amp)) return throw_fb(env);
+  b->p.bgRate = rate;
+  b->p.bgAmp = amp;
+  return undefined_value(env);
+}
+
+static napi_value m_set_params(napi_env env, napi_callback_info info) {
+  napi_value argv[1];
+  Brain *b = this_brain(env, info, 1, argv, NULL);
+  if (!b) return throw_msg(env, "LIFNative.setParams: not a live brain");
+  fb_params p = b->p;
+  napi_valuetype t;
+  if (napi_typeof(env, argv[0], &t) != napi_ok || t != napi_object || !merge_params(env, argv[0], &p))
+    return throw_msg(env, "LIFNative.setParams(q): an object of numbers");
+  if (fb_set_params(b->brains, 0, &p)) return throw_fb(env);
+  b->p = p;
+  b->dt = p.dt;
   return undefined_value(env);
 }
 
@@ -282,7 +303,8 @@ static napi_value m_reset(napi_env env, napi_callback_info info) {
   return undefined_value(env);
 }
 
-static napi_value m_wake(napi_env env, napi_callback_info info) {
+/* wake (LIFWasm) and flush (LIFGpu): nothing to do, host writes apply before the next step */
+static napi_value m_nothing(napi_env env, napi_callback_info info) {
   (void)info;
   return undefined_value(env);
 }
@@ -330,14 +352,14 @@ static bool named(napi_env env, napi_value obj, const char *name, napi_value *ou
   return napi_get_named_property(env, obj, name, out) == napi_ok && !is_undefined(env, *out);
 }
 
-/* params: the DEFAULTS names (src/lif.js:6-15); coba as a boolean or a number. */
-static bool read_params(napi_env env, napi_value obj, fb_params *p) {
+/* params named as DEFAULTS names them (src/lif.js:6-15), merged over *p; coba as a boolean or a
+ * number. */
+static bool merge_params(napi_env env, napi_value obj, fb_params *p) {
   static const char *names[] = {"dt", "vRest", "vThresh", "vReset", "tauM", "tauSyn", "tRef", "delay", "traceTau",
                                 "adaptInc", "adaptTau", "depU", "depTau", "eExc", "eInh", "bgRate", "bgAmp", "preInh"};
   double *slot[] = {&p->dt, &p->vRest, &p->vThresh, &p->vReset, &p->tauM, &p->tauSyn, &p->tRef, &p->delay,
                     &p->traceTau, &p->adaptInc, &p->adaptTau, &p->depU, &p->depTau, &p->eExc, &p->eInh,
                     &p->bgRate, &p->bgAmp, &p->preInh};
-  fb_default_params(p);
   if (!obj) return true;
   for (size_t k = 0; k < sizeof(names) / sizeof(names[0]); k++) {
     napi_value v;
@@ -374,8 +396,9 @@ static napi_value ctor(napi_env env, napi_callback_info info) {
     return throw_msg(env, "LIFNative: sign must be a Float32Array of N");
   fb_params p;
   napi_value po = NULL;
+  fb_default_params(&p);
   named(env, o, "params", &po);
-  if (!read_params(env, po, &p)) return throw_msg(env, "LIFNative: params values must be numbers");
+  if (!merge_params(env, po, &p)) return throw_msg(env, "LIFNative: params values must be numbers");
   double seedv = 1;
   if (named(env, o, "seed", &v) && !get_f64(env, v, &seedv)) return throw_msg(env, "LIFNative: seed must be a number");
   if (!(seedv >= 0 && seedv < 4294967296.0) || seedv != (double)(uint32_t)seedv)
@@ -385,6 +408,7 @@ static napi_value ctor(napi_env env, napi_callback_info info) {
   Brain *b = (Brain *)calloc(1, sizeof(Brain));
   if (!b) return throw_msg(env, "LIFNative: out of host memory");
   b->N = N;
+  b->p = p;
   b->dt = p.dt;
   b->fired = (int32_t *)malloc((size_t)N * sizeof(int32_t));
   if (!b->fired || fb_graph_create(N, (int64_t)E, (const uint32_t *)ip, (const uint32_t *)ix, (const float *)w,
@@ -418,7 +442,10 @@ napi_value flybrain_napi_init(napi_env env, napi_value exports) {
       METHOD("pulse", m_pulse),
       METHOD("setBackground", m_set_background),
       METHOD("reset", m_reset),
-      METHOD("wake", m_wake),
+      METHOD("setParams", m_set_params),
+      METHOD("wake", m_nothing),
+      METHOD("flush", m_nothing),
+      METHOD("destroy", m_dispose),
       METHOD("dispose", m_dispose),
       FIELD("v", FB_FIELD_V),
       FIELD("gE", FB_FIELD_GE),

@@ -121,7 +121,16 @@ static int marshal(void) {
   show("t", rt_prop(b, "t"));
   show("v", rt_prop(b, "v"));
   show("spikeCount", rt_prop(b, "spikeCount"));
+  napi_value q = rt_object();
+  rt_set(q, "tauM", rt_number(12));
+  rt_set(q, "coba", rt_bool(false));
+  show("setParams({tauM: 12, coba: false})", rt_call(b, "setParams", 1, &q));
+  rt_set(q, "dt", rt_number(0.5));
+  show("setParams({dt: 0.5, ...})", rt_call(b, "setParams", 1, &q));
+  a2[0] = rt_number(3);
+  show("setParams(3)", rt_call(b, "setParams", 1, a2));
   show("wake()", rt_call(b, "wake", 0, NULL));
+  show("flush()", rt_call(b, "flush", 0, NULL));
   show("reset()", rt_call(b, "reset", 0, NULL));
   show("t", rt_prop(b, "t"));
   const int32_t l9[1] = {9};
@@ -136,6 +145,7 @@ static int marshal(void) {
   a2[1] = rt_number(1);
   show("setBias(Float32Array [1], 1)", rt_call(b, "setBias", 2, a2));
   show("run()", rt_call(b, "run", 0, NULL));
+  show("destroy()", rt_call(b, "destroy", 0, NULL));
   show("dispose()", rt_call(b, "dispose", 0, NULL));
   show("step()", rt_call(b, "step", 0, NULL));
   show("v", rt_prop(b, "v"));

@@ -115,6 +115,17 @@ int fb_set_background(fb_brains *br, int32_t b, double rate_hz, double amp_mv) {
   return FB_OK;
 }
 
+int fb_set_params(fb_brains *br, int32_t b, const fb_params *params) {
+  (void)br;
+  printf("set_params b=%d dt=%g vThresh=%g tauM=%g bgRate=%g bgAmp=%g coba=%d\n", b, params->dt, params->vThresh,
+         params->tauM, params->bgRate, params->bgAmp, params->coba);
+  if (params->dt != 0.1) {
+    snprintf(g_err, sizeof g_err, "fb_set_params: the ring depth would change");
+    return FB_EINVAL;
+  }
+  return FB_OK;
+}
+
 int fb_reset(fb_brains *br, int32_t b) {
   (void)br;
   printf("reset b=%d\n", b);

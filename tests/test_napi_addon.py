@@ -71,7 +71,13 @@ read field=0 b=0
 v -> Float32Array[4] 0 0.5 1 1.5
 read field=10 b=0
 spikeCount -> Uint32Array[4] 1000 1001 1002 1003
+set_params b=0 dt=0.1 vThresh=-40 tauM=12 bgRate=20 bgAmp=1.5 coba=0
+setParams({tauM: 12, coba: false}) -> undefined
+set_params b=0 dt=0.5 vThresh=-40 tauM=12 bgRate=20 bgAmp=1.5 coba=0
+setParams({dt: 0.5, ...}) -> throws: fb_set_params: the ring depth would change
+setParams(3) -> throws: LIFNative.setParams(q): an object of numbers
 wake() -> undefined
+flush() -> undefined
 reset b=0
 reset() -> undefined
 t -> 0
@@ -82,6 +88,7 @@ setBias(Float32Array [1], 1) -> throws: LIFNative.setBias(ix, mv): an index list
 run() -> throws: LIFNative.run(n): a step count >= 0
 brains_destroy
 graph_destroy
+destroy() -> undefined
 dispose() -> undefined
 step() -> throws: LIFNative.step: not a live brain
 v -> throws: LIFNative: not a live brain
@@ -94,8 +101,9 @@ def test_addon_marshalling_against_a_stand_in_library(tmp_path):
     typed arrays, arrays of numbers or one number, one value broadcast over the list, addG's
     missing increment as 0, params by name over the defaults, the seed as given), returns
     LIFWasm's results (the fired list as an Int32Array, state as Float32Array / Uint32Array, t in
-    ms), turns a failing call into a thrown Error with the library's message, and frees the brain
-    once (dispose, then collection)."""
+    ms), merges setParams over the parameters in force (LIFGpu's Object.assign) and keeps them when
+    the library refuses, turns a failing call into a thrown Error with the library's message, and
+    frees the brain once (destroy, dispose, then collection)."""
     exe = str(tmp_path / "driver")
     _compile(exe, [os.path.join(NAPI, "fake_flybrain.c")])
     r = subprocess.run([exe, "marshal"], capture_output=True, text=True, timeout=60)
